@@ -1,0 +1,210 @@
+"""ctypes wrapper of the oracle (oracle/_build/liborc.so) -- TEST INFRASTRUCTURE ONLY.
+
+Imported only by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+leg.  Grids use the reference's padded layout: real [z][y][2(N/2+1)] float32,
+half spectra [kz][ky][N/2+1] complex64.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liborc.so")
+NZ = 5001
+NU21 = 1420.40575177
+
+
+def build():
+    subprocess.run(["make", "-C", HERE, "all"], check=True, stdout=subprocess.DEVNULL)
+
+
+class Config(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("OmegaM", "OmegaL", "OmegaB", "hhub", "weos", "n_scal", "sig8",
+                                          "r_smooth", "nu_min", "nu_max", "l_box_override", "b_HI")] + [
+        ("n_side", C.c_long), ("n_grid", C.c_int), ("n_nu", C.c_int), ("seed", C.c_uint),
+        ("regular_nu", C.c_int), ("bias_const", C.c_int), ("do_rsd", C.c_int), ("pad_", C.c_int)]
+
+
+class Derived(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("fgrowth_0", "hubble_0", "z_min", "z_max", "r_min", "r_max",
+                                          "l_box")] + [("pos_obs", C.c_double * 3)] + [
+        (n, C.c_double) for n in ("r2_smooth", "glob_idr", "logkmin", "logkmax", "idlogk", "n_scal",
+                                  "sigma8_in", "pk_norm")] + [
+        ("do_smoothing", C.c_int), ("numk", C.c_int)] + [
+        (n, C.c_double * NZ) for n in ("z_z2r", "r_z2r", "z_r2z", "r_r2z", "gd", "gv")]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        P = C.POINTER
+        f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+        f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+        u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+        L.orc_cosmo_set.argtypes = [P(Config), C.c_int, f64p, f64p, f64p, f64p, P(Derived)]
+        L.orc_cosmo_set.restype = C.c_int
+        for fn in ("orc_z_of_r", "orc_r_of_z", "orc_dgrowth_of_r", "orc_vgrowth_of_r"):
+            getattr(L, fn).argtypes = [P(Derived), C.c_double]
+            getattr(L, fn).restype = C.c_double
+        L.orc_modes_mt.argtypes = [P(Config), P(Derived), f64p, f64p, C.c_int, f32p, C.c_void_p]
+        L.orc_modes_philox.argtypes = [P(Config), P(Derived), f64p, f64p, f32p]
+        L.orc_c2r_inplace.argtypes = [C.c_int, f32p]
+        L.orc_c2r_to_double.argtypes = [C.c_int, f32p, f64p]
+        L.orc_normalize.argtypes = [C.c_int, C.c_double, f32p]
+        L.orc_radial_velocity_fd.argtypes = [P(Config), P(Derived), f32p, f32p]
+        L.orc_sigma_dens.argtypes = [C.c_int, f32p, P(C.c_double), P(C.c_double)]
+        L.orc_get_hi.argtypes = [P(Config), P(Derived), C.c_double, f32p, f32p]
+        L.orc_subsample_offsets.argtypes = [C.c_uint, C.c_double, f64p, f64p, f64p]
+        L.orc_vec2pix_ring.argtypes = [C.c_long, f64p]
+        L.orc_vec2pix_ring.restype = C.c_long
+        L.orc_pix2ang_ring.argtypes = [C.c_long, C.c_long, P(C.c_double), P(C.c_double)]
+        L.orc_mk_T_maps.argtypes = [P(Config), P(Derived), f64p, f64p, f32p, f32p, f32p, C.c_void_p]
+        L.orc_channel_prefactors.argtypes = [P(Config), P(Derived), f64p, f64p, f64p]
+        L.orc_philox4x32_10.argtypes = [u32p, u32p, u32p]
+        L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_num_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+class Oracle:
+    """One GetHI configuration evaluated by the oracle, stage by stage."""
+
+    def __init__(self, cfg: dict, k, pk, nu0=None, nuf=None):
+        self.c = Config()
+        defaults = dict(OmegaM=0.3, OmegaL=0.7, OmegaB=0.05, hhub=0.7, weos=-1.0, n_scal=0.96, sig8=0.83,
+                        r_smooth=2.0, nu_min=350.0, nu_max=1050.0, l_box_override=-1.0, b_HI=1.0,
+                        n_side=128, n_grid=512, n_nu=150, seed=1234, regular_nu=0, bias_const=0, do_rsd=1)
+        defaults.update(cfg)
+        for kk, v in defaults.items():
+            setattr(self.c, kk, v)
+        if not self.c.regular_nu:
+            self.nu0 = np.ascontiguousarray(nu0, dtype=np.float64)
+            self.nuf = np.ascontiguousarray(nuf, dtype=np.float64)
+            self.c.n_nu = len(self.nu0)
+            self.c.nu_min = float(self.nu0[0])
+            self.c.nu_max = float(self.nuf[-1])
+        else:
+            self.nu0 = np.zeros(1)
+            self.nuf = np.zeros(1)
+        self.d = Derived()
+        k = np.ascontiguousarray(k, dtype=np.float64)
+        pk = np.ascontiguousarray(pk, dtype=np.float64)
+        self.logk = np.zeros_like(k)
+        self.pk = np.zeros_like(pk)
+        rc = lib().orc_cosmo_set(C.byref(self.c), len(k), k, pk, self.logk, self.pk, C.byref(self.d))
+        if rc != 0:
+            raise ValueError("orc_cosmo_set failed: %d" % rc)
+        self.n = self.c.n_grid
+
+    # ---- shapes
+    def spec_shape(self):
+        return (self.n, self.n, self.n // 2 + 1)
+
+    def real_pad_shape(self):
+        return (self.n, self.n, 2 * (self.n // 2 + 1))
+
+    # ---- stages
+    def modes_mt(self, nthreads=1, with_vpot=True):
+        dk = np.zeros(self.spec_shape(), np.complex64)
+        vk = np.zeros(self.spec_shape(), np.complex64) if with_vpot else None
+        lib().orc_modes_mt(C.byref(self.c), C.byref(self.d), self.logk, self.pk, nthreads,
+                           dk.view(np.float32), vk.view(np.float32).ctypes.data if with_vpot else None)
+        return dk, vk
+
+    def modes_philox(self):
+        dk = np.zeros(self.spec_shape(), np.complex64)
+        lib().orc_modes_philox(C.byref(self.c), C.byref(self.d), self.logk, self.pk, dk.view(np.float32))
+        return dk
+
+    def c2r(self, spec):
+        """In-place padded c2r of a half spectrum, float32 result (FFTW layout)."""
+        buf = np.ascontiguousarray(spec, np.complex64).copy()
+        flat = buf.view(np.float32).reshape(self.real_pad_shape())
+        lib().orc_c2r_inplace(self.n, flat.reshape(-1))
+        return flat
+
+    def c2r_double(self, spec):
+        out = np.zeros((self.n, self.n, self.n), np.float64)
+        lib().orc_c2r_to_double(self.n, np.ascontiguousarray(spec, np.complex64).view(np.float32).reshape(-1),
+                                out.reshape(-1))
+        return out
+
+    def normalize(self, grid):
+        lib().orc_normalize(self.n, self.d.l_box, grid.reshape(-1))
+        return grid
+
+    def radial_velocity_fd(self, vpot_real):
+        rv = np.zeros(self.real_pad_shape(), np.float32)
+        lib().orc_radial_velocity_fd(C.byref(self.c), C.byref(self.d),
+                                     np.ascontiguousarray(vpot_real, np.float32).reshape(-1), rv.reshape(-1))
+        return rv
+
+    def sigma(self, dens):
+        m, s = C.c_double(), C.c_double()
+        lib().orc_sigma_dens(self.n, np.ascontiguousarray(dens, np.float32).reshape(-1), C.byref(m), C.byref(s))
+        return m.value, s.value
+
+    def get_hi(self, dens, rvel, sigma2):
+        d = np.ascontiguousarray(dens, np.float32).copy()
+        r = np.ascontiguousarray(rvel, np.float32).copy()
+        lib().orc_get_hi(C.byref(self.c), C.byref(self.d), sigma2, d.reshape(-1), r.reshape(-1))
+        return d, r
+
+    def subsample_offsets(self):
+        xs, ys, zs = np.zeros(10), np.zeros(10), np.zeros(10)
+        lib().orc_subsample_offsets(self.c.seed, self.d.l_box / self.n, xs, ys, zs)
+        return xs, ys, zs
+
+    def mk_T_maps(self, mass, dz, want_keys=False):
+        npix = 12 * self.c.n_side ** 2
+        maps = np.zeros((self.c.n_nu, npix), np.float32)
+        keys = np.zeros(self.n ** 3 * 10, np.uint32) if want_keys else None
+        lib().orc_mk_T_maps(C.byref(self.c), C.byref(self.d), self.nu0, self.nuf,
+                            np.ascontiguousarray(mass, np.float32).reshape(-1),
+                            np.ascontiguousarray(dz, np.float32).reshape(-1), maps.reshape(-1),
+                            keys.ctypes.data if want_keys else None)
+        return (maps, keys) if want_keys else maps
+
+    def prefactors(self):
+        out = np.zeros(self.c.n_nu)
+        lib().orc_channel_prefactors(C.byref(self.c), C.byref(self.d), self.nu0, self.nuf, out)
+        return out
+
+    def tables(self):
+        d = self.d
+        return np.concatenate([np.ctypeslib.as_array(getattr(d, n)) for n in
+                               ("z_z2r", "r_z2r", "z_r2z", "r_r2z", "gd", "gv")])
+
+
+def vec2pix_ring(nside, v):
+    return lib().orc_vec2pix_ring(nside, np.ascontiguousarray(v, np.float64))
+
+
+def pix2ang_ring(nside, ipix):
+    th, ph = C.c_double(), C.c_double()
+    lib().orc_pix2ang_ring(nside, ipix, C.byref(th), C.byref(ph))
+    return th.value, ph.value
+
+
+def philox(ctr, key):
+    out = np.zeros(4, np.uint32)
+    lib().orc_philox4x32_10(np.asarray(ctr, np.uint32), np.asarray(key, np.uint32), out)
+    return out
+
+
+def set_threads(t):
+    lib().orc_set_threads(int(t))
+
+
+def load_pk(path):
+    a = np.loadtxt(path)
+    return a[:, 0], a[:, 1]

@@ -1,0 +1,192 @@
+/*
+ * Oracle (test infrastructure only): Fourier modes and the real-space stages
+ * of GetHI.  Restates src/fourier.c:24-76 (sigma), :234-305 (modes),
+ * :307-373 (radial velocity) and src/grid_tools.c:103-153 (get_HI), with the
+ * user model of src/user_defined.c:27-35.
+ */
+#include <complex.h>
+#include <math.h>
+#include <stdlib.h>
+#include "orc.h"
+
+static double fraction_HI(double z) { return 0.008 * pow(1 + z, 0.6); }            /* user_defined.c:27-30 */
+static double bias_HI_fit(double z) { return 0.904 + 0.135 * pow(1 + z, 1.696); } /* user_defined.c:32-35 */
+
+static double kval(int i, int n, double dk) { return (2 * i <= n) ? i * dk : -(n - i) * dk; } /* fourier.c:264-283 */
+
+/* libgomp's static schedule: thread t of T gets a contiguous block, the first
+ * (n % T) threads one iteration more. */
+static void static_block(int n, int T, int t, int *s, int *e)
+{
+  int q = n / T, r = n % T;
+  if (t < r) { q++; r = 0; }
+  *s = q * t + r;
+  *e = *s + q;
+}
+
+void orc_modes_mt(const orc_config *c, const orc_derived *d, const double *logk,
+                  const double *pk, int nthreads, float *dens_k, float *vpot_k)
+{
+  int n = c->n_grid, h = n / 2 + 1;
+  double dk = 2 * M_PI / d->l_box;
+  double idk3 = 1. / (dk * dk * dk);
+  double factor = d->fgrowth_0 * d->hubble_0;
+  if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int t = 0; t < nthreads; t++) {
+    int i0, i1;
+    static_block(n, nthreads, t, &i0, &i1);
+    orc_mt rng;
+    orc_mt_seed(&rng, c->seed + (unsigned int)t);
+    for (int ii = i0; ii < i1; ii++) {
+      double kz = kval(ii, n, dk);
+      for (int jj = 0; jj < n; jj++) {
+        double ky = kval(jj, n, dk);
+        for (int kk = 0; kk <= n / 2; kk++) {
+          double kx = kval(kk, n, dk);
+          long index = kk + (long)h * (jj + (long)n * ii);
+          double k_mod2 = kx * kx + ky * ky + kz * kz;
+          if (k_mod2 <= 0) {
+            dens_k[2 * index] = dens_k[2 * index + 1] = 0;
+            if (vpot_k) vpot_k[2 * index] = vpot_k[2 * index + 1] = 0;
+            continue;
+          }
+          double lgk = 0.5 * log10(k_mod2);
+          double sigma2 = orc_pk_linear0(d, logk, pk, lgk) * idk3;
+          if (d->do_smoothing) sigma2 *= exp(-d->r2_smooth * k_mod2);
+          /* rng_delta_gauss, common.c:154-164: phase first, then modulus */
+          double phase = 2 * M_PI * orc_mt_uniform(&rng);
+          double u = orc_mt_uniform(&rng);
+          double mod = sqrt(-sigma2 * log(1 - u));
+          float complex dkc = mod * cexp(I * phase);
+          dens_k[2 * index] = crealf(dkc);
+          dens_k[2 * index + 1] = cimagf(dkc);
+          if (vpot_k) {
+            float complex vk = dkc * factor / k_mod2;
+            vpot_k[2 * index] = crealf(vk);
+            vpot_k[2 * index + 1] = cimagf(vk);
+          }
+        }
+      }
+    }
+  }
+}
+
+/* Production modes: the same amplitude law with counter-based draws.
+ * ctr = (mode id lo, mode id hi, 0, 0), key = (seed, 0x4352494D); the phase
+ * uses out[0]/2^32 and the modulus w = (2^32 - out[1])/2^32 = 1 - u. */
+void orc_modes_philox(const orc_config *c, const orc_derived *d, const double *logk,
+                      const double *pk, float *dens_k)
+{
+  int n = c->n_grid, h = n / 2 + 1;
+  double dk = 2 * M_PI / d->l_box;
+  double idk3 = 1. / (dk * dk * dk);
+#pragma omp parallel for schedule(static)
+  for (int ii = 0; ii < n; ii++) {
+    double kz = kval(ii, n, dk);
+    for (int jj = 0; jj < n; jj++) {
+      double ky = kval(jj, n, dk);
+      for (int kk = 0; kk <= n / 2; kk++) {
+        double kx = kval(kk, n, dk);
+        long index = kk + (long)h * (jj + (long)n * ii);
+        double k_mod2 = kx * kx + ky * ky + kz * kz;
+        if (k_mod2 <= 0) { dens_k[2 * index] = dens_k[2 * index + 1] = 0; continue; }
+        double lgk = 0.5 * log10(k_mod2);
+        double sigma2 = orc_pk_linear0(d, logk, pk, lgk) * idk3;
+        if (d->do_smoothing) sigma2 *= exp(-d->r2_smooth * k_mod2);
+        uint32_t ctr[4] = {(uint32_t)index, (uint32_t)((uint64_t)index >> 32), 0, 0};
+        uint32_t key[2] = {c->seed, 0x4352494Du}, o[4];
+        orc_philox4x32_10(ctr, key, o);
+        double phase = 2 * M_PI * (o[0] * (1.0 / 4294967296.0));
+        double w = (4294967296.0 - (double)o[1]) * (1.0 / 4294967296.0);
+        double mod = sqrt(-sigma2 * log(w));
+        dens_k[2 * index] = (float)(mod * cos(phase));
+        dens_k[2 * index + 1] = (float)(mod * sin(phase));
+      }
+    }
+  }
+}
+
+void orc_radial_velocity_fd(const orc_config *c, const orc_derived *d, const float *vpot,
+                            float *rvel)
+{
+  int n = c->n_grid;
+  double dx = d->l_box / n, idx = 1. / dx;
+  long ngx = 2 * (n / 2 + 1);
+#pragma omp parallel for schedule(static)
+  for (int iz = 0; iz < n; iz++) {
+    long iz_hi = iz + 1, iz_lo = iz - 1, iz_0 = iz;
+    double z = dx * (iz + 0.5) - d->pos_obs[2];
+    if (iz == 0) iz_lo = n - 1;
+    if (iz == n - 1) iz_hi = 0;
+    iz_hi *= ngx * n; iz_lo *= ngx * n; iz_0 *= ngx * n;
+    for (int iy = 0; iy < n; iy++) {
+      long iy_hi = iy + 1, iy_lo = iy - 1, iy_0 = iy;
+      double y = dx * (iy + 0.5) - d->pos_obs[1];
+      if (iy == 0) iy_lo = n - 1;
+      if (iy == n - 1) iy_hi = 0;
+      iy_hi *= ngx; iy_lo *= ngx; iy_0 *= ngx;
+      for (int ix = 0; ix < n; ix++) {
+        long ix_hi = ix + 1, ix_lo = ix - 1, ix_0 = ix;
+        double x = dx * (ix + 0.5) - d->pos_obs[0];
+        double irr = 1. / sqrt(x * x + y * y + z * z);
+        if (ix == 0) ix_lo = n - 1;
+        if (ix == n - 1) ix_hi = 0;
+        double ur0 = x * irr, ur1 = y * irr, ur2 = z * irr;
+        /* float differences, as in fourier.c:359-366 */
+        float dvx = vpot[ix_hi + iy_0 + iz_0] - vpot[ix_lo + iy_0 + iz_0];
+        float dvy = vpot[ix_0 + iy_hi + iz_0] - vpot[ix_0 + iy_lo + iz_0];
+        float dvz = vpot[ix_0 + iy_0 + iz_hi] - vpot[ix_0 + iy_0 + iz_lo];
+        double v0 = 0.5 * idx * dvx, v1 = 0.5 * idx * dvy, v2 = 0.5 * idx * dvz;
+        rvel[ix_0 + iy_0 + iz_0] = v0 * ur0 + v1 * ur1 + v2 * ur2;
+      }
+    }
+  }
+}
+
+void orc_sigma_dens(int n, const float *dens, double *mean, double *sigma2)
+{
+  long ngx = 2 * (n / 2 + 1);
+  long ng_tot = (long)n * n * n;
+  double s2 = 0, m = 0;
+  for (int iz = 0; iz < n; iz++)
+    for (int iy = 0; iy < n; iy++)
+      for (int ix = 0; ix < n; ix++) {
+        float v = dens[ix + iy * ngx + iz * ngx * n];
+        s2 += v * v; /* float product, fourier.c:51 */
+        m += v;
+      }
+  *mean = m / ng_tot;
+  *sigma2 = s2 / ng_tot - (*mean) * (*mean);
+}
+
+void orc_get_hi(const orc_config *c, const orc_derived *d, double sigma2, float *dens, float *rvel)
+{
+  int n = c->n_grid;
+  double dx = d->l_box / n;
+  long ngx = 2 * (n / 2 + 1);
+  double mass_prefac = dx * dx * dx;
+#pragma omp parallel for schedule(static)
+  for (int iz = 0; iz < n; iz++) {
+    double z = dx * (iz + 0.5) - d->pos_obs[2];
+    long iz0 = iz * (ngx * n);
+    for (int iy = 0; iy < n; iy++) {
+      double y = dx * (iy + 0.5) - d->pos_obs[1];
+      long iy0 = iy * ngx;
+      for (int ix = 0; ix < n; ix++) {
+        long index = iz0 + iy0 + ix;
+        double x = dx * (ix + 0.5) - d->pos_obs[0];
+        double r = sqrt(x * x + y * y + z * z);
+        double redshift = orc_z_of_r(d, r);
+        double bias = c->bias_const ? c->b_HI : bias_HI_fit(redshift);
+        double gfd = orc_dgrowth_of_r(d, r) * bias;
+        double delta_gauss = dens[index];
+        double dz_rsd = c->do_rsd ? rvel[index] * orc_vgrowth_of_r(d, r) : 0;
+        double dens_LN = exp(gfd * (delta_gauss - 0.5 * gfd * sigma2));
+        double mass_HI = mass_prefac * fraction_HI(redshift) * dens_LN;
+        dens[index] = mass_HI;
+        rvel[index] = dz_rsd;
+      }
+    }
+  }
+}

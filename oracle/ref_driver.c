@@ -1,0 +1,76 @@
+/*
+ * Test-infrastructure driver: runs the reference's GetHI stages
+ * (src/main_gh.c:24-80 minus point sources and FITS output) and dumps every
+ * stage's buffers as raw files, so the fixture script can turn them into
+ * golden vectors.  Usage: gethi_ref <param.ini> <outdir>
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include "common_gh.h"
+
+extern float *shim_captured[8];
+extern int shim_ncaptured;
+
+static void dump(const char *dir, const char *name, const void *p, size_t bytes)
+{
+  char fn[1024];
+  snprintf(fn, sizeof(fn), "%s/%s", dir, name);
+  FILE *f = fopen(fn, "wb");
+  if (!f) { perror(fn); exit(2); }
+  fwrite(p, 1, bytes, f);
+  fclose(f);
+}
+
+int main(int argc, char **argv)
+{
+  if (argc != 3) { fprintf(stderr, "usage: %s param.ini outdir\n", argv[0]); return 1; }
+  mpi_init(&argc, &argv);
+  ParamGetHI *par = read_run_params(argv[1]);
+  const char *od = argv[2];
+  int n = par->n_grid;
+  size_t ngrid = (size_t)2 * (n / 2 + 1) * n * n;
+
+  char fn[1024];
+  snprintf(fn, sizeof(fn), "%s/params.txt", od);
+  FILE *f = fopen(fn, "w");
+  fprintf(f, "fgrowth_0 %.17g\nhubble_0 %.17g\nz_min %.17g\nz_max %.17g\nr_min %.17g\nr_max %.17g\n",
+          par->fgrowth_0, par->hubble_0, par->z_min, par->z_max, par->r_min, par->r_max);
+  fprintf(f, "l_box %.17g\npos_obs %.17g\nglob_idr %.17g\nr2_smooth %.17g\ndo_smoothing %d\n",
+          par->l_box, par->pos_obs[0], par->glob_idr, par->r2_smooth, par->do_smoothing);
+  fprintf(f, "numk %d\nlogkmin %.17g\nlogkmax %.17g\nidlogk %.17g\nn_nu %d\nnu_min %.17g\nnu_max %.17g\n",
+          par->numk, par->logkmin, par->logkmax, par->idlogk, par->n_nu, par->nu_min, par->nu_max);
+  fprintf(f, "n_grid %d\nn_side %ld\nseed %u\n", par->n_grid, par->n_side, par->seed_rng);
+  double tabs[6 * NZ];
+  memcpy(tabs + 0 * NZ, par->z_arr_z2r, sizeof(double) * NZ);
+  memcpy(tabs + 1 * NZ, par->r_arr_z2r, sizeof(double) * NZ);
+  memcpy(tabs + 2 * NZ, par->z_arr_r2z, sizeof(double) * NZ);
+  memcpy(tabs + 3 * NZ, par->r_arr_r2z, sizeof(double) * NZ);
+  memcpy(tabs + 4 * NZ, par->growth_d_arr, sizeof(double) * NZ);
+  memcpy(tabs + 5 * NZ, par->growth_v_arr, sizeof(double) * NZ);
+  dump(od, "tables.f64", tabs, sizeof(tabs));
+  dump(od, "logk.f64", par->logkarr, sizeof(double) * par->numk);
+  dump(od, "pk.f64", par->pkarr, sizeof(double) * par->numk);
+#ifdef _IRREGULAR_NUTABLE
+  dump(od, "nu0.f64", par->nu0_arr, sizeof(double) * par->n_nu);
+  dump(od, "nuf.f64", par->nuf_arr, sizeof(double) * par->n_nu);
+#endif
+
+  create_d_and_vr_fields(par);
+  fprintf(f, "sigma2_gauss %.17g\n", par->sigma2_gauss);
+  fclose(f);
+  size_t nspec = (size_t)n * n * (n / 2 + 1) * 2 * sizeof(float);
+  dump(od, "dens_k.f32", shim_captured[0], nspec);
+  dump(od, "vpot_k.f32", shim_captured[1], nspec);
+  dump(od, "dens_real.f32", par->grid_dens, ngrid * sizeof(float));
+  dump(od, "vpot_real.f32", par->grid_vpot, ngrid * sizeof(float));
+  dump(od, "rvel.f32", par->grid_rvel, ngrid * sizeof(float));
+
+  get_HI(par);
+  dump(od, "mass.f32", par->grid_dens, ngrid * sizeof(float));
+  dump(od, "dz.f32", par->grid_rvel, ngrid * sizeof(float));
+
+  mk_T_maps(par);
+  dump(od, "maps.f32", par->maps_HI, sizeof(float) * par->n_nu * 12 * par->n_side * par->n_side);
+  return 0;
+}
