@@ -1,0 +1,351 @@
+"""Throughput of the GB300 GetHI realisation path (one JSON line on rank 0).
+
+Workload (default): a 1024^3 realisation in a 4000 Mpc/h box with redshift-
+space distortions (spectral velocity, three c2r FFTs of i k_j/k^2 delta_k),
+Philox modes from an Eisenstein-Hu no-wiggle P(k), 150 frequency shells over
+z 0.3-2.0 and Nside=512 maps.  A step is one whole realisation: modes ->
+4 c2r FFTs -> sigma^2 -> fused lognormal/HI/RSD -> projection -> channel scaling.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config c2]
+
+`value` is voxels/s with everything resident in HBM; `e2e` is the same metric
+through the public C ABI with the per-realisation host inputs copied in from
+pinned memory and the maps copied back to pinned host memory every step.
+Under torchrun each rank runs an independent replica (its own seed) on its own
+GPU; there is no data-path collective.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+NU21 = 1420.40575177
+
+# Synthetic configurations (seeded; the P(k) is the built-in EH no-wiggle table).
+CONFIGS = {
+    "c0": dict(n_grid=128, l_box=1500.0, zmin=0.5, zmax=1.0, n_nu=30, n_side=64, seed=1001, do_rsd=0,
+               bias_model="const", b_HI=1.0, velocity_mode="spectral"),
+    "c1": dict(n_grid=512, l_box=2500.0, zmin=0.3, zmax=2.0, n_nu=150, n_side=256, seed=2001, do_rsd=1,
+               velocity_mode="spectral"),
+    "c2": dict(n_grid=1024, l_box=4000.0, zmin=0.3, zmax=2.0, n_nu=150, n_side=512, seed=3001, do_rsd=1,
+               velocity_mode="spectral"),
+    "c4": dict(n_grid=2048, l_box=6000.0, zmin=0.2, zmax=2.5, n_nu=256, n_side=1024, seed=5001, do_rsd=1,
+               velocity_mode="spectral"),
+}
+COSMO = dict(omega_M=0.315, omega_L=0.685, omega_B=0.049, h=0.67, w=-1.0, ns=0.96, sigma_8=0.83)
+
+
+def params_for(cfg, seed_offset=0):
+    import crime_gb300 as gh
+    c = dict(cfg)
+    zmin, zmax = c.pop("zmin"), c.pop("zmax")
+    c["seed"] = c["seed"] + seed_offset
+    return gh.make_params(pk_filename="EH", frequencies_filename="", nu_min=NU21 / (1 + zmax),
+                          nu_max=NU21 / (1 + zmin), **COSMO, **c)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def read_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (clocks and throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = max(smax, float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_bytes(cls, n, npix, n_nu):
+    """Minimum HBM bytes of one launch of a kernel class (FP32 data)."""
+    n3 = float(n) ** 3
+    return {
+        "zpass": 4 * n3,            # write the half spectrum: 8 B/mode, N^3/2 modes
+        "ypass": 8 * n3,            # read + write 8 B/mode
+        "xpass": 8 * n3,            # read 8 B/mode, write 4 B/cell
+        "xpass_vel": 32.0 / 3 * n3,  # read 8 B/mode, read (2 of 3 comps) + write v_r 4 B/cell
+        "project": 8 * n3 + 4.0 * npix * n_nu,  # read delta, v_r; write the maps once
+        "scale": 8.0 * npix * n_nu,
+    }.get(cls)
+
+
+def bench_ours(args):
+    import torch
+
+    import crime_gb300 as gh
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    cfg = CONFIGS[args.config]
+    n = cfg["n_grid"]
+    p = params_for(cfg, seed_offset=rank)
+    ctx = gh.GetHI(p, device=local)
+    stream = torch.cuda.Stream(device=local)
+    ctx.set_stream(stream.cuda_stream)
+    npix, n_nu = ctx.npix, ctx.n_nu
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+
+    def max_over_ranks(x):
+        if ws == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- device-resident throughput
+    for i in range(args.warmup):
+        ctx.set_seed(cfg["seed"] + rank + 1000 * (i + 1))
+        ctx.run_into(0)
+    barrier()
+    ctx.profile(True)
+    _, launches0 = ctx.kernel_times()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        start.record(stream)
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            ctx.set_seed(cfg["seed"] + rank + 7919 * i)
+            ctx.run_into(0)
+        end.record(stream)
+        barrier()
+        wall = time.perf_counter() - t0
+    ms = max_over_ranks(start.elapsed_time(end))
+    ktimes, launches1 = ctx.kernel_times()
+    ctx.profile(False)
+    fallbacks = ctx.fallback_count()
+
+    # ---- end to end through the C ABI: host inputs in, maps out (pinned)
+    maps_host = torch.empty((n_nu, npix), dtype=torch.float32, pin_memory=True)
+    h2d = ctx.upload_inputs()
+    ctx.run_into(maps_host.data_ptr())
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(args.steps):
+        ctx.set_seed(cfg["seed"] + rank + 104729 * (i + 1))
+        h2d = ctx.upload_inputs()
+        ctx.run_into(maps_host.data_ptr())
+    e1.record(stream)
+    barrier()
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1))
+    assert np.isfinite(maps_host.numpy()).all()
+
+    voxels = float(n) ** 3
+    value = voxels * args.steps * ws / (ms / 1e3)
+    e2e = voxels * args.steps * ws / (e2e_ms / 1e3)
+
+    # ---- roofline of the dominant kernel class
+    peak, peak_kind = read_peaks()
+    dom = max(((k, v) for k, v in ktimes.items() if v[1] > 0 and algorithmic_bytes(k, n, npix, n_nu)),
+              key=lambda kv: kv[1][0])
+    cls, (tot_ms, cnt) = dom
+    per_launch_ms = tot_ms / cnt
+    abytes = algorithmic_bytes(cls, n, npix, n_nu)
+    achieved = abytes / (per_launch_ms / 1e3) / 1e9
+    traffic = None
+    tf = os.path.join(REPO, "profiles", "traffic.json")
+    if os.path.exists(tf):
+        with open(tf) as f:
+            t = json.load(f)
+        if cls in t:
+            traffic = float(t[cls]["bytes_per_cell"]) * voxels if "bytes_per_cell" in t[cls] else None
+    roof = {"bound": "hbm", "kernel": cls, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
+            "algorithmic_bytes_per_launch": abytes, "avg_launch_ms": round(per_launch_ms, 4)}
+    kernels = {k: {"ms_per_step": round(v[0] / args.steps, 4), "launches_per_step": v[1] / args.steps}
+               for k, v in ktimes.items() if v[1] > 0}
+    for k in kernels:
+        b = algorithmic_bytes(k, n, npix, n_nu)
+        if b:
+            kernels[k]["GBps"] = round(b / (ktimes[k][0] / ktimes[k][1] / 1e3) / 1e9, 1)
+
+    line = {
+        "metric": "GetHI %d^3 realisation throughput (voxels/s), FP32 FFT path" % n,
+        "value": value, "unit": "voxels/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32", "data": "synthetic (Philox modes from an EH no-wiggle P(k))",
+        "realisations_per_s": args.steps * ws / (ms / 1e3),
+        "config": {"workload": "%s: %d^3 grid, box %g Mpc/h, RSD (spectral velocity), z %.1f-%.1f in %d shells, "
+                               "Nside=%d" % (args.config, n, cfg["l_box"], cfg["zmin"], cfg["zmax"], cfg["n_nu"],
+                                             cfg["n_side"]),
+                   "n_grid": n, "n_side": cfg["n_side"], "n_nu": cfg["n_nu"], "l_box": cfg["l_box"],
+                   "fft_precision": "fp32", "parallelism": "replicas" if ws > 1 else "single",
+                   "l2": "inputs larger than L2 (each field is %.1f GB)" % (4 * voxels / 1e9)},
+        "e2e": {"value": e2e, "unit": "voxels/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(4 * npix * n_nu)},
+        "gpu_launches": int((launches1 - launches0)),
+        "roofline": roof,
+        "kernels": kernels,
+        "fp64_fallback_samples_last_step": fallbacks,
+        "clocks": clk.summary(),
+        "wall_s": wall,
+        "filled_fraction": ctx.derived().filled_fraction,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.free()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_pipeline(cfg_name, n_sample):
+    """The oracle (C restatement of the reference, OpenMP on all host cores) on a
+    realisation of the workload's box, shells and Nside at n_sample^3 cells.
+    Returns seconds per stage."""
+    from oracle import orc
+    cfg = dict(CONFIGS[cfg_name])
+    k, pk = orc.load_pk(os.path.join(REPO, "tests", "golden", "pk_eh_nowiggle.txt"))
+    o = orc.Oracle(dict(OmegaM=COSMO["omega_M"], OmegaL=COSMO["omega_L"], OmegaB=COSMO["omega_B"],
+                        hhub=COSMO["h"], weos=-1.0, n_scal=COSMO["ns"], sig8=COSMO["sigma_8"], n_grid=n_sample,
+                        n_side=cfg["n_side"], seed=cfg["seed"], regular_nu=1, nu_min=NU21 / (1 + cfg["zmax"]),
+                        nu_max=NU21 / (1 + cfg["zmin"]), n_nu=cfg["n_nu"], l_box_override=cfg["l_box"],
+                        do_rsd=cfg["do_rsd"]), k, pk)
+    t = {}
+    t0 = time.perf_counter()
+    dk, _ = o.modes_mt(nthreads=orc.lib().orc_num_threads(), with_vpot=False)
+    t["modes"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    dens = o.normalize(o.c2r(dk))
+    t["fft_density"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    rv = o.radial_velocity_spectral(dk) if cfg["do_rsd"] else np.zeros_like(dens)
+    t["velocity_3fft"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    _, s2 = o.sigma(dens)
+    mass, dz = o.get_hi(dens, rv, s2)
+    t["sigma_get_hi"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    o.mk_T_maps(mass, dz)
+    t["mk_T_maps"] = time.perf_counter() - t0
+    return t
+
+
+def cpu_baseline(args):
+    from oracle import orc
+    orc.build()
+    n_sample = args.cpu_sample
+    t = cpu_pipeline(args.config, n_sample)
+    tot = sum(t.values())
+    return {"value": n_sample ** 3 / tot, "unit": "voxels/s", "cores": orc.lib().orc_num_threads(), "kind": "port",
+            "sample": "oracle pipeline (modes, 4 FP64 c2r FFTs, sigma, get_HI, mk_T_maps) at %d^3 with the "
+                      "workload's box, shells and Nside; %.1f s" % (n_sample, tot),
+            "stage_s": {k: round(v, 3) for k, v in t.items()}}
+
+
+def bench_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import orc
+    orc.build()
+    n_sample = args.cpu_sample
+    for _ in range(args.warmup):
+        cpu_pipeline(args.config, 32)
+    times = []
+    for _ in range(args.steps):
+        t = cpu_pipeline(args.config, n_sample)
+        times.append(sum(t.values()))
+    tot = sum(times)
+    value = n_sample ** 3 * args.steps / tot
+    cores = orc.lib().orc_num_threads()
+    cfg = CONFIGS[args.config]
+    line = {"impl": "reference", "metric": "GetHI %d^3 realisation throughput (voxels/s), FP32 FFT path"
+            % cfg["n_grid"], "value": value, "unit": "voxels/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp64 (FFT), fp32 grids", "data": "synthetic",
+            "config": {"workload": args.config, "sample_n_grid": n_sample},
+            "cpu_baseline": {"value": value, "unit": "voxels/s", "cores": cores, "kind": "port",
+                             "sample": "oracle pipeline at %d^3 per step with the workload's box, shells and "
+                                       "Nside (the reference does not build on this host without its libraries; "
+                                       "the oracle is its C restatement, pinned bit-exact against it)" % n_sample},
+            "e2e": {"value": value, "unit": "voxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
+    ap.add_argument("--cpu-sample", type=int, default=256)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        bench_reference(args)
+    else:
+        bench_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,69 @@
+"""Build the GB300 GetHI library in-tree: crime_gb300/lib/libgethi_gpu.so (+ the
+GetHI_gpu command-line driver).  sm_103a only; translation units compile in
+parallel.  Usage: python -m crime_gb300.build [--force]"""
+import concurrent.futures as cf
+import os
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(PKG, "csrc")
+OBJ = os.path.join(PKG, "_build")
+LIBDIR = os.path.join(PKG, "lib")
+LIB = os.path.join(LIBDIR, "libgethi_gpu.so")
+EXE = os.path.join(LIBDIR, "GetHI_gpu")
+NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+CU = ["fft.cu", "stages.cu", "api.cu"]
+CXX = ["host.cpp"]
+HDRS = ["common.cuh", "fft.h", "host.h", os.path.join("..", "..", "include", "gethi_gpu.h")]
+
+
+def _newer(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed:\n%s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    return r.stdout + r.stderr
+
+
+def build(force=False, verbose=False):
+    os.makedirs(OBJ, exist_ok=True)
+    os.makedirs(LIBDIR, exist_ok=True)
+    hdrs = [os.path.join(CSRC, h) for h in HDRS]
+    jobs = []
+    for f in CU:
+        src, obj = os.path.join(CSRC, f), os.path.join(OBJ, f + ".o")
+        if force or _newer(obj, [src] + hdrs):
+            jobs.append([NVCC, *ARCH, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
+                         "-Xptxas", "-v" if verbose else "-O3", "--expt-relaxed-constexpr", "-c", src, "-o", obj])
+    for f in CXX:
+        src, obj = os.path.join(CSRC, f), os.path.join(OBJ, f + ".o")
+        if force or _newer(obj, [src] + hdrs):
+            jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-I/usr/local/cuda/include",
+                         "-c", src, "-o", obj])
+    logs = []
+    with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+        for out in ex.map(_run, jobs):
+            logs.append(out)
+    objs = [os.path.join(OBJ, f + ".o") for f in CU + CXX]
+    if force or jobs or _newer(LIB, objs):
+        _run([NVCC, *ARCH, "-shared", "-cudart", "static", *objs, "-o", LIB])
+    drv = os.path.join(CSRC, "gethi_main.c")
+    if os.path.exists(drv) and (force or _newer(EXE, [drv, LIB])):
+        _run(["gcc", "-O2", "-Wall", drv, "-I" + os.path.join(os.path.dirname(PKG), "include"), "-L" + LIBDIR,
+              "-lgethi_gpu", "-Wl,-rpath,$ORIGIN", "-o", EXE])
+    if verbose:
+        print("\n".join(logs))
+    return LIB
+
+
+if __name__ == "__main__":
+    build(force="--force" in sys.argv, verbose="-v" in sys.argv)
+    print(LIB)

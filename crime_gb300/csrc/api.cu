@@ -1,0 +1,647 @@
+// C ABI of the GB300 GetHI path (include/gethi_gpu.h): context lifecycle,
+// device memory plan and the stage sequence of src/main_gh.c:34-74.
+//
+// Device memory per context (N = n_grid, m = N/2):
+//   main  N^3 floats  : delta_k (split half spectrum) -> delta(x) -> HI mass
+//   nyq   N^2 complex : kx = N/2 plane of delta_k
+//   vmain N^3 floats  : velocity potential or one velocity component (scratch)
+//   vnyq  N^2 complex
+//   vr    N^3 floats  : radial velocity -> dz_rsd
+//   maps  n_nu 12 nside^2 floats
+//   plus FP64/FP32 tables, twiddles, per-block partial sums.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/gethi_gpu.h"
+#include "common.cuh"
+#include "fft.h"
+#include "host.h"
+
+using namespace gethi;
+
+struct gethi_ctx {
+  Setup s;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  float2 *main = nullptr, *nyq = nullptr, *vmain = nullptr, *vnyq = nullptr, *modes = nullptr;
+  float *vr = nullptr, *maps = nullptr;
+  float2 *twN = nullptr, *twM = nullptr;
+  double2 *partials = nullptr;
+  double *stats = nullptr;
+  float *pk_f = nullptr, *logk_f = nullptr, *tab_f = nullptr, *prefac = nullptr, *edges_f = nullptr;
+  double *tab_d = nullptr, *edges_d = nullptr;
+  int *counters = nullptr;
+  long npartials = 0;
+  DevCfg cfg;
+  int stage = 0;  // 0: init, 1: fields (delta, v_r), 2: mass and dz
+  cudaEvent_t ev[8] = {};
+  float times[7] = {};
+  int nev = 0;
+  // per-kernel-class device time (profiling on): events around each launch
+  int prof = 0;
+  cudaEvent_t kev[2 * 64] = {};
+  int kcls[64] = {};
+  int nk = 0;
+  double ktime[GETHI_NKCLASS] = {};
+  long kcount[GETHI_NKCLASS] = {};
+  long launches = 0;
+  void *staging = nullptr;  // pinned host copy of the per-realisation inputs
+};
+
+namespace {
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return GETHI_E_CUDA;
+}
+
+#define CK(call)                                           \
+  do {                                                     \
+    cudaError_t e_ = (call);                               \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call);    \
+  } while (0)
+
+template <class T>
+int dalloc(T **p, size_t count)
+{
+  cudaError_t e = cudaMalloc((void **)p, count * sizeof(T) + 256);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    set_error(std::string("cudaMalloc of ") + std::to_string(count * sizeof(T)) + " bytes: " + cudaGetErrorString(e));
+    return GETHI_E_NOMEM;
+  }
+  return GETHI_OK;
+}
+
+void twiddles(std::vector<float2> &t, int L)
+{
+  t.resize(L);
+  for (int k = 0; k < L; k++) {
+    double a = 2 * M_PI * (double)k / L;
+    t[k] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
+}
+
+void fill_cfg(gethi_ctx *c)
+{
+  const Setup &s = c->s;
+  DevCfg &g = c->cfg;
+  std::memset(&g, 0, sizeof(g));
+  g.n = s.p.n_grid;
+  g.m = s.p.n_grid / 2;
+  g.l_box = s.d.l_box;
+  g.dx = s.d.l_box / s.p.n_grid;  // src/pixelize.c:328
+  g.pos_obs = s.d.pos_obs;
+  g.dxf = (float)g.dx;
+  g.pos_obsf = (float)g.pos_obs;
+  g.logk_f = c->logk_f;
+  g.pk_f = c->pk_f;
+  g.numk = s.d.numk;
+  g.logkmin = (float)s.d.logkmin;
+  g.logkmax = (float)s.d.logkmax;
+  g.idlogk = (float)s.d.idlogk;
+  g.n_scal = (float)s.n_scal;
+  double dk = 2 * M_PI / s.d.l_box;
+  g.dk = (float)dk;
+  g.idk3 = (float)(1. / (dk * dk * dk));
+  g.r2_smooth = (float)s.d.r2_smooth;
+  g.do_smoothing = s.d.do_smoothing;
+  g.norm = (float)std::pow(std::sqrt(2 * M_PI) / s.d.l_box, 3);
+  g.vfac = (float)(s.d.fgrowth_0 * s.d.hubble_0);
+  g.seed = s.p.seed;
+  g.z_r2z = c->tab_d;
+  g.r_r2z = c->tab_d + NZ;
+  g.gd = c->tab_d + 2 * NZ;
+  g.gv = c->tab_d + 3 * NZ;
+  g.z_r2z_f = c->tab_f;
+  g.gd_f = c->tab_f + NZ;
+  g.gv_f = c->tab_f + 2 * NZ;
+  g.glob_idr = s.d.glob_idr;
+  g.glob_idr_f = (float)s.d.glob_idr;
+  g.r_tab_max = s.r_r2z[NZ - 1];
+  g.r_tab_max_f = (float)g.r_tab_max;
+  g.n_nu = s.p.n_nu;
+  g.regular_nu = s.d.regular_nu;
+  g.nside = s.p.n_side;
+  g.npix = 12 * s.p.n_side * s.p.n_side;
+  g.nu_min = s.p.nu_min;
+  g.nu_max = s.p.nu_max;
+  g.inv_dnu = s.p.n_nu / (s.p.nu_max - s.p.nu_min);  // src/pixelize.c:330
+  g.nu_edges = c->edges_d;
+  g.nu_edges_f = c->edges_f;
+  g.prefac = c->prefac;
+  for (int i = 0; i < NSUB; i++) {
+    g.xs[i] = s.xs[i];
+    g.ys[i] = s.ys[i];
+    g.zs[i] = s.zs[i];
+  }
+  g.bias_const = s.p.bias_model;
+  g.b_HI = (float)s.p.b_HI;
+  g.do_rsd = s.p.do_rsd;
+  g.mass_prefac = (float)(g.dx * g.dx * g.dx);  // src/grid_tools.c:122
+}
+
+ColGeom geom(float2 *base, long cpp, long pstride, long cstride, long estride, long ncols)
+{
+  ColGeom g;
+  g.base = base;
+  g.cpp = cpp;
+  g.pstride = pstride;
+  g.cstride = cstride;
+  g.estride = estride;
+  g.ncols = ncols;
+  return g;
+}
+
+void record(gethi_ctx *c)
+{
+  if (c->nev < 8) cudaEventRecord(c->ev[c->nev++], c->stream);
+}
+
+// bracket one kernel launch of class `cls` (KC_*) with events when profiling
+struct KTimer {
+  gethi_ctx *c;
+  int slot = -1;
+  KTimer(gethi_ctx *c_, int cls) : c(c_)
+  {
+    c->launches++;
+    if (c->prof && c->nk < 64) {
+      slot = c->nk++;
+      c->kcls[slot] = cls;
+      cudaEventRecord(c->kev[2 * slot], c->stream);
+    }
+  }
+  ~KTimer()
+  {
+    if (slot >= 0) cudaEventRecord(c->kev[2 * slot + 1], c->stream);
+  }
+};
+
+void collect_kernel_times(gethi_ctx *c)
+{
+  for (int i = 0; i < c->nk; i++) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, c->kev[2 * i], c->kev[2 * i + 1]) == cudaSuccess) {
+      c->ktime[c->kcls[i]] += ms;
+      c->kcount[c->kcls[i]]++;
+    }
+  }
+  c->nk = 0;
+}
+
+// One field: Z pass (modes generated on the fly), Y pass, X pass with epilogue.
+int field_fft(gethi_ctx *c, float2 *main, float2 *nyq, int kind, const float2 *src, int epi, int comp, int first)
+{
+  const DevCfg &g = c->cfg;
+  const long n = g.n, m = g.m;
+  cudaStream_t st = c->stream;
+  {
+    KTimer t(c, KC_ZPASS);
+    CK(col_pass(g, geom(main, n * m, 0, 1, n * m, n * m), 0, true, kind, src, c->twN, st));
+  }
+  {
+    KTimer t(c, KC_NYQ);
+    CK(col_pass(g, geom(nyq, n, 0, 1, n, n), 1, true, kind, src, c->twN, st));
+  }
+  {
+    KTimer t(c, KC_YPASS);
+    CK(col_pass(g, geom(main, m, n * m, 1, m, n * m), 0, false, kind, nullptr, c->twN, st));
+  }
+  {
+    KTimer t(c, KC_NYQ);
+    CK(col_pass(g, geom(nyq, n, 0, n, 1, n), 1, false, kind, nullptr, c->twN, st));
+  }
+  {
+    KTimer t(c, epi ? KC_XPASS_VEL : KC_XPASS);
+    CK(row_pass(g, main, nyq, c->twN, c->twM, g.norm, epi, c->vr, comp, first, c->partials, st));
+  }
+  return GETHI_OK;
+}
+
+}  // namespace
+
+extern "C" int gethi_gpu_init(const gethi_params *p, int device, gethi_ctx **out)
+{
+  if (!p || !out) return GETHI_E_ARG;
+  *out = nullptr;
+  if (!fft_supported(p->n_grid)) {
+    set_error("n_grid " + std::to_string(p->n_grid) + " not supported (16,24,32,64,128,256,384,512,1024,2048)");
+    return GETHI_E_ARG;
+  }
+  gethi_ctx *c = new gethi_ctx();
+  std::string err;
+  int rc = setup_build(*p, c->s, err);
+  if (rc) {
+    set_error(err);
+    delete c;
+    return rc;
+  }
+  c->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) {
+    delete c;
+    return cuda_fail(e, "cudaSetDevice");
+  }
+  const Setup &s = c->s;
+  const long n = s.p.n_grid, m = n / 2;
+  const size_t ncell = (size_t)n * n * n;
+  const long npix = 12 * s.p.n_side * s.p.n_side;
+  c->npartials = row_pass_blocks((int)n);
+  if ((rc = dalloc(&c->main, ncell / 2)) || (rc = dalloc(&c->nyq, (size_t)n * n)) ||
+      (rc = dalloc(&c->vmain, ncell / 2)) || (rc = dalloc(&c->vnyq, (size_t)n * n)) ||
+      (rc = dalloc(&c->vr, ncell)) || (rc = dalloc(&c->maps, (size_t)npix * s.p.n_nu)) ||
+      (rc = dalloc(&c->twN, (size_t)n)) || (rc = dalloc(&c->twM, (size_t)m)) ||
+      (rc = dalloc(&c->partials, (size_t)c->npartials)) || (rc = dalloc(&c->stats, 4)) ||
+      (rc = dalloc(&c->pk_f, (size_t)s.d.numk)) || (rc = dalloc(&c->logk_f, (size_t)s.d.numk)) ||
+      (rc = dalloc(&c->tab_f, (size_t)3 * NZ)) || (rc = dalloc(&c->tab_d, (size_t)4 * NZ)) ||
+      (rc = dalloc(&c->prefac, (size_t)s.p.n_nu)) || (rc = dalloc(&c->edges_f, (size_t)s.p.n_nu + 1)) ||
+      (rc = dalloc(&c->edges_d, (size_t)s.p.n_nu + 1)) || (rc = dalloc(&c->counters, 16))) {
+    gethi_gpu_free(c);
+    return rc;
+  }
+  // tables
+  std::vector<float2> t;
+  twiddles(t, (int)n);
+  cudaMemcpy(c->twN, t.data(), sizeof(float2) * n, cudaMemcpyHostToDevice);
+  twiddles(t, (int)m);
+  cudaMemcpy(c->twM, t.data(), sizeof(float2) * m, cudaMemcpyHostToDevice);
+  std::vector<float> f(s.d.numk);
+  for (int i = 0; i < s.d.numk; i++) f[i] = (float)s.pk[i];
+  cudaMemcpy(c->pk_f, f.data(), sizeof(float) * s.d.numk, cudaMemcpyHostToDevice);
+  for (int i = 0; i < s.d.numk; i++) f[i] = (float)s.logk[i];
+  cudaMemcpy(c->logk_f, f.data(), sizeof(float) * s.d.numk, cudaMemcpyHostToDevice);
+  std::vector<double> td(4 * NZ);
+  std::vector<float> tf(3 * NZ);
+  for (int i = 0; i < NZ; i++) {
+    td[i] = s.z_r2z[i];
+    td[NZ + i] = s.r_r2z[i];
+    td[2 * NZ + i] = s.gd[i];
+    td[3 * NZ + i] = s.gv[i];
+    tf[i] = (float)s.z_r2z[i];
+    tf[NZ + i] = (float)s.gd[i];
+    tf[2 * NZ + i] = (float)s.gv[i];
+  }
+  cudaMemcpy(c->tab_d, td.data(), sizeof(double) * 4 * NZ, cudaMemcpyHostToDevice);
+  cudaMemcpy(c->tab_f, tf.data(), sizeof(float) * 3 * NZ, cudaMemcpyHostToDevice);
+  std::vector<double> ed(s.p.n_nu + 1);
+  std::vector<float> ef(s.p.n_nu + 1), pf(s.p.n_nu);
+  for (int i = 0; i < s.p.n_nu; i++) {
+    ed[i] = s.nu0[i];
+    pf[i] = (float)s.prefac[i];
+  }
+  ed[s.p.n_nu] = s.nuf[s.p.n_nu - 1];
+  for (int i = 0; i <= s.p.n_nu; i++) ef[i] = (float)ed[i];
+  cudaMemcpy(c->edges_d, ed.data(), sizeof(double) * (s.p.n_nu + 1), cudaMemcpyHostToDevice);
+  cudaMemcpy(c->edges_f, ef.data(), sizeof(float) * (s.p.n_nu + 1), cudaMemcpyHostToDevice);
+  cudaMemcpy(c->prefac, pf.data(), sizeof(float) * s.p.n_nu, cudaMemcpyHostToDevice);
+  if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+    gethi_gpu_free(c);
+    return cuda_fail(e, "cudaStreamCreate");
+  }
+  c->own_stream = true;
+  for (int i = 0; i < 8; i++) cudaEventCreate(&c->ev[i]);
+  for (int i = 0; i < 128; i++) cudaEventCreate(&c->kev[i]);
+  fill_cfg(c);
+  if ((e = cudaGetLastError()) != cudaSuccess) {
+    gethi_gpu_free(c);
+    return cuda_fail(e, "gethi_gpu_init");
+  }
+  *out = c;
+  return GETHI_OK;
+}
+
+extern "C" void gethi_gpu_free(gethi_ctx *c)
+{
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  void *bufs[] = {c->main, c->nyq, c->vmain, c->vnyq, c->modes, c->vr, c->maps, c->twN, c->twM, c->partials,
+                  c->stats, c->pk_f, c->logk_f, c->tab_f, c->tab_d, c->prefac, c->edges_f, c->edges_d, c->counters};
+  for (void *b : bufs)
+    if (b) cudaFree(b);
+  for (auto &ev : c->ev)
+    if (ev) cudaEventDestroy(ev);
+  for (auto &ev : c->kev)
+    if (ev) cudaEventDestroy(ev);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  if (c->staging) cudaFreeHost(c->staging);
+  delete c;
+}
+
+extern "C" int gethi_gpu_set_stream(gethi_ctx *c, void *stream)
+{
+  if (!c) return GETHI_E_ARG;
+  if (c->own_stream && c->stream) {
+    cudaStreamSynchronize(c->stream);
+    cudaStreamDestroy(c->stream);
+  }
+  if (stream) {
+    c->stream = (cudaStream_t)stream;
+    c->own_stream = false;
+  } else {
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    c->own_stream = true;
+  }
+  return GETHI_OK;
+}
+
+extern "C" int gethi_gpu_get_derived(const gethi_ctx *c, gethi_derived *out)
+{
+  if (!c || !out) return GETHI_E_ARG;
+  *out = c->s.d;
+  if (c->stage >= 1) {
+    double st[2];
+    if (cudaMemcpy(st, c->stats, sizeof(st), cudaMemcpyDeviceToHost) == cudaSuccess) {
+      out->mean_gauss = st[0];
+      out->sigma2_gauss = st[1];
+    }
+  }
+  return GETHI_OK;
+}
+
+extern "C" int gethi_gpu_make_fields(gethi_ctx *c, const float *modes_k)
+{
+  if (!c) return GETHI_E_ARG;
+  CK(cudaSetDevice(c->device));
+  const Setup &s = c->s;
+  const long n = s.p.n_grid, h = n / 2 + 1;
+  const float2 *src = nullptr;
+  std::vector<float> host_modes;
+  if (!modes_k && s.p.rng == 1) {  // mt_validation: the reference's own draws, made on the host
+    host_modes.resize((size_t)2 * n * n * h);
+    modes_mt(s, s.p.omp_threads_for_modes, host_modes.data());
+    modes_k = host_modes.data();
+  }
+  if (modes_k) {
+    if (!c->modes) {
+      int rc = dalloc(&c->modes, (size_t)n * n * h);
+      if (rc) return rc;
+    }
+    CK(cudaMemcpyAsync(c->modes, modes_k, sizeof(float2) * n * n * h, cudaMemcpyHostToDevice, c->stream));
+    src = c->modes;
+  }
+  c->nev = 0;
+  record(c);
+  int rc = field_fft(c, c->main, c->nyq, FIELD_DENS, src, 0, 0, 0);
+  if (rc) return rc;
+  {
+    KTimer t(c, KC_SIGMA);
+    CK(finish_sigma(c->partials, (int)c->npartials, (double)n * n * n, c->stats, c->stream));
+  }
+  record(c);
+  if (s.p.do_rsd) {
+    if (s.p.velocity_mode == 1) {
+      for (int comp = 0; comp < 3; comp++)
+        if ((rc = field_fft(c, c->vmain, c->vnyq, FIELD_VX + comp, src, 1, comp, comp == 0))) return rc;
+    } else {
+      if ((rc = field_fft(c, c->vmain, c->vnyq, FIELD_VPOT, src, 0, 0, 0))) return rc;
+      KTimer t(c, KC_FDVEL);
+      CK(radial_velocity_fd(c->cfg, reinterpret_cast<const float *>(c->vmain), c->vr, c->stream));
+    }
+  } else {
+    CK(cudaMemsetAsync(c->vr, 0, sizeof(float) * n * n * n, c->stream));
+  }
+  record(c);
+  c->stage = 1;
+  return GETHI_OK;
+}
+
+extern "C" int gethi_gpu_get_hi(gethi_ctx *c)
+{
+  if (!c) return GETHI_E_ARG;
+  if (c->stage != 1) {
+    set_error("get_hi needs the fields of gethi_gpu_make_fields");
+    return GETHI_E_STATE;
+  }
+  CK(cudaSetDevice(c->device));
+  {
+    KTimer t(c, KC_GETHI);
+    CK(get_hi(c->cfg, c->stats, reinterpret_cast<float *>(c->main), c->vr, c->stream));
+  }
+  c->stage = 2;
+  return GETHI_OK;
+}
+
+static int maps_common(gethi_ctx *c, float *maps_out, int fused)
+{
+  const Setup &s = c->s;
+  const long npix = 12 * s.p.n_side * s.p.n_side;
+  CK(cudaMemsetAsync(c->maps, 0, sizeof(float) * npix * s.p.n_nu, c->stream));
+  CK(cudaMemsetAsync(c->counters, 0, sizeof(int) * 16, c->stream));
+  {
+    KTimer t(c, KC_PROJECT);
+    CK(project(c->cfg, c->stats, reinterpret_cast<const float *>(c->main), c->vr, fused, c->maps, c->counters,
+               c->stream));
+  }
+  {
+    KTimer t(c, KC_SCALE);
+    CK(scale_maps(c->cfg, c->maps, c->stream));
+  }
+  record(c);
+  if (maps_out) {
+    CK(cudaMemcpyAsync(maps_out, c->maps, sizeof(float) * npix * s.p.n_nu, cudaMemcpyDeviceToHost, c->stream));
+    record(c);
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  for (int i = 0; i + 1 < c->nev && i < 7; i++) cudaEventElapsedTime(&c->times[i], c->ev[i], c->ev[i + 1]);
+  collect_kernel_times(c);
+  return GETHI_OK;
+}
+
+extern "C" int gethi_gpu_make_maps(gethi_ctx *c, float *maps_out)
+{
+  if (!c) return GETHI_E_ARG;
+  if (c->stage != 2) {
+    set_error("make_maps needs the HI grids of gethi_gpu_get_hi");
+    return GETHI_E_STATE;
+  }
+  CK(cudaSetDevice(c->device));
+  if (c->nev == 0) record(c);
+  return maps_common(c, maps_out, 0);
+}
+
+extern "C" int gethi_gpu_run(gethi_ctx *c, float *maps_out)
+{
+  if (!c) return GETHI_E_ARG;
+  int rc = gethi_gpu_make_fields(c, nullptr);
+  if (rc) return rc;
+  rc = maps_common(c, maps_out, 1);
+  if (rc) return rc;
+  c->stage = 3;  // mass is not materialised by the fused path
+  if (c->s.p.write_maps && maps_out) return gethi_gpu_write_maps(c, maps_out);
+  return GETHI_OK;
+}
+
+extern "C" int gethi_gpu_write_maps(const gethi_ctx *c, const float *maps)
+{
+  if (!c || !maps) return GETHI_E_ARG;
+  const Setup &s = c->s;
+  const long npix = 12 * s.p.n_side * s.p.n_side;
+  for (int i = 0; i < s.p.n_nu; i++) {
+    char fn[600];
+    std::snprintf(fn, sizeof(fn), "%s_%03d.fits", s.p.prefix_out, i + 1);  // src/io_gh.c:75
+    if (write_fits_map(fn, maps + (size_t)i * npix, s.p.n_side)) {
+      set_error(std::string("cannot write ") + fn);
+      return GETHI_E_IO;
+    }
+  }
+  return GETHI_OK;
+}
+
+extern "C" int gethi_gpu_download_grids(const gethi_ctx *c, float *dens, float *rvel)
+{
+  if (!c) return GETHI_E_ARG;
+  const long n = c->s.p.n_grid;
+  CK(cudaStreamSynchronize(c->stream));
+  if (dens) CK(cudaMemcpy(dens, c->main, sizeof(float) * n * n * n, cudaMemcpyDeviceToHost));
+  if (rvel) CK(cudaMemcpy(rvel, c->vr, sizeof(float) * n * n * n, cudaMemcpyDeviceToHost));
+  return GETHI_OK;
+}
+
+extern "C" int gethi_gpu_upload_grids(gethi_ctx *c, const float *dens, const float *rvel, int stage)
+{
+  if (!c || stage < 1 || stage > 2) return GETHI_E_ARG;
+  const long n = c->s.p.n_grid;
+  CK(cudaStreamSynchronize(c->stream));
+  if (dens) CK(cudaMemcpy(c->main, dens, sizeof(float) * n * n * n, cudaMemcpyHostToDevice));
+  if (rvel) CK(cudaMemcpy(c->vr, rvel, sizeof(float) * n * n * n, cudaMemcpyHostToDevice));
+  c->stage = stage;
+  return GETHI_OK;
+}
+
+extern "C" int gethi_gpu_sample_keys(gethi_ctx *c, uint32_t *keys, int exact_fp64)
+{
+  if (!c || !keys) return GETHI_E_ARG;
+  const long n = c->s.p.n_grid;
+  uint32_t *dk = nullptr;
+  int rc = dalloc(&dk, (size_t)n * n * n * NSUB);
+  if (rc) return rc;
+  cudaError_t e = sample_keys(c->cfg, c->vr, dk, exact_fp64, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(keys, dk, sizeof(uint32_t) * n * n * n * NSUB, cudaMemcpyDeviceToHost);
+  cudaFree(dk);
+  if (e != cudaSuccess) return cuda_fail(e, "sample_keys");
+  return GETHI_OK;
+}
+
+extern "C" int gethi_gpu_download_modes(gethi_ctx *c, float *modes_k)
+{
+  if (!c || !modes_k) return GETHI_E_ARG;
+  const long n = c->s.p.n_grid, h = n / 2 + 1;
+  float2 *d = nullptr;
+  int rc = dalloc(&d, (size_t)n * n * h);
+  if (rc) return rc;
+  cudaError_t e = gen_modes(c->cfg, d, FIELD_DENS, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(modes_k, d, sizeof(float2) * n * n * h, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_fail(e, "download_modes");
+  return GETHI_OK;
+}
+
+extern "C" int gethi_gpu_stage_times(const gethi_ctx *c, float *ms, int n)
+{
+  if (!c || !ms) return GETHI_E_ARG;
+  int k = c->nev > 0 ? c->nev - 1 : 0;
+  for (int i = 0; i < n; i++) ms[i] = i < k ? c->times[i] : 0.f;
+  return k;
+}
+
+extern "C" int gethi_gpu_profile(gethi_ctx *c, int on)
+{
+  if (!c) return GETHI_E_ARG;
+  c->prof = on;
+  c->nk = 0;
+  for (int i = 0; i < GETHI_NKCLASS; i++) {
+    c->ktime[i] = 0;
+    c->kcount[i] = 0;
+  }
+  return GETHI_OK;
+}
+
+extern "C" int gethi_gpu_kernel_times(const gethi_ctx *c, double *ms, long *count, long *launches)
+{
+  if (!c) return GETHI_E_ARG;
+  for (int i = 0; i < GETHI_NKCLASS; i++) {
+    if (ms) ms[i] = c->ktime[i];
+    if (count) count[i] = c->kcount[i];
+  }
+  if (launches) *launches = c->launches;
+  return GETHI_NKCLASS;
+}
+
+extern "C" int gethi_gpu_fallback_count(const gethi_ctx *c, long *n)
+{
+  if (!c || !n) return GETHI_E_ARG;
+  int v = 0;
+  CK(cudaMemcpy(&v, c->counters, sizeof(int), cudaMemcpyDeviceToHost));
+  *n = v;
+  return GETHI_OK;
+}
+
+extern "C" int gethi_gpu_set_seed(gethi_ctx *c, unsigned int seed)
+{
+  if (!c) return GETHI_E_ARG;
+  c->s.p.seed = seed;
+  c->cfg.seed = seed;
+  return GETHI_OK;
+}
+
+// Host inputs of one realisation (P(k), distance/growth tables, shell edges,
+// channel factors) copied again from the host-side setup, through pinned
+// staging, on the context's stream.  Returns the number of bytes copied.
+extern "C" long gethi_gpu_upload_inputs(gethi_ctx *c)
+{
+  if (!c) return GETHI_E_ARG;
+  const Setup &s = c->s;
+  const int nk = s.d.numk, nn = s.p.n_nu;
+  size_t bytes = sizeof(float) * (2 * nk + 3 * NZ + nn + nn + 1) + sizeof(double) * (4 * NZ + nn + 1);
+  if (!c->staging) {
+    if (cudaHostAlloc(&c->staging, bytes, cudaHostAllocDefault) != cudaSuccess) {
+      c->staging = nullptr;
+      set_error("cudaHostAlloc of the input staging buffer failed");
+      return GETHI_E_NOMEM;
+    }
+    char *p = (char *)c->staging;
+    double *td = (double *)p;
+    for (int i = 0; i < NZ; i++) {
+      td[i] = s.z_r2z[i];
+      td[NZ + i] = s.r_r2z[i];
+      td[2 * NZ + i] = s.gd[i];
+      td[3 * NZ + i] = s.gv[i];
+    }
+    double *ed = td + 4 * NZ;
+    for (int i = 0; i < nn; i++) ed[i] = s.nu0[i];
+    ed[nn] = s.nuf[nn - 1];
+    float *f = (float *)(ed + nn + 1);
+    for (int i = 0; i < nk; i++) f[i] = (float)s.pk[i];
+    for (int i = 0; i < nk; i++) f[nk + i] = (float)s.logk[i];
+    float *tf = f + 2 * nk;
+    for (int i = 0; i < NZ; i++) {
+      tf[i] = (float)s.z_r2z[i];
+      tf[NZ + i] = (float)s.gd[i];
+      tf[2 * NZ + i] = (float)s.gv[i];
+    }
+    float *pf = tf + 3 * NZ;
+    for (int i = 0; i < nn; i++) pf[i] = (float)s.prefac[i];
+    float *ef = pf + nn;
+    for (int i = 0; i <= nn; i++) ef[i] = (float)ed[i];
+  }
+  cudaStream_t st = c->stream;
+  char *p = (char *)c->staging;
+  double *td = (double *)p, *ed = td + 4 * NZ;
+  float *f = (float *)(ed + nn + 1), *tf = f + 2 * nk, *pf = tf + 3 * NZ, *ef = pf + nn;
+  CK(cudaMemcpyAsync(c->tab_d, td, sizeof(double) * 4 * NZ, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->edges_d, ed, sizeof(double) * (nn + 1), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->pk_f, f, sizeof(float) * nk, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->logk_f, f + nk, sizeof(float) * nk, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->tab_f, tf, sizeof(float) * 3 * NZ, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->prefac, pf, sizeof(float) * nn, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->edges_f, ef, sizeof(float) * (nn + 1), cudaMemcpyHostToDevice, st));
+  return (long)bytes;
+}

@@ -1,0 +1,440 @@
+// 3D complex-to-real FFT of the GetHI fields on GB300, FP32.
+//
+// Replaces fftw_wrap (src/fourier.c:78-99, fftwf_plan_dft_c2r_3d, sign +1,
+// unnormalised) plus the normalisation loop (src/fourier.c:397-412), the
+// Gaussian variance (src/fourier.c:24-76) and, for velocity_mode=spectral,
+// the radial projection of the velocity.
+//
+// Layout in HBM ("split half spectrum"): for kx < N/2 the modes live in
+// main[kz][ky][kx] (row length m = N/2 complex, rows 16-byte aligned); the
+// kx = N/2 (Nyquist) plane lives in nyq[kz][ky].  The transform is three
+// passes, each one read and one write of the field:
+//   pass Z: inverse c2c along kz of every (ky,kx) column; in the first pass the
+//           modes are produced on the fly (Philox or an uploaded spectrum), so
+//           the spectrum is never read from HBM;
+//   pass Y: inverse c2c along ky;
+//   pass X: per (z,y) row the N-point c2r is an N/2-point complex FFT of
+//           Z[k] = (X_k + X*_{m-k}) + i e^{2 pi i k/N} (X_k - X*_{m-k}); the result
+//           (x[2j], x[2j+1]) overwrites the row in place, so the real field is a
+//           compact N^3 float grid with the same bytes as main.
+// Only Re X_0 and Re X_{N/2} enter the x c2r, i.e. the result is the real part
+// of the full inverse DFT of the Hermitian-extended spectrum (the reference
+// draws the kx=0 and kx=N/2 planes without Hermitian symmetry).
+#include <cstdio>
+
+#include "common.cuh"
+#include "fft.h"
+
+namespace gethi {
+
+// ---------------------------------------------------------------------------
+// Fourier modes
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float pk_lookup(const DevCfg &c, float lgk)  // src/cosmo.c:153-170
+{
+  int ik = (int)floorf((lgk - c.logkmin) * c.idlogk);
+  if (lgk - c.logkmin < 0) ik = -1;
+  if (ik < 0) return __ldg(&c.pk_f[0]) * exp10f(c.n_scal * (lgk - c.logkmin));
+  if (ik < c.numk - 1) {
+    float p0 = __ldg(&c.pk_f[ik]), p1 = __ldg(&c.pk_f[ik + 1]);
+    return p0 + (lgk - __ldg(&c.logk_f[ik])) * (p1 - p0) * c.idlogk;
+  }
+  return __ldg(&c.pk_f[c.numk - 1]) * exp10f(-3.f * (lgk - c.logkmax));
+}
+
+// Production draw: amplitude law of src/fourier.c:292-298 with Philox4x32-10.
+// ctr = (mode id lo, hi, 0, 0), key = (seed, 0x4352494D); phase from out.x,
+// modulus from w = 1 - out.y/2^32 (never 0).
+__device__ __forceinline__ float2 philox_mode(const DevCfg &c, int ii, int jj, int kk, float k2)
+{
+  float lgk = 0.5f * log10f(k2);
+  float sigma2 = pk_lookup(c, lgk) * c.idk3;
+  if (c.do_smoothing) sigma2 *= expf(-c.r2_smooth * k2);
+  uint64_t id = (uint64_t)kk + (uint64_t)(c.m + 1) * ((uint64_t)jj + (uint64_t)c.n * ii);
+  uint4 o = philox4x32_10(make_uint4((uint32_t)id, (uint32_t)(id >> 32), 0u, 0u), make_uint2(c.seed, 0x4352494Du));
+  float u = (float)o.x * 2.3283064365386963e-10f;
+  uint32_t mw = 0u - o.y;
+  float w = mw ? (float)mw * 2.3283064365386963e-10f : 1.0f;
+  float amp = sqrtf(-sigma2 * logf(w));
+  float s, co;
+  sincospif(2.f * u, &s, &co);
+  return make_float2(amp * co, amp * s);
+}
+
+// Mode (kz index ii, ky index jj, kx index kk) of field `kind`.
+// src != nullptr: delta_k from a host spectrum in the reference layout.
+__device__ __forceinline__ float2 mode_value(const DevCfg &c, int ii, int jj, int kk, int kind,
+                                             const float2 *__restrict__ src)
+{
+  const int n = c.n;
+  float kz = kval(ii, n, c.dk), ky = kval(jj, n, c.dk), kx = kval(kk, n, c.dk);
+  float k2 = kx * kx + ky * ky + kz * kz;
+  if (k2 <= 0.f) return make_float2(0.f, 0.f);
+  float2 d = src ? __ldg(&src[((size_t)ii * n + jj) * (size_t)(c.m + 1) + kk]) : philox_mode(c, ii, jj, kk, k2);
+  if (kind == FIELD_DENS) return d;
+  float f = c.vfac / k2;  // phi_k = delta_k f0 H0 / k^2, src/fourier.c:298
+  if (kind == FIELD_VPOT) return cscale(d, f);
+  // v_j = i k_j phi_k; the derivative of a Nyquist component is set to zero
+  float kj = kind == FIELD_VX ? (2 * kk == n ? 0.f : kx) : kind == FIELD_VY ? (2 * jj == n ? 0.f : ky) : (2 * ii == n ? 0.f : kz);
+  return cmul_i(cscale(d, f * kj));
+}
+
+// ---------------------------------------------------------------------------
+// column passes (Z and Y)
+// element (col, e) of a column set lives at base + (col/cpp) pstride + (col%cpp) cstride + e estride
+// ---------------------------------------------------------------------------
+template <int L, int P, int TX, class Rad, bool GEN>
+__global__ void __launch_bounds__(TX *(L / P)) col_pass_kernel(DevCfg c, ColGeom g, int nyq, int kind,
+                                                               const float2 *__restrict__ src,
+                                                               const float2 *__restrict__ tw)
+{
+  constexpr int T = L / P;
+  constexpr int R0 = radix_first(Rad{}), RL = radix_last(Rad{});
+  extern __shared__ float2 smem[];
+  const int tid = threadIdx.x, cl = tid % TX, t = tid / TX;
+  const long col = (long)blockIdx.x * TX + cl;
+  const bool active = col < g.ncols;
+  const long cb = (col / g.cpp) * g.pstride + (col % g.cpp) * g.cstride;
+  float2 v[P];
+#pragma unroll
+  for (int j = 0; j < P / R0; j++)
+#pragma unroll
+    for (int r = 0; r < R0; r++) {
+      const int e = t + T * j + (L / R0) * r;
+      float2 x = make_float2(0.f, 0.f);
+      if (active) {
+        if constexpr (GEN) {
+          int ky = nyq ? (int)col : (int)(col / c.m), kx = nyq ? c.m : (int)(col % c.m);
+          x = mode_value(c, e, ky, kx, kind, src);
+        } else {
+          x = g.base[cb + (long)e * g.estride];
+        }
+      }
+      v[j * R0 + r] = x;
+    }
+  stockham_run<L, P>(v, smem + cl, TX, t, tw, Rad{});
+  if (active) {
+#pragma unroll
+    for (int j = 0; j < P / RL; j++)
+#pragma unroll
+      for (int r = 0; r < RL; r++) {
+        const int e = t + T * j + (L / RL) * r;
+        g.base[cb + (long)e * g.estride] = v[j * RL + r];
+      }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// row pass (X): c2r of every (z,y) row, fused epilogues
+//   EPI 0: write the real row in place (x scale) and accumulate sum, sum of squares
+//   EPI 1: add (x scale) * (cell_j - obs_j)/r into the radial-velocity grid
+// ---------------------------------------------------------------------------
+template <int M, int P, int RW, class Rad, int EPI>
+__global__ void __launch_bounds__(RW *(M / P)) row_pass_kernel(DevCfg c, float2 *main, const float2 *__restrict__ nyq,
+                                                               long nrows, const float2 *__restrict__ twN,
+                                                               const float2 *__restrict__ twM, float scale,
+                                                               float *vr, int comp, int first,
+                                                               double2 *partials)
+{
+  constexpr int T = M / P;
+  constexpr int R0 = radix_first(Rad{}), RL = radix_last(Rad{});
+  extern __shared__ float2 smem[];
+  const int tid = threadIdx.x, rl = tid / T, t = tid % T;
+  const long row = (long)blockIdx.x * RW + rl;
+  const bool active = row < nrows;
+  float2 *srow = smem + rl * M;
+  float2 *grow = main + row * (long)M;
+  for (int i = t; i < M; i += T) srow[i] = active ? grow[i] : make_float2(0.f, 0.f);
+  __syncthreads();
+  const float2 xm = active ? nyq[row] : make_float2(0.f, 0.f);
+  float2 v[P];
+#pragma unroll
+  for (int j = 0; j < P / R0; j++)
+#pragma unroll
+    for (int r = 0; r < R0; r++) {
+      const int k = t + T * j + (M / R0) * r;
+      float2 a = srow[k], b = k == 0 ? xm : srow[M - k];
+      if (k == 0) {
+        a.y = 0.f;
+        b.y = 0.f;
+      }
+      float2 s = make_float2(a.x + b.x, a.y - b.y);  // a + conj(b)
+      float2 d = make_float2(a.x - b.x, a.y + b.y);  // a - conj(b)
+      v[j * R0 + r] = cadd(s, cmul_i(cmul(__ldg(&twN[k]), d)));
+    }
+  stockham_run<M, P>(v, srow, 1, t, twM, Rad{});
+
+  double s1 = 0, s2 = 0;
+  if (active) {
+    if constexpr (EPI == 0) {
+#pragma unroll
+      for (int j = 0; j < P / RL; j++)
+#pragma unroll
+        for (int r = 0; r < RL; r++) {
+          const int e = t + T * j + (M / RL) * r;
+          float2 x = cscale(v[j * RL + r], scale);
+          grow[e] = x;
+          s1 += (double)x.x + (double)x.y;
+          s2 += (double)(x.x * x.x) + (double)(x.y * x.y);  // float squares, src/fourier.c:51
+        }
+    } else {
+      const int iy = (int)(row % c.n), iz = (int)(row / c.n);
+      const float y = c.dxf * (iy + 0.5f) - c.pos_obsf, z = c.dxf * (iz + 0.5f) - c.pos_obsf;
+      float *vrow = vr + row * (long)c.n;
+#pragma unroll
+      for (int j = 0; j < P / RL; j++)
+#pragma unroll
+        for (int r = 0; r < RL; r++) {
+          const int e = t + T * j + (M / RL) * r;
+          float2 x = cscale(v[j * RL + r], scale);
+          float x0 = c.dxf * (2 * e + 0.5f) - c.pos_obsf, x1 = c.dxf * (2 * e + 1.5f) - c.pos_obsf;
+          float i0 = rsqrtf(x0 * x0 + y * y + z * z), i1 = rsqrtf(x1 * x1 + y * y + z * z);
+          float u0 = comp == 0 ? x0 * i0 : (comp == 1 ? y * i0 : z * i0);
+          float u1 = comp == 0 ? x1 * i1 : (comp == 1 ? y * i1 : z * i1);
+          float2 old = first ? make_float2(0.f, 0.f) : *reinterpret_cast<float2 *>(vrow + 2 * e);
+          *reinterpret_cast<float2 *>(vrow + 2 * e) = make_float2(old.x + x.x * u0, old.y + x.y * u1);
+        }
+    }
+  }
+  if constexpr (EPI == 0) {
+    // block reduction of the two sums -> partials[blockIdx.x]
+    __shared__ double red[2][32];
+    for (int o = 16; o > 0; o >>= 1) {
+      s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+      s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    const int w = tid >> 5, lane = tid & 31, nw = (RW * T + 31) >> 5;
+    __syncthreads();
+    if (lane == 0) {
+      red[0][w] = s1;
+      red[1][w] = s2;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      double a = 0, b = 0;
+      for (int i = 0; i < nw; i++) {
+        a += red[0][i];
+        b += red[1][i];
+      }
+      partials[blockIdx.x] = make_double2(a, b);
+    }
+  }
+}
+
+// Kahan-compensated FP64 sum of the per-block partials -> stats = (mean, sigma^2)
+__global__ void finish_sigma_kernel(const double2 *__restrict__ partials, int np, double ncells, double *stats)
+{
+  __shared__ double sh[4][256];
+  double a = 0, ca = 0, b = 0, cb = 0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) {
+    double2 p = partials[i];
+    double y = p.x - ca, t = a + y;
+    ca = (t - a) - y;
+    a = t;
+    y = p.y - cb;
+    t = b + y;
+    cb = (t - b) - y;
+    b = t;
+  }
+  sh[0][threadIdx.x] = a;
+  sh[1][threadIdx.x] = -ca;
+  sh[2][threadIdx.x] = b;
+  sh[3][threadIdx.x] = -cb;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double A = 0, CA = 0, B = 0, CB = 0;
+    for (int i = 0; i < (int)blockDim.x; i++) {
+      double y = sh[0][i] - CA, t = A + y;
+      CA = (t - A) - y;
+      A = t;
+      y = sh[1][i] - CA;
+      t = A + y;
+      CA = (t - A) - y;
+      A = t;
+      y = sh[2][i] - CB;
+      t = B + y;
+      CB = (t - B) - y;
+      B = t;
+      y = sh[3][i] - CB;
+      t = B + y;
+      CB = (t - B) - y;
+      B = t;
+    }
+    double mean = A / ncells;
+    stats[0] = mean;
+    stats[1] = B / ncells - mean * mean;  // src/fourier.c:74
+  }
+}
+
+// standalone mode generator (inspection): reference layout [kz][ky][N/2+1]
+__global__ void modes_kernel(DevCfg c, float2 *out, int kind)
+{
+  const long h = c.m + 1;
+  const long total = (long)c.n * c.n * h;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    int kk = (int)(i % h);
+    long rest = i / h;
+    int jj = (int)(rest % c.n), ii = (int)(rest / c.n);
+    out[i] = mode_value(c, ii, jj, kk, kind, nullptr);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// launch plumbing
+// ---------------------------------------------------------------------------
+template <int L>
+struct ColPlan;
+template <int M>
+struct RowPlan;
+// columns: L = N; P points per thread, TX columns per block
+template <> struct ColPlan<2048> { static constexpr int P = 32, TX = 4; using R = Radices<32, 8, 8>; };
+template <> struct ColPlan<1024> { static constexpr int P = 32, TX = 8; using R = Radices<32, 32>; };
+template <> struct ColPlan<512> { static constexpr int P = 32, TX = 16; using R = Radices<32, 16>; };
+template <> struct ColPlan<384> { static constexpr int P = 24, TX = 16; using R = Radices<8, 8, 6>; };
+template <> struct ColPlan<256> { static constexpr int P = 16, TX = 16; using R = Radices<16, 16>; };
+template <> struct ColPlan<128> { static constexpr int P = 16, TX = 16; using R = Radices<16, 8>; };
+template <> struct ColPlan<64> { static constexpr int P = 8, TX = 16; using R = Radices<8, 8>; };
+template <> struct ColPlan<32> { static constexpr int P = 8, TX = 16; using R = Radices<8, 4>; };
+template <> struct ColPlan<24> { static constexpr int P = 12, TX = 16; using R = Radices<12, 2>; };
+template <> struct ColPlan<16> { static constexpr int P = 4, TX = 16; using R = Radices<4, 4>; };
+// rows: M = N/2
+template <> struct RowPlan<1024> { static constexpr int P = 32, RW = 4; using R = Radices<32, 8, 4>; };
+template <> struct RowPlan<512> { static constexpr int P = 32, RW = 16; using R = Radices<32, 16>; };
+template <> struct RowPlan<256> { static constexpr int P = 16, RW = 16; using R = Radices<16, 16>; };
+template <> struct RowPlan<192> { static constexpr int P = 24, RW = 16; using R = Radices<8, 8, 3>; };
+template <> struct RowPlan<128> { static constexpr int P = 16, RW = 16; using R = Radices<16, 8>; };
+template <> struct RowPlan<64> { static constexpr int P = 8, RW = 32; using R = Radices<8, 8>; };
+template <> struct RowPlan<32> { static constexpr int P = 8, RW = 32; using R = Radices<8, 4>; };
+template <> struct RowPlan<16> { static constexpr int P = 4, RW = 32; using R = Radices<4, 4>; };
+template <> struct RowPlan<12> { static constexpr int P = 12, RW = 32; using R = Radices<12>; };
+template <> struct RowPlan<8> { static constexpr int P = 8, RW = 32; using R = Radices<8>; };
+
+template <int L, bool GEN>
+static cudaError_t launch_col(const DevCfg &c, const ColGeom &g, int nyq, int kind, const float2 *src,
+                              const float2 *tw, cudaStream_t st)
+{
+  using PL = ColPlan<L>;
+  constexpr int threads = PL::TX * (L / PL::P);
+  const size_t sm = sizeof(float2) * PL::TX * L;
+  auto kern = col_pass_kernel<L, PL::P, PL::TX, typename PL::R, GEN>;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    attr = true;
+  }
+  long blocks = (g.ncols + PL::TX - 1) / PL::TX;
+  kern<<<(unsigned)blocks, threads, sm, st>>>(c, g, nyq, kind, src, tw);
+  return cudaGetLastError();
+}
+
+template <int M, int EPI>
+static cudaError_t launch_row(const DevCfg &c, float2 *main, const float2 *nyq, long nrows, const float2 *twN,
+                              const float2 *twM, float scale, float *vr, int comp, int first, double2 *partials,
+                              cudaStream_t st)
+{
+  using PL = RowPlan<M>;
+  constexpr int threads = PL::RW * (M / PL::P);
+  const size_t sm = sizeof(float2) * PL::RW * M;
+  auto kern = row_pass_kernel<M, PL::P, PL::RW, typename PL::R, EPI>;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    attr = true;
+  }
+  long blocks = (nrows + PL::RW - 1) / PL::RW;
+  kern<<<(unsigned)blocks, threads, sm, st>>>(c, main, nyq, nrows, twN, twM, scale, vr, comp, first, partials);
+  return cudaGetLastError();
+}
+
+long row_pass_blocks(int n)
+{
+  long nrows = (long)n * n;
+  int rw = 0;
+  switch (n / 2) {
+    case 1024: rw = RowPlan<1024>::RW; break;
+    case 512: rw = RowPlan<512>::RW; break;
+    case 256: rw = RowPlan<256>::RW; break;
+    case 192: rw = RowPlan<192>::RW; break;
+    case 128: rw = RowPlan<128>::RW; break;
+    case 64: rw = RowPlan<64>::RW; break;
+    case 32: rw = RowPlan<32>::RW; break;
+    case 16: rw = RowPlan<16>::RW; break;
+    case 12: rw = RowPlan<12>::RW; break;
+    case 8: rw = RowPlan<8>::RW; break;
+    default: return -1;
+  }
+  return (nrows + rw - 1) / rw;
+}
+
+bool fft_supported(int n)
+{
+  switch (n) {
+    case 16: case 24: case 32: case 64: case 128: case 256: case 384: case 512: case 1024: case 2048: return true;
+    default: return false;
+  }
+}
+
+#define GETHI_COL_DISPATCH(GENV)                                                                    \
+  switch (c.n) {                                                                                    \
+    case 2048: return launch_col<2048, GENV>(c, g, nyq, kind, src, tw, st);                        \
+    case 1024: return launch_col<1024, GENV>(c, g, nyq, kind, src, tw, st);                        \
+    case 512: return launch_col<512, GENV>(c, g, nyq, kind, src, tw, st);                          \
+    case 384: return launch_col<384, GENV>(c, g, nyq, kind, src, tw, st);                          \
+    case 256: return launch_col<256, GENV>(c, g, nyq, kind, src, tw, st);                          \
+    case 128: return launch_col<128, GENV>(c, g, nyq, kind, src, tw, st);                          \
+    case 64: return launch_col<64, GENV>(c, g, nyq, kind, src, tw, st);                            \
+    case 32: return launch_col<32, GENV>(c, g, nyq, kind, src, tw, st);                            \
+    case 24: return launch_col<24, GENV>(c, g, nyq, kind, src, tw, st);                            \
+    case 16: return launch_col<16, GENV>(c, g, nyq, kind, src, tw, st);                            \
+    default: return cudaErrorInvalidValue;                                                          \
+  }
+
+cudaError_t col_pass(const DevCfg &c, const ColGeom &g, int nyq, bool gen, int kind, const float2 *src,
+                     const float2 *tw, cudaStream_t st)
+{
+  if (gen) {
+    GETHI_COL_DISPATCH(true)
+  } else {
+    GETHI_COL_DISPATCH(false)
+  }
+}
+
+#define GETHI_ROW_DISPATCH(EPIV)                                                                          \
+  switch (c.m) {                                                                                          \
+    case 1024: return launch_row<1024, EPIV>(c, main, nyq, nrows, twN, twM, scale, vr, comp, first, partials, st); \
+    case 512: return launch_row<512, EPIV>(c, main, nyq, nrows, twN, twM, scale, vr, comp, first, partials, st);   \
+    case 256: return launch_row<256, EPIV>(c, main, nyq, nrows, twN, twM, scale, vr, comp, first, partials, st);   \
+    case 192: return launch_row<192, EPIV>(c, main, nyq, nrows, twN, twM, scale, vr, comp, first, partials, st);   \
+    case 128: return launch_row<128, EPIV>(c, main, nyq, nrows, twN, twM, scale, vr, comp, first, partials, st);   \
+    case 64: return launch_row<64, EPIV>(c, main, nyq, nrows, twN, twM, scale, vr, comp, first, partials, st);     \
+    case 32: return launch_row<32, EPIV>(c, main, nyq, nrows, twN, twM, scale, vr, comp, first, partials, st);     \
+    case 16: return launch_row<16, EPIV>(c, main, nyq, nrows, twN, twM, scale, vr, comp, first, partials, st);     \
+    case 12: return launch_row<12, EPIV>(c, main, nyq, nrows, twN, twM, scale, vr, comp, first, partials, st);     \
+    case 8: return launch_row<8, EPIV>(c, main, nyq, nrows, twN, twM, scale, vr, comp, first, partials, st);       \
+    default: return cudaErrorInvalidValue;                                                                \
+  }
+
+cudaError_t row_pass(const DevCfg &c, float2 *main, const float2 *nyq, const float2 *twN, const float2 *twM,
+                     float scale, int epi, float *vr, int comp, int first, double2 *partials, cudaStream_t st)
+{
+  const long nrows = (long)c.n * c.n;
+  if (epi == 0) {
+    GETHI_ROW_DISPATCH(0)
+  } else {
+    GETHI_ROW_DISPATCH(1)
+  }
+}
+
+cudaError_t finish_sigma(const double2 *partials, int np, double ncells, double *stats, cudaStream_t st)
+{
+  finish_sigma_kernel<<<1, 256, 0, st>>>(partials, np, ncells, stats);
+  return cudaGetLastError();
+}
+
+cudaError_t gen_modes(const DevCfg &c, float2 *out, int kind, cudaStream_t st)
+{
+  modes_kernel<<<1024, 256, 0, st>>>(c, out, kind);
+  return cudaGetLastError();
+}
+
+}  // namespace gethi

@@ -1,0 +1,35 @@
+// Launchers of the GetHI FFT passes and realisation-stage kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace gethi {
+
+enum KernelClass { KC_ZPASS = 0, KC_YPASS, KC_XPASS, KC_XPASS_VEL, KC_NYQ, KC_SIGMA, KC_FDVEL, KC_GETHI, KC_PROJECT, KC_SCALE };
+
+enum FieldKind { FIELD_DENS = 0, FIELD_VPOT = 1, FIELD_VX = 2, FIELD_VY = 3, FIELD_VZ = 4 };
+
+struct ColGeom {
+  float2 *base;
+  long cpp, pstride, cstride, estride, ncols;
+};
+
+bool fft_supported(int n);
+long row_pass_blocks(int n);
+cudaError_t col_pass(const DevCfg &c, const ColGeom &g, int nyq, bool gen, int kind, const float2 *src,
+                     const float2 *tw, cudaStream_t st);
+cudaError_t row_pass(const DevCfg &c, float2 *main, const float2 *nyq, const float2 *twN, const float2 *twM,
+                     float scale, int epi, float *vr, int comp, int first, double2 *partials, cudaStream_t st);
+cudaError_t finish_sigma(const double2 *partials, int np, double ncells, double *stats, cudaStream_t st);
+cudaError_t gen_modes(const DevCfg &c, float2 *out, int kind, cudaStream_t st);
+
+// stages.cu
+cudaError_t radial_velocity_fd(const DevCfg &c, const float *vpot, float *rvel, cudaStream_t st);
+cudaError_t get_hi(const DevCfg &c, const double *stats, float *dens, float *rvel, cudaStream_t st);
+cudaError_t project(const DevCfg &c, const double *stats, const float *a, const float *b, int fused, float *maps,
+                    int *err, cudaStream_t st);
+cudaError_t scale_maps(const DevCfg &c, float *maps, cudaStream_t st);
+cudaError_t sample_keys(const DevCfg &c, const float *dz, uint32_t *keys, int exact, cudaStream_t st);
+
+}  // namespace gethi

@@ -1,0 +1,273 @@
+"""Host-side mirror of GetHI's stage interface over the GB300 C ABI.
+
+The reference drives one realisation as (src/main_gh.c:34-74)
+
+    par = read_run_params(fname)      # src/io_gh.c:188
+    create_d_and_vr_fields(par)       # src/fourier.c:375
+    get_HI(par)                       # src/grid_tools.c:103
+    mk_T_maps(par)                    # src/pixelize.c:303
+    write_maps(par)                   # src/io_gh.c:109
+    param_gethi_free(par)             # src/io_gh.c:298
+
+and this module keeps those names on a ``GetHI`` object whose work runs in
+libgethi_gpu.so (include/gethi_gpu.h).  There is no CPU fallback: without the
+built library every call raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libgethi_gpu.so")
+NZ = 5001
+
+GETHI_ERRORS = {-1: "GETHI_E_ARG", -2: "GETHI_E_IO", -3: "GETHI_E_COSMO", -4: "GETHI_E_CUDA",
+                -5: "GETHI_E_NOMEM", -6: "GETHI_E_STATE", -7: "GETHI_E_DEVICE"}
+
+
+class GetHIError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (GETHI_ERRORS.get(code, "?"), code, msg))
+        self.code = code
+
+
+class Params(C.Structure):
+    """gethi_params of include/gethi_gpu.h (the .ini keys of src/io_gh.c:211-249 + new keys)."""
+    _fields_ = [("prefix_out", C.c_char * 256), ("pk_filename", C.c_char * 256),
+                ("frequencies_filename", C.c_char * 256)] + \
+        [(n, C.c_double) for n in ("omega_M", "omega_L", "omega_B", "h", "w", "ns", "sigma_8", "r_smooth",
+                                   "nu_min", "nu_max")] + \
+        [("n_nu", C.c_int), ("n_grid", C.c_int), ("n_side", C.c_long), ("seed", C.c_uint),
+         ("do_psources", C.c_int), ("l_box", C.c_double), ("bias_model", C.c_int), ("b_HI", C.c_double)] + \
+        [(n, C.c_int) for n in ("do_rsd", "velocity_mode", "gaussianise", "fft_precision", "rng",
+                                "omp_threads_for_modes", "write_maps")]
+
+
+class Derived(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("fgrowth_0", "hubble_0", "z_min", "z_max", "r_min", "r_max", "l_box",
+                                          "pos_obs", "r2_smooth", "glob_idr", "logkmin", "logkmax", "idlogk",
+                                          "pk_norm", "sigma8_in", "sigma2_gauss", "mean_gauss")] + \
+        [(n, C.c_int) for n in ("do_smoothing", "numk", "n_nu", "regular_nu")] + [("filled_fraction", C.c_double)]
+
+
+_CHOICES = {"bias_model": ("fit", "const"), "velocity_mode": ("fd", "spectral"),
+            "fft_precision": ("fp32", "tc_split"), "rng": ("philox", "mt_validation")}
+
+_lib = None
+
+
+def lib():
+    """Load libgethi_gpu.so (raises if it was not built: there is no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libgethi_gpu.so is not built (%s); run `python -m crime_gb300.build`" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        P = C.POINTER
+        vp = C.c_void_p
+        L.gethi_params_default.argtypes = [P(Params)]
+        L.gethi_read_params.argtypes = [C.c_char_p, P(Params)]
+        L.gethi_host_setup.argtypes = [P(Params), P(Derived), vp, vp, vp, vp, vp]
+        L.gethi_host_modes_mt.argtypes = [P(Params), C.c_int, vp]
+        L.gethi_gpu_init.argtypes = [P(Params), C.c_int, P(vp)]
+        L.gethi_gpu_free.argtypes = [vp]
+        L.gethi_gpu_free.restype = None
+        L.gethi_gpu_set_stream.argtypes = [vp, vp]
+        L.gethi_gpu_get_derived.argtypes = [vp, P(Derived)]
+        L.gethi_last_error.restype = C.c_char_p
+        L.gethi_gpu_make_fields.argtypes = [vp, vp]
+        L.gethi_gpu_get_hi.argtypes = [vp]
+        L.gethi_gpu_make_maps.argtypes = [vp, vp]
+        L.gethi_gpu_write_maps.argtypes = [vp, vp]
+        L.gethi_gpu_run.argtypes = [vp, vp]
+        L.gethi_gpu_download_grids.argtypes = [vp, vp, vp]
+        L.gethi_gpu_upload_grids.argtypes = [vp, vp, vp, C.c_int]
+        L.gethi_gpu_sample_keys.argtypes = [vp, vp, C.c_int]
+        L.gethi_gpu_download_modes.argtypes = [vp, vp]
+        L.gethi_gpu_stage_times.argtypes = [vp, vp, C.c_int]
+        L.gethi_gpu_profile.argtypes = [vp, C.c_int]
+        L.gethi_gpu_set_seed.argtypes = [vp, C.c_uint]
+        L.gethi_gpu_upload_inputs.argtypes = [vp]
+        L.gethi_gpu_upload_inputs.restype = C.c_long
+        L.gethi_gpu_kernel_times.argtypes = [vp, vp, vp, vp]
+        L.gethi_gpu_fallback_count.argtypes = [vp, vp]
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        raise GetHIError(rc, lib().gethi_last_error().decode(errors="replace"))
+    return rc
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def default_params():
+    p = Params()
+    _check(lib().gethi_params_default(C.byref(p)))
+    return p
+
+
+def make_params(**kw):
+    """Reference defaults (src/io_gh.c:133-186) overridden by keyword arguments
+    named like the .ini keys (n_grid=..., omega_M=..., velocity_mode="spectral")."""
+    p = default_params()
+    for k, v in kw.items():
+        if k in _CHOICES and isinstance(v, str):
+            v = _CHOICES[k].index(v)
+        if isinstance(getattr(p, k), bytes):
+            v = str(v).encode()
+        setattr(p, k, v)
+    return p
+
+
+def read_params(fname):
+    p = Params()
+    _check(lib().gethi_read_params(os.fsencode(fname), C.byref(p)))
+    return p
+
+
+def host_setup(p):
+    """FP64 host setup without a GPU: derived values, tables, P(k), offsets, prefactors."""
+    d = Derived()
+    _check(lib().gethi_host_setup(C.byref(p), C.byref(d), None, None, None, None, None))
+    tables = np.zeros(6 * NZ)
+    logk, pk = np.zeros(d.numk), np.zeros(d.numk)
+    offs, pref = np.zeros(30), np.zeros(d.n_nu)
+    _check(lib().gethi_host_setup(C.byref(p), C.byref(d), _ptr(tables), _ptr(logk), _ptr(pk), _ptr(offs),
+                                  _ptr(pref)))
+    return dict(derived=d, tables=tables, logk=logk, pk=pk, offsets=offs.reshape(10, 3), prefac=pref)
+
+
+def host_modes_mt(p, nthreads=1):
+    n = p.n_grid
+    out = np.zeros((n, n, n // 2 + 1), np.complex64)
+    _check(lib().gethi_host_modes_mt(C.byref(p), int(nthreads), out.ctypes.data))
+    return out
+
+
+class GetHI:
+    """One GetHI configuration on one GPU (the ParamGetHI of src/common_gh.h:58-129)."""
+
+    def __init__(self, params, device=0):
+        self.params = params
+        self._ctx = C.c_void_p()
+        _check(lib().gethi_gpu_init(C.byref(params), int(device), C.byref(self._ctx)))
+        self.n = params.n_grid
+        self.npix = 12 * params.n_side ** 2
+        self.n_nu = self.derived().n_nu
+
+    # -- lifecycle
+    def free(self):
+        if self._ctx:
+            lib().gethi_gpu_free(self._ctx)
+            self._ctx = C.c_void_p()
+
+    param_gethi_free = free
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle):
+        _check(lib().gethi_gpu_set_stream(self._ctx, C.c_void_p(stream_handle)))
+
+    def derived(self):
+        d = Derived()
+        _check(lib().gethi_gpu_get_derived(self._ctx, C.byref(d)))
+        return d
+
+    # -- stages, named as in the reference
+    def create_d_and_vr_fields(self, modes_k=None):
+        m = None if modes_k is None else np.ascontiguousarray(modes_k, np.complex64)
+        _check(lib().gethi_gpu_make_fields(self._ctx, _ptr(m)))
+
+    def get_HI(self):
+        _check(lib().gethi_gpu_get_hi(self._ctx))
+
+    def mk_T_maps(self, download=True):
+        maps = np.zeros((self.n_nu, self.npix), np.float32) if download else None
+        _check(lib().gethi_gpu_make_maps(self._ctx, _ptr(maps)))
+        return maps
+
+    def write_maps(self, maps):
+        _check(lib().gethi_gpu_write_maps(self._ctx, _ptr(np.ascontiguousarray(maps, np.float32))))
+
+    def run(self, maps=None):
+        """All stages, get_HI fused into the projection. Returns the maps (host)."""
+        if maps is None:
+            maps = np.zeros((self.n_nu, self.npix), np.float32)
+        _check(lib().gethi_gpu_run(self._ctx, _ptr(maps)))
+        return maps
+
+    def set_seed(self, seed):
+        _check(lib().gethi_gpu_set_seed(self._ctx, int(seed) & 0xFFFFFFFF))
+
+    def upload_inputs(self):
+        r = lib().gethi_gpu_upload_inputs(self._ctx)
+        if r < 0:
+            _check(int(r))
+        return int(r)
+
+    def run_into(self, maps_ptr):
+        """All stages into an existing host buffer given as an address (pinned memory)."""
+        _check(lib().gethi_gpu_run(self._ctx, C.c_void_p(maps_ptr)))
+
+    # -- inspection
+    def grids(self):
+        n = self.n
+        d = np.zeros((n, n, n), np.float32)
+        v = np.zeros((n, n, n), np.float32)
+        _check(lib().gethi_gpu_download_grids(self._ctx, _ptr(d), _ptr(v)))
+        return d, v
+
+    def upload_grids(self, dens, rvel, stage):
+        n = self.n
+        d = np.ascontiguousarray(dens, np.float32).reshape(n, n, n)
+        v = np.ascontiguousarray(rvel, np.float32).reshape(n, n, n)
+        _check(lib().gethi_gpu_upload_grids(self._ctx, _ptr(d), _ptr(v), int(stage)))
+
+    def sample_keys(self, exact=True):
+        keys = np.zeros(self.n ** 3 * 10, np.uint32)
+        _check(lib().gethi_gpu_sample_keys(self._ctx, _ptr(keys), int(bool(exact))))
+        return keys
+
+    def device_modes(self):
+        n = self.n
+        out = np.zeros((n, n, n // 2 + 1), np.complex64)
+        _check(lib().gethi_gpu_download_modes(self._ctx, _ptr(out)))
+        return out
+
+    KERNEL_CLASSES = ("zpass", "ypass", "xpass", "xpass_vel", "nyq", "sigma", "fd_vel", "get_hi", "project",
+                      "scale")
+
+    def profile(self, on=True):
+        _check(lib().gethi_gpu_profile(self._ctx, int(on)))
+
+    def kernel_times(self):
+        ms = np.zeros(10)
+        cnt = np.zeros(10, np.int64)
+        launches = np.zeros(1, np.int64)
+        lib().gethi_gpu_kernel_times(self._ctx, _ptr(ms), _ptr(cnt), _ptr(launches))
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.KERNEL_CLASSES)}, int(launches[0])
+
+    def fallback_count(self):
+        v = np.zeros(1, np.int64)
+        _check(lib().gethi_gpu_fallback_count(self._ctx, _ptr(v)))
+        return int(v[0])
+
+    def stage_times(self):
+        ms = np.zeros(8, np.float32)
+        k = lib().gethi_gpu_stage_times(self._ctx, _ptr(ms), 8)
+        return ms[:max(k, 0)]
+
+
+def read_run_params(fname, device=0):
+    """src/io_gh.c:188: parse the .ini and set the run up (on the GPU)."""
+    return GetHI(read_params(fname), device)

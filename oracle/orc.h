@@ -99,6 +99,8 @@ void orc_normalize(int n, double l_box, float *data);          /* fourier.c:397-
 /* ---- real-space stages ---- */
 void orc_radial_velocity_fd(const orc_config *c, const orc_derived *d, const float *vpot,
                             float *rvel);                       /* fourier.c:307-373 */
+void orc_radial_velocity_spectral(const orc_config *c, const orc_derived *d, const float *dens_k,
+                                  float *rvel);
 void orc_sigma_dens(int n, const float *dens, double *mean, double *sigma2); /* fourier.c:24-76 */
 void orc_get_hi(const orc_config *c, const orc_derived *d, double sigma2, float *dens,
                 float *rvel);                                   /* grid_tools.c:103-153 */

@@ -60,6 +60,7 @@ def lib():
         L.orc_c2r_to_double.argtypes = [C.c_int, f32p, f64p]
         L.orc_normalize.argtypes = [C.c_int, C.c_double, f32p]
         L.orc_radial_velocity_fd.argtypes = [P(Config), P(Derived), f32p, f32p]
+        L.orc_radial_velocity_spectral.argtypes = [P(Config), P(Derived), f32p, f32p]
         L.orc_sigma_dens.argtypes = [C.c_int, f32p, P(C.c_double), P(C.c_double)]
         L.orc_get_hi.argtypes = [P(Config), P(Derived), C.c_double, f32p, f32p]
         L.orc_subsample_offsets.argtypes = [C.c_uint, C.c_double, f64p, f64p, f64p]
@@ -146,6 +147,13 @@ class Oracle:
         rv = np.zeros(self.real_pad_shape(), np.float32)
         lib().orc_radial_velocity_fd(C.byref(self.c), C.byref(self.d),
                                      np.ascontiguousarray(vpot_real, np.float32).reshape(-1), rv.reshape(-1))
+        return rv
+
+    def radial_velocity_spectral(self, dens_k):
+        rv = np.zeros(self.real_pad_shape(), np.float32)
+        lib().orc_radial_velocity_spectral(C.byref(self.c), C.byref(self.d),
+                                           np.ascontiguousarray(dens_k, np.complex64).view(np.float32).reshape(-1),
+                                           rv.reshape(-1))
         return rv
 
     def sigma(self, dens):

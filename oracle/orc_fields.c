@@ -190,3 +190,61 @@ void orc_get_hi(const orc_config *c, const orc_derived *d, double sigma2, float 
     }
   }
 }
+
+/* Spectral radial velocity (velocity_mode=spectral, not in the reference):
+ * v_j(x) = c2r(i k_j phi_k) with phi_k = delta_k f0 H0 / k^2 (src/fourier.c:298)
+ * and the derivative of a Nyquist component set to zero, normalised like
+ * src/fourier.c:403 and projected on the unit vector from the observer.
+ * FP64 throughout; rvel is the padded [z][y][2(N/2+1)] float grid. */
+void orc_radial_velocity_spectral(const orc_config *c, const orc_derived *d, const float *dens_k, float *rvel)
+{
+  int n = c->n_grid, h = n / 2 + 1;
+  size_t nh = (size_t)n * n * h, n3 = (size_t)n * n * n;
+  double dk = 2 * M_PI / d->l_box, factor = d->fgrowth_0 * d->hubble_0;
+  double norm = pow(sqrt(2 * M_PI) / d->l_box, 3), dx = d->l_box / n;
+  float *spec = (float *)malloc(sizeof(float) * 2 * nh);
+  double *comp = (double *)malloc(sizeof(double) * n3), *acc = (double *)calloc(n3, sizeof(double));
+  for (int j = 0; j < 3; j++) {
+    /* the c2r helper reads float input: keep i k_j phi_k in double until the
+     * final rounding by splitting into hi + lo float parts */
+    float *lo = (float *)malloc(sizeof(float) * 2 * nh);
+    for (int ii = 0; ii < n; ii++)
+      for (int jj = 0; jj < n; jj++)
+        for (int kk = 0; kk < h; kk++) {
+          size_t idx = kk + (size_t)h * (jj + (size_t)n * ii);
+          double kx = kval(kk, n, dk), ky = kval(jj, n, dk), kz = kval(ii, n, dk);
+          double k2 = kx * kx + ky * ky + kz * kz;
+          double kj = j == 0 ? (2 * kk == n ? 0 : kx) : j == 1 ? (2 * jj == n ? 0 : ky) : (2 * ii == n ? 0 : kz);
+          double re = 0, im = 0;
+          if (k2 > 0) {
+            double f = factor / k2 * kj;
+            re = -dens_k[2 * idx + 1] * f;
+            im = dens_k[2 * idx] * f;
+          }
+          spec[2 * idx] = (float)re;
+          spec[2 * idx + 1] = (float)im;
+          lo[2 * idx] = (float)(re - (double)spec[2 * idx]);
+          lo[2 * idx + 1] = (float)(im - (double)spec[2 * idx + 1]);
+        }
+    orc_c2r_to_double(n, spec, comp);
+    double *c2 = (double *)malloc(sizeof(double) * n3);
+    orc_c2r_to_double(n, lo, c2);
+    for (int iz = 0; iz < n; iz++)
+      for (int iy = 0; iy < n; iy++)
+        for (int ix = 0; ix < n; ix++) {
+          size_t q = ix + (size_t)n * (iy + (size_t)n * iz);
+          double x = dx * (ix + 0.5) - d->pos_obs[0], y = dx * (iy + 0.5) - d->pos_obs[1], z = dx * (iz + 0.5) - d->pos_obs[2];
+          double u = (j == 0 ? x : j == 1 ? y : z) / sqrt(x * x + y * y + z * z);
+          acc[q] += (comp[q] + c2[q]) * norm * u;
+        }
+    free(c2);
+    free(lo);
+  }
+  for (int iz = 0; iz < n; iz++)
+    for (int iy = 0; iy < n; iy++)
+      for (int ix = 0; ix < n; ix++)
+        rvel[ix + 2 * (size_t)h * (iy + (size_t)n * iz)] = (float)acc[ix + (size_t)n * (iy + (size_t)n * iz)];
+  free(spec);
+  free(comp);
+  free(acc);
+}

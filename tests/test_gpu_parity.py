@@ -1,0 +1,172 @@
+"""GPU path against the oracle and the reference's golden vectors, through the C ABI.
+
+Tolerances: integer work (per-sample pixel and shell keys) is bit-exact;
+FP32 fields against FP64 references are compared by relative L2 norm
+(FFT: 2e-6, finite-difference velocity: 2e-5), HI mass/dz element-wise to
+2e-5 relative, maps element-wise to 1e-5 relative (FP32 sums in a different
+order than the reference's atomics)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, load_case, oracle_for_case
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gh():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from crime_gb300 import build
+    build.build()
+    import crime_gb300
+    return crime_gb300
+
+
+def params_for_case(gh, case, **extra):
+    kw = dict(omega_M=0.315, omega_L=0.685, omega_B=0.049, h=0.67, w=-1.0, ns=0.96, sigma_8=0.83,
+              pk_filename=os.path.join(GOLDEN, "pk_eh_nowiggle.txt"), n_grid=int(case["cfg_n_grid"]),
+              n_side=int(case["cfg_n_side"]), seed=int(case["cfg_seed"]),
+              r_smooth=float(case["cfg_r_smooth"]) if "cfg_r_smooth" in case else 2.0)
+    if int(case["cfg_regular_nu"]):
+        kw.update(frequencies_filename="", nu_min=float(case["cfg_nu_min"]), nu_max=float(case["cfg_nu_max"]),
+                  n_nu=int(case["cfg_n_nu"]))
+    else:
+        kw.update(frequencies_filename=os.path.join(GOLDEN, "nutable_8.txt"))
+    kw.update(extra)
+    return gh.make_params(**kw)
+
+
+def cells(a, n):
+    """real cells of a padded reference grid -> compact [z][y][x]"""
+    return np.asarray(a).reshape(n, n, 2 * (n // 2 + 1))[:, :, :n]
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+CASES = ["case_irr32", "case_reg24"]
+
+
+@pytest.fixture(scope="module", params=CASES)
+def run(request, gh):
+    g = load_case(request.param)
+    n = int(g["cfg_n_grid"])
+    ctx = gh.GetHI(params_for_case(gh, g))
+    modes = g["dens_k"].view(np.complex64).reshape(n, n, n // 2 + 1)
+    ctx.create_d_and_vr_fields(modes)
+    yield g, ctx, n
+    ctx.free()
+
+
+def test_fields_vs_reference(run):
+    g, ctx, n = run
+    dens, vr = ctx.grids()
+    assert rel_l2(dens, cells(g["dens_real"], n)) < 2e-6
+    assert rel_l2(vr, cells(g["rvel"], n)) < 2e-5
+    d = ctx.derived()
+    assert abs(d.sigma2_gauss / g["p_sigma2_gauss"] - 1) < 2e-6
+
+
+def test_get_hi_vs_reference(run):
+    g, ctx, n = run
+    ctx.upload_grids(cells(g["dens_real"], n), cells(g["rvel"], n), stage=1)
+    ctx.get_HI()
+    mass, dz = ctx.grids()
+    np.testing.assert_allclose(mass, cells(g["mass"], n), rtol=2e-5, atol=0)
+    ref_dz = cells(g["dz"], n)
+    np.testing.assert_allclose(dz, ref_dz, rtol=2e-5, atol=2e-5 * np.abs(ref_dz).max())
+
+
+@pytest.mark.parametrize("exact", [True, False], ids=["fp64", "fp32_certified"])
+def test_sample_keys_bitexact(run, exact):
+    g, ctx, n = run
+    ctx.upload_grids(cells(g["mass"], n), cells(g["dz"], n), stage=2)
+    keys = ctx.sample_keys(exact=exact)
+    o = oracle_for_case(g)
+    _, okeys = o.mk_T_maps(g["mass"], g["dz"], want_keys=True)
+    assert np.count_nonzero(okeys != 0xFFFFFFFF) > 0.3 * okeys.size
+    np.testing.assert_array_equal(keys, okeys)
+
+
+def test_maps_vs_reference(run):
+    g, ctx, n = run
+    ctx.upload_grids(cells(g["mass"], n), cells(g["dz"], n), stage=2)
+    maps = ctx.mk_T_maps()
+    ref = g["maps"].reshape(maps.shape)
+    np.testing.assert_allclose(maps, ref, rtol=1e-5, atol=1e-6 * np.abs(ref).max())
+
+
+def test_philox_modes_vs_oracle(gh):
+    g = load_case("case_irr32")
+    ctx = gh.GetHI(params_for_case(gh, g))
+    dm = ctx.device_modes()
+    ctx.free()
+    om = oracle_for_case(g).modes_philox()
+    amp = np.abs(om)
+    assert np.all(np.abs(dm - om) <= 3e-5 * amp + 1e-30)
+
+
+def test_spectral_velocity_vs_oracle(gh):
+    g = load_case("case_irr32")
+    n = int(g["cfg_n_grid"])
+    ctx = gh.GetHI(params_for_case(gh, g, velocity_mode="spectral"))
+    modes = g["dens_k"].view(np.complex64).reshape(n, n, n // 2 + 1)
+    ctx.create_d_and_vr_fields(modes)
+    _, vr = ctx.grids()
+    ctx.free()
+    ref = cells(oracle_for_case(g).radial_velocity_spectral(modes), n)
+    assert rel_l2(vr, ref) < 2e-6
+
+
+def test_stage_order_and_errors(gh):
+    g = load_case("case_reg24")
+    ctx = gh.GetHI(params_for_case(gh, g))
+    with pytest.raises(gh.GetHIError) as e:
+        ctx.get_HI()
+    assert e.value.code == -6
+    with pytest.raises(gh.GetHIError) as e:
+        ctx.mk_T_maps()
+    assert e.value.code == -6
+    ctx.free()
+    with pytest.raises(gh.GetHIError) as e:
+        gh.GetHI(params_for_case(gh, g, n_grid=48))
+    assert e.value.code == -1
+
+
+@pytest.mark.parametrize("vmode", ["fd", "spectral"])
+def test_production_run_vs_oracle(gh, vmode):
+    """Philox modes end to end (run() fuses get_HI into the projection) against
+    the oracle fed with the same modes: FP64 FFTs, FP64 lognormal, reference binning."""
+    g = load_case("case_irr32")
+    n = int(g["cfg_n_grid"])
+    ctx = gh.GetHI(params_for_case(gh, g, velocity_mode=vmode))
+    maps = ctx.run()
+    modes = ctx.device_modes()
+    ctx.free()
+    o = oracle_for_case(g)
+    dens = o.normalize(o.c2r(modes))
+    if vmode == "fd":
+        k = np.fft.fftfreq(n, 1.0 / n) * (2 * np.pi / o.d.l_box)
+        kx = np.abs(k[: n // 2 + 1])
+        kx[n // 2] = n // 2 * 2 * np.pi / o.d.l_box
+        kz, ky = k.copy(), k.copy()
+        kz[n // 2] = ky[n // 2] = n // 2 * 2 * np.pi / o.d.l_box
+        k2 = kz[:, None, None] ** 2 + ky[None, :, None] ** 2 + kx[None, None, :] ** 2
+        k2[0, 0, 0] = 1
+        vk = (modes.astype(np.complex128) * (o.d.fgrowth_0 * o.d.hubble_0) / k2).astype(np.complex64)
+        rv = o.radial_velocity_fd(o.normalize(o.c2r(vk)))
+    else:
+        rv = o.radial_velocity_spectral(modes)
+    _, s2 = o.sigma(dens)
+    mass, dz = o.get_hi(dens, rv, s2)
+    ref = o.mk_T_maps(mass, dz)
+    assert rel_l2(maps, ref) < 1e-4
+    close = np.isclose(maps, ref, rtol=1e-5, atol=1e-6 * np.abs(ref).max())
+    assert close.mean() > 0.995
