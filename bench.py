@@ -119,7 +119,8 @@ def algorithmic_bytes(cls, n, npix, n_nu):
     """Minimum HBM bytes of one launch of a kernel class (FP32 data)."""
     n3 = float(n) ** 3
     return {
-        "zpass": 4 * n3,            # write the half spectrum: 8 B/mode, N^3/2 modes
+        "zpass": 8 * n3,            # write the raw modes and the transformed column: 2 x 8 B/mode
+        "zpass_raw": 8 * n3,        # read the raw modes, write the transformed column
         "ypass": 8 * n3,            # read + write 8 B/mode
         "xpass": 8 * n3,            # read 8 B/mode, write 4 B/cell
         "xpass_vel": 32.0 / 3 * n3,  # read 8 B/mode, read (2 of 3 comps) + write v_r 4 B/cell

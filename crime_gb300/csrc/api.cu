@@ -28,6 +28,7 @@ struct gethi_ctx {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   float2 *main = nullptr, *nyq = nullptr, *vmain = nullptr, *vnyq = nullptr, *modes = nullptr;
+  float2 *raw = nullptr, *rawnyq = nullptr;  // delta_k kept for the velocity fields
   float *vr = nullptr, *maps = nullptr;
   float2 *twN = nullptr, *twM = nullptr;
   double2 *partials = nullptr;
@@ -195,26 +196,29 @@ void collect_kernel_times(gethi_ctx *c)
 }
 
 // One field: Z pass (modes generated on the fly), Y pass, X pass with epilogue.
-int field_fft(gethi_ctx *c, float2 *main, float2 *nyq, int kind, const float2 *src, int epi, int comp, int first)
+// The first field (delta) draws the modes and keeps them in raw/rawnyq; later
+// fields read them back (zmode 2) instead of drawing again.
+int field_fft(gethi_ctx *c, float2 *main, float2 *nyq, int kind, const float2 *src, int epi, int comp, int first,
+              int zmode)
 {
   const DevCfg &g = c->cfg;
   const long n = g.n, m = g.m;
   cudaStream_t st = c->stream;
   {
-    KTimer t(c, KC_ZPASS);
-    CK(col_pass(g, geom(main, n * m, 0, 1, n * m, n * m), 0, true, kind, src, c->twN, st));
+    KTimer t(c, zmode == 1 ? KC_ZPASS : KC_ZPASS_RAW);
+    CK(col_pass(g, geom(main, n * m, 0, 1, n * m, n * m), 0, zmode, kind, src, c->twN, c->raw, st));
   }
   {
     KTimer t(c, KC_NYQ);
-    CK(col_pass(g, geom(nyq, n, 0, 1, n, n), 1, true, kind, src, c->twN, st));
+    CK(col_pass(g, geom(nyq, n, 0, 1, n, n), 1, zmode, kind, src, c->twN, c->rawnyq, st));
   }
   {
     KTimer t(c, KC_YPASS);
-    CK(col_pass(g, geom(main, m, n * m, 1, m, n * m), 0, false, kind, nullptr, c->twN, st));
+    CK(col_pass(g, geom(main, m, n * m, 1, m, n * m), 0, 0, kind, nullptr, c->twN, nullptr, st));
   }
   {
     KTimer t(c, KC_NYQ);
-    CK(col_pass(g, geom(nyq, n, 0, n, 1, n), 1, false, kind, nullptr, c->twN, st));
+    CK(col_pass(g, geom(nyq, n, 0, n, 1, n), 1, 0, kind, nullptr, c->twN, nullptr, st));
   }
   {
     KTimer t(c, epi ? KC_XPASS_VEL : KC_XPASS);
@@ -255,6 +259,7 @@ extern "C" int gethi_gpu_init(const gethi_params *p, int device, gethi_ctx **out
   if ((rc = dalloc(&c->main, ncell / 2)) || (rc = dalloc(&c->nyq, (size_t)n * n)) ||
       (rc = dalloc(&c->vmain, ncell / 2)) || (rc = dalloc(&c->vnyq, (size_t)n * n)) ||
       (rc = dalloc(&c->vr, ncell)) || (rc = dalloc(&c->maps, (size_t)npix * s.p.n_nu)) ||
+      (s.p.do_rsd && ((rc = dalloc(&c->raw, ncell / 2)) || (rc = dalloc(&c->rawnyq, (size_t)n * n)))) ||
       (rc = dalloc(&c->twN, (size_t)n)) || (rc = dalloc(&c->twM, (size_t)m)) ||
       (rc = dalloc(&c->partials, (size_t)c->npartials)) || (rc = dalloc(&c->stats, 4)) ||
       (rc = dalloc(&c->pk_f, (size_t)s.d.numk)) || (rc = dalloc(&c->logk_f, (size_t)s.d.numk)) ||
@@ -320,7 +325,7 @@ extern "C" void gethi_gpu_free(gethi_ctx *c)
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  void *bufs[] = {c->main, c->nyq, c->vmain, c->vnyq, c->modes, c->vr, c->maps, c->twN, c->twM, c->partials,
+  void *bufs[] = {c->main, c->nyq, c->vmain, c->vnyq, c->modes, c->raw, c->rawnyq, c->vr, c->maps, c->twN, c->twM, c->partials,
                   c->stats, c->pk_f, c->logk_f, c->tab_f, c->tab_d, c->prefac, c->edges_f, c->edges_d, c->counters};
   for (void *b : bufs)
     if (b) cudaFree(b);
@@ -387,7 +392,7 @@ extern "C" int gethi_gpu_make_fields(gethi_ctx *c, const float *modes_k)
   }
   c->nev = 0;
   record(c);
-  int rc = field_fft(c, c->main, c->nyq, FIELD_DENS, src, 0, 0, 0);
+  int rc = field_fft(c, c->main, c->nyq, FIELD_DENS, src, 0, 0, 0, 1);
   if (rc) return rc;
   {
     KTimer t(c, KC_SIGMA);
@@ -397,9 +402,9 @@ extern "C" int gethi_gpu_make_fields(gethi_ctx *c, const float *modes_k)
   if (s.p.do_rsd) {
     if (s.p.velocity_mode == 1) {
       for (int comp = 0; comp < 3; comp++)
-        if ((rc = field_fft(c, c->vmain, c->vnyq, FIELD_VX + comp, src, 1, comp, comp == 0))) return rc;
+        if ((rc = field_fft(c, c->vmain, c->vnyq, FIELD_VX + comp, src, 1, comp, comp == 0, 2))) return rc;
     } else {
-      if ((rc = field_fft(c, c->vmain, c->vnyq, FIELD_VPOT, src, 0, 0, 0))) return rc;
+      if ((rc = field_fft(c, c->vmain, c->vnyq, FIELD_VPOT, src, 0, 0, 0, 2))) return rc;
       KTimer t(c, KC_FDVEL);
       CK(radial_velocity_fd(c->cfg, reinterpret_cast<const float *>(c->vmain), c->vr, c->stream));
     }
@@ -521,7 +526,8 @@ extern "C" int gethi_gpu_sample_keys(gethi_ctx *c, uint32_t *keys, int exact_fp6
   uint32_t *dk = nullptr;
   int rc = dalloc(&dk, (size_t)n * n * n * NSUB);
   if (rc) return rc;
-  cudaError_t e = sample_keys(c->cfg, c->vr, dk, exact_fp64, c->stream);
+  cudaError_t e = cudaMemsetAsync(c->counters, 0, sizeof(int) * 16, c->stream);
+  if (e == cudaSuccess) e = sample_keys(c->cfg, c->vr, dk, exact_fp64, c->counters, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e == cudaSuccess) e = cudaMemcpy(keys, dk, sizeof(uint32_t) * n * n * n * NSUB, cudaMemcpyDeviceToHost);
   cudaFree(dk);

@@ -83,10 +83,24 @@ __device__ __forceinline__ float2 mode_value(const DevCfg &c, int ii, int jj, in
 // column passes (Z and Y)
 // element (col, e) of a column set lives at base + (col/cpp) pstride + (col%cpp) cstride + e estride
 // ---------------------------------------------------------------------------
-template <int L, int P, int TX, class Rad, bool GEN>
+// kind transform of a stored delta_k (mode ii, jj, kk): FIELD_DENS, FIELD_VPOT or FIELD_V*
+__device__ __forceinline__ float2 field_from_delta(const DevCfg &c, float2 d, int ii, int jj, int kk, int kind)
+{
+  if (kind == FIELD_DENS) return d;
+  const int n = c.n;
+  float kz = kval(ii, n, c.dk), ky = kval(jj, n, c.dk), kx = kval(kk, n, c.dk);
+  float k2 = kx * kx + ky * ky + kz * kz;
+  if (k2 <= 0.f) return make_float2(0.f, 0.f);
+  float f = c.vfac / k2;
+  if (kind == FIELD_VPOT) return cscale(d, f);
+  float kj = kind == FIELD_VX ? (2 * kk == n ? 0.f : kx) : kind == FIELD_VY ? (2 * jj == n ? 0.f : ky) : (2 * ii == n ? 0.f : kz);
+  return cmul_i(cscale(d, f * kj));
+}
+
+template <int L, int P, int TX, class Rad, int MODE>
 __global__ void __launch_bounds__(TX *(L / P)) col_pass_kernel(DevCfg c, ColGeom g, int nyq, int kind,
                                                                const float2 *__restrict__ src,
-                                                               const float2 *__restrict__ tw)
+                                                               const float2 *__restrict__ tw, float2 *raw)
 {
   constexpr int T = L / P;
   constexpr int R0 = radix_first(Rad{}), RL = radix_last(Rad{});
@@ -103,9 +117,14 @@ __global__ void __launch_bounds__(TX *(L / P)) col_pass_kernel(DevCfg c, ColGeom
       const int e = t + T * j + (L / R0) * r;
       float2 x = make_float2(0.f, 0.f);
       if (active) {
-        if constexpr (GEN) {
+        if constexpr (MODE == 1) {
           int ky = nyq ? (int)col : (int)(col / c.m), kx = nyq ? c.m : (int)(col % c.m);
-          x = mode_value(c, e, ky, kx, kind, src);
+          x = mode_value(c, e, ky, kx, FIELD_DENS, src);
+          if (raw) raw[cb + (long)e * g.estride] = x;
+          x = field_from_delta(c, x, e, ky, kx, kind);
+        } else if constexpr (MODE == 2) {
+          int ky = nyq ? (int)col : (int)(col / c.m), kx = nyq ? c.m : (int)(col % c.m);
+          x = field_from_delta(c, __ldg(&raw[cb + (long)e * g.estride]), e, ky, kx, kind);
         } else {
           x = g.base[cb + (long)e * g.estride];
         }
@@ -167,6 +186,14 @@ __global__ void __launch_bounds__(RW *(M / P)) row_pass_kernel(DevCfg c, float2 
   double s1 = 0, s2 = 0;
   if (active) {
     if constexpr (EPI == 0) {
+      // per-thread sums in FP32 with Neumaier compensation (P values each),
+      // carried to FP64 for the block and grid reductions
+      float a1 = 0.f, c1 = 0.f, a2 = 0.f, c2 = 0.f;
+      auto nsum = [](float &acc, float &comp, float v) {
+        float t = acc + v;
+        comp += fabsf(acc) >= fabsf(v) ? (acc - t) + v : (v - t) + acc;
+        acc = t;
+      };
 #pragma unroll
       for (int j = 0; j < P / RL; j++)
 #pragma unroll
@@ -174,9 +201,13 @@ __global__ void __launch_bounds__(RW *(M / P)) row_pass_kernel(DevCfg c, float2 
           const int e = t + T * j + (M / RL) * r;
           float2 x = cscale(v[j * RL + r], scale);
           grow[e] = x;
-          s1 += (double)x.x + (double)x.y;
-          s2 += (double)(x.x * x.x) + (double)(x.y * x.y);  // float squares, src/fourier.c:51
+          nsum(a1, c1, x.x);
+          nsum(a1, c1, x.y);
+          nsum(a2, c2, x.x * x.x);  // float squares, src/fourier.c:51
+          nsum(a2, c2, x.y * x.y);
         }
+      s1 = (double)a1 + (double)c1;
+      s2 = (double)a2 + (double)c2;
     } else {
       const int iy = (int)(row % c.n), iz = (int)(row / c.n);
       const float y = c.dxf * (iy + 0.5f) - c.pos_obsf, z = c.dxf * (iz + 0.5f) - c.pos_obsf;
@@ -309,9 +340,9 @@ template <> struct RowPlan<16> { static constexpr int P = 4, RW = 32; using R = 
 template <> struct RowPlan<12> { static constexpr int P = 12, RW = 32; using R = Radices<12>; };
 template <> struct RowPlan<8> { static constexpr int P = 8, RW = 32; using R = Radices<8>; };
 
-template <int L, bool GEN>
+template <int L, int GEN>
 static cudaError_t launch_col(const DevCfg &c, const ColGeom &g, int nyq, int kind, const float2 *src,
-                              const float2 *tw, cudaStream_t st)
+                              const float2 *tw, float2 *raw, cudaStream_t st)
 {
   using PL = ColPlan<L>;
   constexpr int threads = PL::TX * (L / PL::P);
@@ -323,7 +354,7 @@ static cudaError_t launch_col(const DevCfg &c, const ColGeom &g, int nyq, int ki
     attr = true;
   }
   long blocks = (g.ncols + PL::TX - 1) / PL::TX;
-  kern<<<(unsigned)blocks, threads, sm, st>>>(c, g, nyq, kind, src, tw);
+  kern<<<(unsigned)blocks, threads, sm, st>>>(c, g, nyq, kind, src, tw, raw);
   return cudaGetLastError();
 }
 
@@ -376,26 +407,28 @@ bool fft_supported(int n)
 
 #define GETHI_COL_DISPATCH(GENV)                                                                    \
   switch (c.n) {                                                                                    \
-    case 2048: return launch_col<2048, GENV>(c, g, nyq, kind, src, tw, st);                        \
-    case 1024: return launch_col<1024, GENV>(c, g, nyq, kind, src, tw, st);                        \
-    case 512: return launch_col<512, GENV>(c, g, nyq, kind, src, tw, st);                          \
-    case 384: return launch_col<384, GENV>(c, g, nyq, kind, src, tw, st);                          \
-    case 256: return launch_col<256, GENV>(c, g, nyq, kind, src, tw, st);                          \
-    case 128: return launch_col<128, GENV>(c, g, nyq, kind, src, tw, st);                          \
-    case 64: return launch_col<64, GENV>(c, g, nyq, kind, src, tw, st);                            \
-    case 32: return launch_col<32, GENV>(c, g, nyq, kind, src, tw, st);                            \
-    case 24: return launch_col<24, GENV>(c, g, nyq, kind, src, tw, st);                            \
-    case 16: return launch_col<16, GENV>(c, g, nyq, kind, src, tw, st);                            \
+    case 2048: return launch_col<2048, GENV>(c, g, nyq, kind, src, tw, raw, st);                        \
+    case 1024: return launch_col<1024, GENV>(c, g, nyq, kind, src, tw, raw, st);                        \
+    case 512: return launch_col<512, GENV>(c, g, nyq, kind, src, tw, raw, st);                          \
+    case 384: return launch_col<384, GENV>(c, g, nyq, kind, src, tw, raw, st);                          \
+    case 256: return launch_col<256, GENV>(c, g, nyq, kind, src, tw, raw, st);                          \
+    case 128: return launch_col<128, GENV>(c, g, nyq, kind, src, tw, raw, st);                          \
+    case 64: return launch_col<64, GENV>(c, g, nyq, kind, src, tw, raw, st);                            \
+    case 32: return launch_col<32, GENV>(c, g, nyq, kind, src, tw, raw, st);                            \
+    case 24: return launch_col<24, GENV>(c, g, nyq, kind, src, tw, raw, st);                            \
+    case 16: return launch_col<16, GENV>(c, g, nyq, kind, src, tw, raw, st);                            \
     default: return cudaErrorInvalidValue;                                                          \
   }
 
-cudaError_t col_pass(const DevCfg &c, const ColGeom &g, int nyq, bool gen, int kind, const float2 *src,
-                     const float2 *tw, cudaStream_t st)
+cudaError_t col_pass(const DevCfg &c, const ColGeom &g, int nyq, int mode, int kind, const float2 *src,
+                     const float2 *tw, float2 *raw, cudaStream_t st)
 {
-  if (gen) {
-    GETHI_COL_DISPATCH(true)
+  if (mode == 1) {
+    GETHI_COL_DISPATCH(1)
+  } else if (mode == 2) {
+    GETHI_COL_DISPATCH(2)
   } else {
-    GETHI_COL_DISPATCH(false)
+    GETHI_COL_DISPATCH(0)
   }
 }
 

@@ -6,7 +6,10 @@
 
 namespace gethi {
 
-enum KernelClass { KC_ZPASS = 0, KC_YPASS, KC_XPASS, KC_XPASS_VEL, KC_NYQ, KC_SIGMA, KC_FDVEL, KC_GETHI, KC_PROJECT, KC_SCALE };
+enum KernelClass {
+  KC_ZPASS = 0, KC_YPASS, KC_XPASS, KC_XPASS_VEL, KC_NYQ, KC_SIGMA, KC_FDVEL, KC_GETHI, KC_PROJECT, KC_SCALE,
+  KC_ZPASS_RAW
+};
 
 enum FieldKind { FIELD_DENS = 0, FIELD_VPOT = 1, FIELD_VX = 2, FIELD_VY = 3, FIELD_VZ = 4 };
 
@@ -17,8 +20,10 @@ struct ColGeom {
 
 bool fft_supported(int n);
 long row_pass_blocks(int n);
-cudaError_t col_pass(const DevCfg &c, const ColGeom &g, int nyq, bool gen, int kind, const float2 *src,
-                     const float2 *tw, cudaStream_t st);
+// mode 0: transform in place; 1: draw delta_k (Philox or src) and store it to raw
+// (if non-null) before transforming field `kind`; 2: read delta_k from raw
+cudaError_t col_pass(const DevCfg &c, const ColGeom &g, int nyq, int mode, int kind, const float2 *src,
+                     const float2 *tw, float2 *raw, cudaStream_t st);
 cudaError_t row_pass(const DevCfg &c, float2 *main, const float2 *nyq, const float2 *twN, const float2 *twM,
                      float scale, int epi, float *vr, int comp, int first, double2 *partials, cudaStream_t st);
 cudaError_t finish_sigma(const double2 *partials, int np, double ncells, double *stats, cudaStream_t st);
@@ -30,6 +35,7 @@ cudaError_t get_hi(const DevCfg &c, const double *stats, float *dens, float *rve
 cudaError_t project(const DevCfg &c, const double *stats, const float *a, const float *b, int fused, float *maps,
                     int *err, cudaStream_t st);
 cudaError_t scale_maps(const DevCfg &c, float *maps, cudaStream_t st);
-cudaError_t sample_keys(const DevCfg &c, const float *dz, uint32_t *keys, int exact, cudaStream_t st);
+cudaError_t sample_keys(const DevCfg &c, const float *dz, uint32_t *keys, int exact, int *counters,
+                        cudaStream_t st);
 
 }  // namespace gethi

@@ -159,39 +159,48 @@ __device__ __noinline__ uint32_t key_exact(const DevCfg &c, int ix, int iy, int 
 }
 
 // ---------------------------------------------------------------------------
-// FP32 fast key with error margins.  Returns false when a floor or comparison
-// of the exact computation lies within the FP32 error bound of a boundary; the
-// caller then uses key_exact.  Bounds (5x safety on the estimated error):
-//   shells: relative error of nu < 6e-7       -> margin 3e-6 nu
-//   pixels: error of the floor arguments < nside (0.64 dtt + 0.75 dcos) + 2 ulp
+// FP32 fast key with certified margins.  Geometry is in cell units relative to
+// the observer: X = (ix - n/2) + (0.5 + xs/dx), which FP32 holds to half an
+// ulp of |X|.  Every floor and comparison of the exact computation is made on
+// an FP32 value whose worst-case error is bounded below; if the value lies
+// within twice that bound of the decision boundary the sample is "uncertain"
+// and key_exact decides it.  Error budget (relative unless stated):
+//   position 6e-8; R = sqrt(R^2) 3.6e-7; table redshift abs 1e-6 + 3e-7 (1+z);
+//   nu 6e-7 -> shell margin 1.2e-6 nu.
+//   angle: the octant angle a = atan2f(min,max) in [0, pi/4] has <= 3 ulp
+//   (1.8e-7) + 6e-8 from the position; cos(theta) = Z/R <= 2.5e-7 abs.
+//   floor arguments are split into an exact integer/half-integer part and a
+//   remainder of magnitude <= nside + 1, so their rounding is <= 2 ulp(nside+1).
 // ---------------------------------------------------------------------------
 struct FastConst {
-  float xsf[kNSUB], ysf[kNSUB], zsf[kNSUB];
+  float xsp[kNSUB], ysp[kNSUB], zsp[kNSUB];  // 0.5 + offset/dx
+  float idr_cell;                             // glob_idr * dx
+  float half_n;                               // n/2
 };
 
 __device__ __forceinline__ bool near_int(float u, float m) { return fabsf(u - rintf(u)) < m; }
 
-__device__ __forceinline__ bool key_fast(const DevCfg &c, const float *__restrict__ ef, float x, float y, float z,
-                                         float dz, float epos, uint32_t &key)
+__device__ __forceinline__ bool key_fast(const DevCfg &c, const FastConst &f, const float *ef, float X, float Y,
+                                         float Z, float dz, uint32_t &key)
 {
-  float rho2 = x * x + y * y;
-  float r = sqrtf(rho2 + z * z);
-  float tr = r * c.glob_idr_f;
+  const float rho2 = X * X + Y * Y;
+  const float R = sqrtf(rho2 + Z * Z);
+  const float tr = R * f.idr_cell;
   if (!(tr < (float)(kNZ - 2))) return false;
-  int ir = (int)tr;
-  float fr = tr - ir;
-  float z0 = __ldg(&c.z_r2z_f[ir]), z1 = __ldg(&c.z_r2z_f[ir + 1]);
-  float red = (z0 + (z1 - z0) * fr) + dz;
-  float nu = 1420.40575177f / (1.f + red);
-  float mnu = 3e-6f * nu;
+  const int ir = (int)tr;
+  const float fr = tr - (float)ir;
+  const float z0 = __ldg(&c.z_r2z_f[ir]), z1 = __ldg(&c.z_r2z_f[ir + 1]);
+  const float zz = 1.f + ((z0 + (z1 - z0) * fr) + dz);
+  const float nu = 1420.40575177f / zz;
+  const float mnu = 1.2e-6f * nu + 4e-6f * (z1 - z0) * nu / zz;
   int inu;
   if (c.regular_nu) {
-    float t = (nu - (float)c.nu_min) * (float)c.inv_dnu;
-    if (near_int(t, mnu * (float)c.inv_dnu + 1e-6f * fabsf(t))) return false;
-    inu = (int)t;
+    const float t = (nu - (float)c.nu_min) * (float)c.inv_dnu;
+    if (near_int(t, mnu * (float)c.inv_dnu + 2.4e-7f * fabsf(t))) return false;
+    inu = (int)t;  // truncation, src/pixelize.c:369
   } else {
     const int nn = c.n_nu;
-    float e0 = __ldg(&ef[0]), en = __ldg(&ef[nn]);
+    const float e0 = ef[0], en = ef[nn];
     if (nu < e0) {
       if (e0 - nu < mnu) return false;
       inu = -1;
@@ -201,11 +210,11 @@ __device__ __forceinline__ bool key_fast(const DevCfg &c, const float *__restric
     } else {
       int lo = 0, hi = nn;
       while (hi - lo > 1) {
-        int mid = (lo + hi) >> 1;
-        if (nu >= __ldg(&ef[mid])) lo = mid;
+        const int mid = (lo + hi) >> 1;
+        if (nu >= ef[mid]) lo = mid;
         else hi = mid;
       }
-      if (nu - __ldg(&ef[lo]) < mnu || __ldg(&ef[lo + 1]) - nu < mnu) return false;
+      if (nu - ef[lo] < mnu || ef[lo + 1] - nu < mnu) return false;
       inu = lo;
     }
   }
@@ -213,49 +222,60 @@ __device__ __forceinline__ bool key_fast(const DevCfg &c, const float *__restric
     key = 0xFFFFFFFFu;
     return true;
   }
-  // pixel
-  const float fn = (float)c.nside;
-  float ir_ = 1.f / r;
-  float cth = z * ir_;
-  float za = fabsf(cth);
-  float rho = sqrtf(rho2);
-  float dcos = 2.5e-7f + epos * ir_;
-  if (fabsf(za - 0.6666667f) < 4.f * dcos + 1e-6f) return false;
-  float phi = atan2f(y, x);
-  float dtt = 0.6366198f * (4.8e-7f + 2.4e-7f * fabsf(phi) + epos / fmaxf(rho, 1e-30f));
-  float tt = phi * 0.63661977f;
-  if (tt < 0.f) tt += 4.f;
+  // ---- pixel (RING scheme)
+  const int nside = (int)c.nside;
+  const float fn = (float)nside;
+  const float cth = Z / R;
+  const float za = fabsf(cth);
+  const float dcos = 2.5e-7f;
+  if (fabsf(za - 0.6666667f) < 2.f * (dcos + 1e-7f)) return false;
+  // octant decomposition: phi = base*pi/4 + sgn*a, a in [0, pi/4]
+  const float ax = fabsf(X), ay = fabsf(Y);
+  const bool swap = ay > ax;
+  const float a = atan2f(swap ? ax : ay, swap ? ay : ax);
+  // tt = 2 phi / pi in [0,4): quadrant q (0..3) and in-quadrant part w in [0,1)
+  const float a2 = a * 0.63661977f;  // in [0, 0.5]
+  float w;
+  int q;
+  if (Y >= 0.f) {
+    if (X >= 0.f) { q = 0; w = swap ? 1.f - a2 : a2; }
+    else { q = 1; w = swap ? a2 : 1.f - a2; }
+  } else {
+    if (X < 0.f) { q = 2; w = swap ? 1.f - a2 : a2; }
+    else { q = 3; w = swap ? a2 : 1.f - a2; }
+  }
+  if (w >= 1.f) { w -= 1.f; q = (q + 1) & 3; }
+  const float dw = 0.63661977f * (1.8e-7f + 6e-8f) + 1.2e-7f;  // error of w
   const int npix = (int)c.npix;
   int pix;
   if (za <= 0.6666667f) {
-    float t1 = fn * (0.5f + tt), t2 = fn * cth * 0.75f;
-    float u1 = t1 - t2, u2 = t1 + t2;
-    float mu = 5.f * (fn * (dtt + 0.75f * dcos) + 2.4e-7f * (fabsf(t1) + fabsf(t2)) + 1e-6f);
-    if (near_int(u1, mu) || near_int(u2, mu)) return false;
-    int jp = (int)u1, jm = (int)u2;
-    int nside = (int)c.nside;
-    int ring = nside + 1 + jp - jm;
-    int kshift = 1 - (ring & 1);
+    // u1 = nside (0.5 + q + w) - 0.75 nside cth, u2 = ... + 0.75 nside cth
+    const float t2 = fn * cth * 0.75f;
+    const float v = fn * (0.5f + w);  // <= 1.5 nside
+    const float v1 = v - t2, v2 = v + t2;
+    const float mu = 2.f * (fn * (dw + 0.75f * dcos) + 3.f * 1.2e-7f * (1.5f * fn + 1.f));
+    if (near_int(v1, mu) || near_int(v2, mu)) return false;
+    const int jp = (int)floorf(v1) + q * nside, jm = (int)floorf(v2) + q * nside;
+    const int ring = nside + 1 + jp - jm;
+    const int kshift = 1 - (ring & 1);
     int ip = (jp + jm - nside + kshift + 1) / 2;
     ip %= 4 * nside;
     if (ip < 0) ip += 4 * nside;
     pix = 2 * nside * (nside - 1) + (ring - 1) * 4 * nside + ip;
   } else {
-    float ft = floorf(tt);
-    float tp = tt - ft;
-    // nside sqrt(3(1-|z|)) in the cancellation-free form nside (rho/r) / sqrt((1+|z|)/3)
-    float tmp = fn * (rho * ir_) * rsqrtf((1.f + za) * (1.f / 3.f));
-    float dtmp = tmp * (1e-6f + epos / fmaxf(rho, 1e-30f));
-    float u3 = tp * tmp, u4 = (1.f - tp) * tmp;
-    float mu = 5.f * (tmp * dtt + dtmp + 2.4e-7f * tmp + 1e-6f);
-    if (near_int(u3, mu) || near_int(u4, mu) || near_int(tp, 5.f * dtt + 1e-6f)) return false;
-    int jp = (int)u3, jm = (int)u4;
-    int ring = jp + jm + 1;
-    float u5 = tt * ring;
-    if (near_int(u5, 5.f * (ring * dtt + 4.8e-7f * u5 + 1e-6f))) return false;
-    int ip = (int)u5;
+    // polar caps: tmp = nside sqrt(3(1-|z|)) = nside (rho/R) / sqrt((1+|z|)/3)
+    const float rho = sqrtf(rho2);
+    const float tmp = fn * (rho / R) * rsqrtf((1.f + za) * (1.f / 3.f));
+    const float u3 = w * tmp, u4 = (1.f - w) * tmp;
+    const float mu = 2.f * (tmp * (dw + 6e-7f) + 2.f * 1.2e-7f * (tmp + 1.f));
+    if (near_int(u3, mu) || near_int(u4, mu) || w < 2.f * dw || 1.f - w < 2.f * dw) return false;
+    const int jp = (int)u3, jm = (int)u4;
+    const int ring = jp + jm + 1;
+    // ip = floor(tt * ring) = q ring + floor(w ring)
+    const float u5 = w * (float)ring;
+    if (near_int(u5, 2.f * ((float)ring * dw + 2.4e-7f * (u5 + 1.f)))) return false;
+    int ip = q * ring + (int)u5;
     ip %= 4 * ring;
-    if (ip < 0) ip += 4 * ring;
     pix = (cth > 0) ? 2 * ring * (ring - 1) + ip : npix - 2 * ring * (ring + 1) + ip;
   }
   key = (uint32_t)pix + (uint32_t)npix * (uint32_t)inu;
@@ -264,41 +284,66 @@ __device__ __forceinline__ bool key_fast(const DevCfg &c, const float *__restric
 
 // ---------------------------------------------------------------------------
 // projection: 10 sub-samples per cell -> maps[bin][pix] += mass/10
-// (src/pixelize.c:343-384).  Each block works through a contiguous chunk of
-// cells; samples whose FP32 key is not certain are queued in shared memory and
-// resolved with the exact FP64 key at the end of the chunk, so the FP64 units
-// run on full warps.
+// (src/pixelize.c:343-384).  One block per 8x8x8 tile of cells.  Each thread
+// merges runs of equal keys among its cell's sub-samples; the tile's
+// (key, mass) pairs are then accumulated per distinct key in a shared-memory
+// table, and each distinct key of the tile is added to the map once.  Samples
+// whose FP32 key is uncertain are queued and resolved with the FP64 key by the
+// whole block at the end of the tile.
 // ---------------------------------------------------------------------------
 constexpr int kProjThreads = 256;
-constexpr int kQueueCap = 2048;
+constexpr int kTile = 8;
+constexpr int kQueueCap = 1024;
+constexpr int kHash = 4096;
+constexpr int kProbe = 16;
+constexpr int kEdgesSmem = 516;
+
+__device__ __forceinline__ void tile_add(uint32_t *hkey, float *hval, float *maps, uint32_t key, float val)
+{
+  uint32_t h = (key * 2654435761u) >> 20;  // 12 bits
+#pragma unroll 1
+  for (int p = 0; p < kProbe; p++) {
+    const uint32_t s = (h + p) & (kHash - 1);
+    const uint32_t prev = atomicCAS(&hkey[s], 0xFFFFFFFFu, key);
+    if (prev == 0xFFFFFFFFu || prev == key) {
+      atomicAdd(&hval[s], val);
+      return;
+    }
+  }
+  atomicAdd(&maps[key], val);  // table crowded: straight to the map
+}
 
 template <bool FUSED>
-__global__ void __launch_bounds__(kProjThreads) project_kernel(DevCfg c, FastConst fc, const double *__restrict__ stats,
+__global__ void __launch_bounds__(kProjThreads) project_kernel(DevCfg c, FastConst f, const double *__restrict__ stats,
                                                                const float *__restrict__ a, const float *__restrict__ b,
-                                                               float *__restrict__ maps, long cells_per_block,
-                                                               int *__restrict__ counters)
+                                                               float *__restrict__ maps, int *__restrict__ counters)
 {
+  __shared__ uint32_t hkey[kHash];
+  __shared__ float hval[kHash];
   __shared__ uint32_t q_cell[kQueueCap];
   __shared__ float q_val[kQueueCap], q_dz[kQueueCap];
   __shared__ uint8_t q_sub[kQueueCap];
+  __shared__ float sef[kEdgesSmem];
   __shared__ int q_n;
-  __shared__ float sef[260];
-  if (threadIdx.x == 0) q_n = 0;
-  if (!c.regular_nu)
-    for (int i = threadIdx.x; i <= c.n_nu && i < 260; i += blockDim.x) sef[i] = (float)c.nu_edges[i];
+  const int tid = threadIdx.x;
+  for (int i = tid; i < kHash; i += kProjThreads) {
+    hkey[i] = 0xFFFFFFFFu;
+    hval[i] = 0.f;
+  }
+  const bool smem_edges = !c.regular_nu && c.n_nu < kEdgesSmem;
+  if (smem_edges)
+    for (int i = tid; i <= c.n_nu; i += kProjThreads) sef[i] = c.nu_edges_f[i];
+  if (tid == 0) q_n = 0;
   __syncthreads();
-  const float *ef = c.n_nu < 260 ? sef : c.nu_edges_f;
-  const int n = c.n;
-  const long total = (long)n * n * n;
+  const float *ef = smem_edges ? sef : c.nu_edges_f;
+  const int n = c.n, nt = n / kTile;
+  const int bx = blockIdx.x % nt, by = (blockIdx.x / nt) % nt, bz = blockIdx.x / (nt * nt);
   const float sigma2 = FUSED ? (float)stats[1] : 0.f;
-  const float epos = 4.f * 6e-8f * (0.5f * (float)c.l_box) * 1.7320508f;
-  const long c0 = blockIdx.x * cells_per_block;
-  const long c1 = min(total, c0 + cells_per_block);
   int nfall = 0;
-  for (long i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
-    const int ix = (int)(i % n);
-    const long rest = i / n;
-    const int iy = (int)(rest % n), iz = (int)(rest / n);
+#pragma unroll 1
+  for (int k = 0; k < 2; k++) {
+    const int ix = bx * kTile + (tid & 7), iy = by * kTile + ((tid >> 3) & 7), iz = bz * kTile + (tid >> 6) + 4 * k;
+    const long i = ((long)iz * n + iy) * n + ix;
     float mass, dz;
     if (FUSED) {
       CellHI h = cell_hi(c, sigma2, ix, iy, iz, a[i], b[i]);
@@ -309,41 +354,51 @@ __global__ void __launch_bounds__(kProjThreads) project_kernel(DevCfg c, FastCon
       dz = b[i];
     }
     const float msub = mass / 10.f;  // src/pixelize.c:356
-    const float x0 = c.dxf * (ix + 0.5f) - c.pos_obsf, y0 = c.dxf * (iy + 0.5f) - c.pos_obsf,
-                z0 = c.dxf * (iz + 0.5f) - c.pos_obsf;
-#pragma unroll 2
+    const float Xc = (float)ix - f.half_n, Yc = (float)iy - f.half_n, Zc = (float)iz - f.half_n;
+    uint32_t cur = 0xFFFFFFFFu;
+    float acc = 0.f;
+#pragma unroll 1
     for (int is = 0; is < kNSUB; is++) {
       uint32_t key;
-      bool ok = key_fast(c, ef, x0 + fc.xsf[is], y0 + fc.ysf[is], z0 + fc.zsf[is], dz, epos, key);
-      if (ok) {
-        if (key != 0xFFFFFFFFu) atomicAdd(&maps[key], msub);
-      } else {
-        int slot = atomicAdd(&q_n, 1);
+      if (!key_fast(c, f, ef, Xc + f.xsp[is], Yc + f.ysp[is], Zc + f.zsp[is], dz, key)) {
+        const int slot = atomicAdd(&q_n, 1);
         if (slot < kQueueCap) {
-          q_cell[slot] = (uint32_t)(i - c0);
+          q_cell[slot] = (uint32_t)(tid + kProjThreads * k);
           q_sub[slot] = (uint8_t)is;
           q_val[slot] = msub;
           q_dz[slot] = dz;
         } else {
           key = key_exact(c, ix, iy, iz, is, dz);
-          if (key != 0xFFFFFFFFu) atomicAdd(&maps[key], msub);
+          if (key != 0xFFFFFFFFu) tile_add(hkey, hval, maps, key, msub);
         }
         nfall++;
+        continue;
+      }
+      if (key == 0xFFFFFFFFu) continue;
+      if (key == cur) {
+        acc += msub;
+      } else {
+        if (cur != 0xFFFFFFFFu) tile_add(hkey, hval, maps, cur, acc);
+        cur = key;
+        acc = msub;
       }
     }
+    if (cur != 0xFFFFFFFFu) tile_add(hkey, hval, maps, cur, acc);
   }
   __syncthreads();
   const int qn = min(q_n, kQueueCap);
-  for (int k = threadIdx.x; k < qn; k += blockDim.x) {
-    long i = c0 + q_cell[k];
-    const int ix = (int)(i % n);
-    const long rest = i / n;
-    uint32_t key = key_exact(c, ix, (int)(rest % n), (int)(rest / n), q_sub[k], q_dz[k]);
-    if (key != 0xFFFFFFFFu) atomicAdd(&maps[key], q_val[k]);
+  for (int j = tid; j < qn; j += kProjThreads) {
+    const int lc = (int)q_cell[j], k = lc / kProjThreads, t = lc % kProjThreads;
+    const int ix = bx * kTile + (t & 7), iy = by * kTile + ((t >> 3) & 7), iz = bz * kTile + (t >> 6) + 4 * k;
+    const uint32_t key = key_exact(c, ix, iy, iz, q_sub[j], q_dz[j]);
+    if (key != 0xFFFFFFFFu) tile_add(hkey, hval, maps, key, q_val[j]);
   }
+  __syncthreads();
+  for (int s = tid; s < kHash; s += kProjThreads)
+    if (hkey[s] != 0xFFFFFFFFu) atomicAdd(&maps[hkey[s]], hval[s]);
   if (counters) {
     for (int o = 16; o > 0; o >>= 1) nfall += __shfl_xor_sync(0xffffffffu, nfall, o);
-    if ((threadIdx.x & 31) == 0 && nfall) atomicAdd(&counters[0], nfall);
+    if ((tid & 31) == 0 && nfall) atomicAdd(&counters[0], nfall);
   }
 }
 
@@ -356,27 +411,30 @@ __global__ void scale_maps_kernel(DevCfg c, float *maps)
 }
 
 // per-sample keys (validation): exact FP64, or fast FP32 with FP64 fallback
-__global__ void sample_keys_kernel(DevCfg c, FastConst fc, const float *__restrict__ dzg, uint32_t *keys, int exact)
+__global__ void sample_keys_kernel(DevCfg c, FastConst f, const float *__restrict__ dzg, uint32_t *keys, int exact,
+                                   int *counters)
 {
   const int n = c.n;
   const long total = (long)n * n * n;
-  const float epos = 4.f * 6e-8f * (0.5f * (float)c.l_box) * 1.7320508f;
+  int nfall = 0;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
     const int ix = (int)(i % n);
     const long rest = i / n;
     const int iy = (int)(rest % n), iz = (int)(rest / n);
     const float dz = dzg[i];
-    const float x0 = c.dxf * (ix + 0.5f) - c.pos_obsf, y0 = c.dxf * (iy + 0.5f) - c.pos_obsf,
-                z0 = c.dxf * (iz + 0.5f) - c.pos_obsf;
+    const float Xc = (float)ix - f.half_n, Yc = (float)iy - f.half_n, Zc = (float)iz - f.half_n;
     for (int is = 0; is < kNSUB; is++) {
       uint32_t key;
       bool ok = false;
-      if (!exact)
-        ok = key_fast(c, c.nu_edges_f, x0 + fc.xsf[is], y0 + fc.ysf[is], z0 + fc.zsf[is], dz, epos, key);
-      if (!ok) key = key_exact(c, ix, iy, iz, is, dz);
+      if (!exact) ok = key_fast(c, f, c.nu_edges_f, Xc + f.xsp[is], Yc + f.ysp[is], Zc + f.zsp[is], dz, key);
+      if (!ok) {
+        key = key_exact(c, ix, iy, iz, is, dz);
+        nfall++;
+      }
       keys[i * kNSUB + is] = key;
     }
   }
+  if (counters) atomicAdd(&counters[1], nfall);
 }
 
 // ---------------------------------------------------------------------------
@@ -404,22 +462,24 @@ static FastConst fast_const(const DevCfg &c)
 {
   FastConst f;
   for (int i = 0; i < kNSUB; i++) {
-    f.xsf[i] = (float)c.xs[i];
-    f.ysf[i] = (float)c.ys[i];
-    f.zsf[i] = (float)c.zs[i];
+    f.xsp[i] = (float)(0.5 + c.xs[i] / c.dx);
+    f.ysp[i] = (float)(0.5 + c.ys[i] / c.dx);
+    f.zsp[i] = (float)(0.5 + c.zs[i] / c.dx);
   }
+  f.idr_cell = (float)(c.glob_idr * c.dx);
+  f.half_n = (float)(c.n / 2);
   return f;
 }
 
 cudaError_t project(const DevCfg &c, const double *stats, const float *a, const float *b, int fused, float *maps,
                     int *counters, cudaStream_t st)
 {
-  long total = (long)c.n * c.n * c.n;
-  long cpb = 4096;
-  long blocks = (total + cpb - 1) / cpb;
-  FastConst fc = fast_const(c);
-  if (fused) project_kernel<true><<<(unsigned)blocks, kProjThreads, 0, st>>>(c, fc, stats, a, b, maps, cpb, counters);
-  else project_kernel<false><<<(unsigned)blocks, kProjThreads, 0, st>>>(c, fc, stats, a, b, maps, cpb, counters);
+  if (c.n % kTile) return cudaErrorInvalidValue;
+  const long nt = c.n / kTile;
+  const unsigned blocks = (unsigned)(nt * nt * nt);
+  FastConst f = fast_const(c);
+  if (fused) project_kernel<true><<<blocks, kProjThreads, 0, st>>>(c, f, stats, a, b, maps, counters);
+  else project_kernel<false><<<blocks, kProjThreads, 0, st>>>(c, f, stats, a, b, maps, counters);
   return cudaGetLastError();
 }
 
@@ -429,10 +489,10 @@ cudaError_t scale_maps(const DevCfg &c, float *maps, cudaStream_t st)
   return cudaGetLastError();
 }
 
-cudaError_t sample_keys(const DevCfg &c, const float *dz, uint32_t *keys, int exact, cudaStream_t st)
+cudaError_t sample_keys(const DevCfg &c, const float *dz, uint32_t *keys, int exact, int *counters, cudaStream_t st)
 {
   long total = (long)c.n * c.n * c.n;
-  sample_keys_kernel<<<grid_for(total, 128), 128, 0, st>>>(c, fast_const(c), dz, keys, exact);
+  sample_keys_kernel<<<grid_for(total, 128), 128, 0, st>>>(c, fast_const(c), dz, keys, exact, counters);
   return cudaGetLastError();
 }
 

@@ -245,14 +245,14 @@ class GetHI:
         return out
 
     KERNEL_CLASSES = ("zpass", "ypass", "xpass", "xpass_vel", "nyq", "sigma", "fd_vel", "get_hi", "project",
-                      "scale")
+                      "scale", "zpass_raw")
 
     def profile(self, on=True):
         _check(lib().gethi_gpu_profile(self._ctx, int(on)))
 
     def kernel_times(self):
-        ms = np.zeros(10)
-        cnt = np.zeros(10, np.int64)
+        ms = np.zeros(len(self.KERNEL_CLASSES))
+        cnt = np.zeros(len(self.KERNEL_CLASSES), np.int64)
         launches = np.zeros(1, np.int64)
         lib().gethi_gpu_kernel_times(self._ctx, _ptr(ms), _ptr(cnt), _ptr(launches))
         return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.KERNEL_CLASSES)}, int(launches[0])

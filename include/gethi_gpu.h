@@ -134,7 +134,7 @@ int gethi_gpu_stage_times(const gethi_ctx *ctx, float *ms, int n);
 
 /* ---- measurement ---- */
 /* kernel classes timed when profiling is on (events around each launch) */
-#define GETHI_KC_ZPASS 0      /* Z pass with on-the-fly modes (main block) */
+#define GETHI_KC_ZPASS 0      /* Z pass drawing the modes on the fly (main block) */
 #define GETHI_KC_YPASS 1      /* Y pass (main block) */
 #define GETHI_KC_XPASS 2      /* X pass, real field written in place (+ sigma partial sums) */
 #define GETHI_KC_XPASS_VEL 3  /* X pass accumulating the radial velocity */
@@ -144,7 +144,8 @@ int gethi_gpu_stage_times(const gethi_ctx *ctx, float *ms, int n);
 #define GETHI_KC_GETHI 7
 #define GETHI_KC_PROJECT 8
 #define GETHI_KC_SCALE 9
-#define GETHI_NKCLASS 10
+#define GETHI_KC_ZPASS_RAW 10 /* Z pass of a velocity field from the stored modes */
+#define GETHI_NKCLASS 11
 int gethi_gpu_profile(gethi_ctx *ctx, int on);
 /* accumulated ms and launch counts per class since profiling was switched on,
  * and the total number of kernels this context has launched */

@@ -170,3 +170,54 @@ def test_production_run_vs_oracle(gh, vmode):
     assert rel_l2(maps, ref) < 1e-4
     close = np.isclose(maps, ref, rtol=1e-5, atol=1e-6 * np.abs(ref).max())
     assert close.mean() > 0.995
+
+
+def synthetic_params(gh, **kw):
+    nu21 = 1420.40575177
+    base = dict(omega_M=0.315, omega_L=0.685, omega_B=0.049, h=0.67, w=-1.0, ns=0.96, sigma_8=0.83,
+                pk_filename=os.path.join(GOLDEN, "pk_eh_nowiggle.txt"), frequencies_filename="",
+                nu_min=nu21 / 3.0, nu_max=nu21 / 1.3, n_nu=150, seed=11)
+    base.update(kw)
+    return gh.make_params(**base)
+
+
+def test_fast_keys_certified_high_nside(gh):
+    """FP32 keys with margins == FP64 keys on 21M samples at Nside=512, random dz."""
+    n = 128
+    ctx = gh.GetHI(synthetic_params(gh, n_grid=n, n_side=512, l_box=2000.0))
+    rng = np.random.default_rng(5)
+    mass = rng.lognormal(0, 1, (n, n, n)).astype(np.float32)
+    dz = rng.normal(0, 3e-3, (n, n, n)).astype(np.float32)
+    ctx.upload_grids(mass, dz, stage=2)
+    exact = ctx.sample_keys(exact=True)
+    fast = ctx.sample_keys(exact=False)
+    ctx.free()
+    assert np.count_nonzero(exact != 0xFFFFFFFF) > 0.5 * exact.size
+    np.testing.assert_array_equal(fast, exact)
+
+
+def test_projection_many_keys_per_tile(gh):
+    """Small box, high Nside: every sample of a tile is its own pixel, so the
+    per-tile key table overflows; maps must still match the oracle."""
+    from oracle import orc
+    n, nside = 32, 1024
+    nu21 = 1420.40575177
+    p = synthetic_params(gh, n_grid=n, n_side=nside, l_box=300.0, nu_min=nu21 / 1.12, nu_max=nu21 / 1.02, n_nu=4)
+    ctx = gh.GetHI(p)
+    rng = np.random.default_rng(9)
+    mass = rng.lognormal(0, 1, (n, n, n)).astype(np.float32)
+    dz = rng.normal(0, 1e-3, (n, n, n)).astype(np.float32)
+    ctx.upload_grids(mass, dz, stage=2)
+    maps = ctx.mk_T_maps()
+    ctx.free()
+    k, pk = orc.load_pk(os.path.join(GOLDEN, "pk_eh_nowiggle.txt"))
+    o = orc.Oracle(dict(OmegaM=0.315, OmegaL=0.685, OmegaB=0.049, hhub=0.67, weos=-1.0, n_scal=0.96, sig8=0.83,
+                        n_grid=n, n_side=nside, seed=11, regular_nu=1, nu_min=p.nu_min, nu_max=p.nu_max, n_nu=4,
+                        l_box_override=300.0), k, pk)
+    pad = np.zeros((n, n, 2 * (n // 2 + 1)), np.float32)
+    padz = np.zeros_like(pad)
+    pad[:, :, :n] = mass
+    padz[:, :, :n] = dz
+    ref = o.mk_T_maps(pad, padz)
+    assert np.count_nonzero(ref) > 10000
+    np.testing.assert_allclose(maps, ref, rtol=1e-5, atol=1e-6 * np.abs(ref).max())
