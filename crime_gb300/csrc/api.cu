@@ -51,6 +51,8 @@ struct gethi_ctx {
   long kcount[GETHI_NKCLASS] = {};
   long launches = 0;
   void *staging = nullptr;  // pinned host copy of the per-realisation inputs
+  void *fq = nullptr;       // queue of samples whose FP32 key is uncertain
+  long fq_cap = 0;
 };
 
 namespace {
@@ -335,6 +337,7 @@ extern "C" void gethi_gpu_free(gethi_ctx *c)
     if (ev) cudaEventDestroy(ev);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   if (c->staging) cudaFreeHost(c->staging);
+  if (c->fq) cudaFree(c->fq);
   delete c;
 }
 
@@ -438,10 +441,20 @@ static int maps_common(gethi_ctx *c, float *maps_out, int fused)
   const long npix = 12 * s.p.n_side * s.p.n_side;
   CK(cudaMemsetAsync(c->maps, 0, sizeof(float) * npix * s.p.n_nu, c->stream));
   CK(cudaMemsetAsync(c->counters, 0, sizeof(int) * 16, c->stream));
+  if (!c->fq) {
+    long cap = fallback_queue_capacity((int)s.p.n_grid);
+    int rc = dalloc(reinterpret_cast<char **>(&c->fq), (size_t)cap * fallback_entry_bytes());
+    if (rc) return rc;
+    c->fq_cap = cap;
+  }
   {
     KTimer t(c, KC_PROJECT);
     CK(project(c->cfg, c->stats, reinterpret_cast<const float *>(c->main), c->vr, fused, c->maps, c->counters,
-               c->stream));
+               c->fq, c->fq_cap, c->stream));
+  }
+  {
+    KTimer t(c, KC_FIXUP);
+    CK(fixup(c->cfg, c->fq, c->counters, c->fq_cap, c->maps, c->stream));
   }
   {
     KTimer t(c, KC_SCALE);

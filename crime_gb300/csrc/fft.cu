@@ -53,9 +53,11 @@ __device__ __forceinline__ float2 philox_mode(const DevCfg &c, int ii, int jj, i
   uint64_t id = (uint64_t)kk + (uint64_t)(c.m + 1) * ((uint64_t)jj + (uint64_t)c.n * ii);
   uint4 o = philox4x32_10(make_uint4((uint32_t)id, (uint32_t)(id >> 32), 0u, 0u), make_uint2(c.seed, 0x4352494Du));
   float u = (float)o.x * 2.3283064365386963e-10f;
-  uint32_t mw = 0u - o.y;
-  float w = mw ? (float)mw * 2.3283064365386963e-10f : 1.0f;
-  float amp = sqrtf(-sigma2 * logf(w));
+  // ln(1 - u2), u2 = out.y/2^32: log1p keeps the relative accuracy for small u2,
+  // the direct log of the exact remainder 2^32 - out.y for u2 >= 1/2
+  float lnw = o.y < 0x80000000u ? log1pf(-(float)o.y * 2.3283064365386963e-10f)
+                                : logf((float)(0u - o.y) * 2.3283064365386963e-10f);
+  float amp = sqrtf(-sigma2 * lnw);
   float s, co;
   sincospif(2.f * u, &s, &co);
   return make_float2(amp * co, amp * s);

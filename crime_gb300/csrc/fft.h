@@ -8,7 +8,7 @@ namespace gethi {
 
 enum KernelClass {
   KC_ZPASS = 0, KC_YPASS, KC_XPASS, KC_XPASS_VEL, KC_NYQ, KC_SIGMA, KC_FDVEL, KC_GETHI, KC_PROJECT, KC_SCALE,
-  KC_ZPASS_RAW
+  KC_ZPASS_RAW, KC_FIXUP
 };
 
 enum FieldKind { FIELD_DENS = 0, FIELD_VPOT = 1, FIELD_VX = 2, FIELD_VY = 3, FIELD_VZ = 4 };
@@ -32,8 +32,12 @@ cudaError_t gen_modes(const DevCfg &c, float2 *out, int kind, cudaStream_t st);
 // stages.cu
 cudaError_t radial_velocity_fd(const DevCfg &c, const float *vpot, float *rvel, cudaStream_t st);
 cudaError_t get_hi(const DevCfg &c, const double *stats, float *dens, float *rvel, cudaStream_t st);
+// counters: [0] uncertain samples, [1] sample_keys fallbacks, [2..3] 64-bit fallback-queue length
 cudaError_t project(const DevCfg &c, const double *stats, const float *a, const float *b, int fused, float *maps,
-                    int *err, cudaStream_t st);
+                    int *counters, void *fq, long fq_cap, cudaStream_t st);
+cudaError_t fixup(const DevCfg &c, const void *fq, const int *counters, long fq_cap, float *maps, cudaStream_t st);
+long fallback_queue_capacity(int n);
+size_t fallback_entry_bytes();
 cudaError_t scale_maps(const DevCfg &c, float *maps, cudaStream_t st);
 cudaError_t sample_keys(const DevCfg &c, const float *dz, uint32_t *keys, int exact, int *counters,
                         cudaStream_t st);

@@ -176,27 +176,54 @@ struct FastConst {
   float xsp[kNSUB], ysp[kNSUB], zsp[kNSUB];  // 0.5 + offset/dx
   float idr_cell;                             // glob_idr * dx
   float half_n;                               // n/2
+  float nu_min, inv_dnu;                      // regular table
 };
 
 __device__ __forceinline__ bool near_int(float u, float m) { return fabsf(u - rintf(u)) < m; }
 
+// atan(t) for t in [0,1] as t P(t^2), P of degree 8 (coefficients from a
+// weighted least-squares fit toward minimax); evaluated in FP32 with FMAs the
+// error stays below 8.6e-8 (checked on 2e6 points against FP64 atan).
+__device__ __forceinline__ float atan01(float t)
+{
+  const float s = t * t;
+  float p = 0.0024567206855863333f;
+  p = fmaf(p, s, -0.014401344582438469f);
+  p = fmaf(p, s, 0.03978120908141136f);
+  p = fmaf(p, s, -0.07234856486320496f);
+  p = fmaf(p, s, 0.10498946160078049f);
+  p = fmaf(p, s, -0.14161229133605957f);
+  p = fmaf(p, s, 0.19985906779766083f);
+  p = fmaf(p, s, -0.33332598209381104f);
+  p = fmaf(p, s, 0.9999998807907104f);
+  return p * t;
+}
+
+// Error bounds used below (absolute unless noted), with a factor 2 on top:
+//   position X,Y,Z: 6e-8 relative; R^2 (3 FMAs): 2.4e-7 rel; rsqrt.approx: 1.3e-7 rel
+//   R = R^2 rsqrt(R^2): 3.1e-7 rel; cos(theta) = Z rsqrt(R^2): 3.7e-7
+//   1+z from the FP32 table: |z1-z0| tr 3.7e-7 + 4 ulp(1+z); nu (approximate division): +2.7e-7 rel
+//   octant angle: atan01 8.6e-8 + ratio (2 ulp) 9e-8; w = 2a/pi or 1-2a/pi: 2.05e-7
+//   floor arguments: nside (dw + 6e-8 + 0.75 dcos) + 4 half-ulps at 1.5 nside
 __device__ __forceinline__ bool key_fast(const DevCfg &c, const FastConst &f, const float *ef, float X, float Y,
                                          float Z, float dz, uint32_t &key)
 {
-  const float rho2 = X * X + Y * Y;
-  const float R = sqrtf(rho2 + Z * Z);
+  const float rho2 = fmaf(Y, Y, X * X);
+  const float R2 = fmaf(Z, Z, rho2);
+  const float iR = rsqrtf(R2);
+  const float R = R2 * iR;
   const float tr = R * f.idr_cell;
-  if (!(tr < (float)(kNZ - 2))) return false;
+  if (!(tr < (float)(kNZ - 2)) || !(rho2 > 0.f)) return false;
   const int ir = (int)tr;
   const float fr = tr - (float)ir;
   const float z0 = __ldg(&c.z_r2z_f[ir]), z1 = __ldg(&c.z_r2z_f[ir + 1]);
-  const float zz = 1.f + ((z0 + (z1 - z0) * fr) + dz);
-  const float nu = 1420.40575177f / zz;
-  const float mnu = 1.2e-6f * nu + 4e-6f * (z1 - z0) * nu / zz;
+  const float zz = 1.f + (fmaf(z1 - z0, fr, z0) + dz);
+  const float nu = __fdividef(1420.40575177f, zz);
+  const float mnu = 2.f * nu * (__fdividef(fabsf(z1 - z0) * tr * 3.7e-7f, zz) + 4.8e-7f + 2.7e-7f);
   int inu;
   if (c.regular_nu) {
-    const float t = (nu - (float)c.nu_min) * (float)c.inv_dnu;
-    if (near_int(t, mnu * (float)c.inv_dnu + 2.4e-7f * fabsf(t))) return false;
+    const float t = (nu - f.nu_min) * f.inv_dnu;
+    if (near_int(t, (mnu + 1.2e-7f * nu) * f.inv_dnu + 4e-7f * fabsf(t) + 1e-6f)) return false;
     inu = (int)t;  // truncation, src/pixelize.c:369
   } else {
     const int nn = c.n_nu;
@@ -225,57 +252,50 @@ __device__ __forceinline__ bool key_fast(const DevCfg &c, const FastConst &f, co
   // ---- pixel (RING scheme)
   const int nside = (int)c.nside;
   const float fn = (float)nside;
-  const float cth = Z / R;
+  const float cth = Z * iR;
   const float za = fabsf(cth);
-  const float dcos = 2.5e-7f;
-  if (fabsf(za - 0.6666667f) < 2.f * (dcos + 1e-7f)) return false;
-  // octant decomposition: phi = base*pi/4 + sgn*a, a in [0, pi/4]
+  const float dcos = 3.7e-7f;
+  if (fabsf(za - 0.6666667f) < 2.f * dcos + 6e-8f) return false;
+  // octant decomposition: a = atan(min/max) in [0, pi/4]; tt = 2 phi/pi = q + w
   const float ax = fabsf(X), ay = fabsf(Y);
   const bool swap = ay > ax;
-  const float a = atan2f(swap ? ax : ay, swap ? ay : ax);
-  // tt = 2 phi / pi in [0,4): quadrant q (0..3) and in-quadrant part w in [0,1)
-  const float a2 = a * 0.63661977f;  // in [0, 0.5]
-  float w;
-  int q;
-  if (Y >= 0.f) {
-    if (X >= 0.f) { q = 0; w = swap ? 1.f - a2 : a2; }
-    else { q = 1; w = swap ? a2 : 1.f - a2; }
-  } else {
-    if (X < 0.f) { q = 2; w = swap ? 1.f - a2 : a2; }
-    else { q = 3; w = swap ? a2 : 1.f - a2; }
+  const float a2 = atan01(__fdividef(fminf(ax, ay), fmaxf(ax, ay))) * 0.63661977f;  // in [0, 0.5]
+  const bool upper = Y >= 0.f, right = X >= 0.f;
+  int q = upper ? (right ? 0 : 1) : (right ? 3 : 2);
+  // w = a2 when the octant runs counter-clockwise from the quadrant start, else 1 - a2
+  const bool ccw = (q == 0 || q == 2) ? !swap : swap;
+  float w = ccw ? a2 : 1.f - a2;
+  if (w >= 1.f) {
+    w -= 1.f;
+    q = (q + 1) & 3;
   }
-  if (w >= 1.f) { w -= 1.f; q = (q + 1) & 3; }
-  const float dw = 0.63661977f * (1.8e-7f + 6e-8f) + 1.2e-7f;  // error of w
+  const float dw = 2.05e-7f;
   const int npix = (int)c.npix;
   int pix;
   if (za <= 0.6666667f) {
-    // u1 = nside (0.5 + q + w) - 0.75 nside cth, u2 = ... + 0.75 nside cth
     const float t2 = fn * cth * 0.75f;
-    const float v = fn * (0.5f + w);  // <= 1.5 nside
+    const float v = fn * (0.5f + w);
     const float v1 = v - t2, v2 = v + t2;
-    const float mu = 2.f * (fn * (dw + 0.75f * dcos) + 3.f * 1.2e-7f * (1.5f * fn + 1.f));
+    const float mu = 2.f * (fn * (dw + 6e-8f + 0.75f * dcos) + 2.f * 1.2e-7f * (1.5f * fn + 1.f));
     if (near_int(v1, mu) || near_int(v2, mu)) return false;
     const int jp = (int)floorf(v1) + q * nside, jm = (int)floorf(v2) + q * nside;
     const int ring = nside + 1 + jp - jm;
-    const int kshift = 1 - (ring & 1);
-    int ip = (jp + jm - nside + kshift + 1) / 2;
-    ip %= 4 * nside;
-    if (ip < 0) ip += 4 * nside;
+    const int num = jp + jm - nside + (1 - (ring & 1)) + 1;  // >= -1
+    int ip = (num + (num < 0)) >> 1;                          // C division by 2 (toward zero)
+    if (ip >= 4 * nside) ip -= 4 * nside;
     pix = 2 * nside * (nside - 1) + (ring - 1) * 4 * nside + ip;
   } else {
-    // polar caps: tmp = nside sqrt(3(1-|z|)) = nside (rho/R) / sqrt((1+|z|)/3)
-    const float rho = sqrtf(rho2);
-    const float tmp = fn * (rho / R) * rsqrtf((1.f + za) * (1.f / 3.f));
+    // polar caps: nside sqrt(3(1-|z|)) = nside (rho/R) / sqrt((1+|z|)/3)
+    const float st = rho2 * rsqrtf(rho2) * iR;
+    const float tmp = fn * st * rsqrtf((1.f + za) * (1.f / 3.f));
     const float u3 = w * tmp, u4 = (1.f - w) * tmp;
-    const float mu = 2.f * (tmp * (dw + 6e-7f) + 2.f * 1.2e-7f * (tmp + 1.f));
+    const float mu = 2.f * (tmp * (dw + 1e-6f) + 2.f * 1.2e-7f * (tmp + 1.f));
     if (near_int(u3, mu) || near_int(u4, mu) || w < 2.f * dw || 1.f - w < 2.f * dw) return false;
     const int jp = (int)u3, jm = (int)u4;
     const int ring = jp + jm + 1;
-    // ip = floor(tt * ring) = q ring + floor(w ring)
     const float u5 = w * (float)ring;
     if (near_int(u5, 2.f * ((float)ring * dw + 2.4e-7f * (u5 + 1.f)))) return false;
-    int ip = q * ring + (int)u5;
-    ip %= 4 * ring;
+    const int ip = q * ring + (int)u5;  // floor(tt ring) < 4 ring
     pix = (cth > 0) ? 2 * ring * (ring - 1) + ip : npix - 2 * ring * (ring + 1) + ip;
   }
   key = (uint32_t)pix + (uint32_t)npix * (uint32_t)inu;
@@ -313,10 +333,17 @@ __device__ __forceinline__ void tile_add(uint32_t *hkey, float *hval, float *map
   atomicAdd(&maps[key], val);  // table crowded: straight to the map
 }
 
+// one uncertain sample: tile, (local cell << 4 | sub-sample), mass/10, dz
+struct FallbackEntry {
+  uint32_t tile, sub;
+  float msub, dz;
+};
+
 template <bool FUSED>
 __global__ void __launch_bounds__(kProjThreads) project_kernel(DevCfg c, FastConst f, const double *__restrict__ stats,
                                                                const float *__restrict__ a, const float *__restrict__ b,
-                                                               float *__restrict__ maps, int *__restrict__ counters)
+                                                               float *__restrict__ maps, int *__restrict__ counters,
+                                                               FallbackEntry *__restrict__ fq, long fq_cap)
 {
   __shared__ uint32_t hkey[kHash];
   __shared__ float hval[kHash];
@@ -386,8 +413,23 @@ __global__ void __launch_bounds__(kProjThreads) project_kernel(DevCfg c, FastCon
     if (cur != 0xFFFFFFFFu) tile_add(hkey, hval, maps, cur, acc);
   }
   __syncthreads();
+  // hand the uncertain samples to the global queue (resolved by fixup_kernel on
+  // full warps); whatever does not fit is resolved here
+  __shared__ long q_base;
   const int qn = min(q_n, kQueueCap);
+  if (tid == 0) q_base = qn ? (long)atomicAdd((unsigned long long *)&counters[2], (unsigned long long)qn) : 0;
+  __syncthreads();
   for (int j = tid; j < qn; j += kProjThreads) {
+    const long g = q_base + j;
+    if (g < fq_cap) {
+      FallbackEntry e;
+      e.tile = blockIdx.x;
+      e.sub = (q_cell[j] << 4) | q_sub[j];
+      e.msub = q_val[j];
+      e.dz = q_dz[j];
+      fq[g] = e;
+      continue;
+    }
     const int lc = (int)q_cell[j], k = lc / kProjThreads, t = lc % kProjThreads;
     const int ix = bx * kTile + (t & 7), iy = by * kTile + ((t >> 3) & 7), iz = bz * kTile + (t >> 6) + 4 * k;
     const uint32_t key = key_exact(c, ix, iy, iz, q_sub[j], q_dz[j]);
@@ -399,6 +441,22 @@ __global__ void __launch_bounds__(kProjThreads) project_kernel(DevCfg c, FastCon
   if (counters) {
     for (int o = 16; o > 0; o >>= 1) nfall += __shfl_xor_sync(0xffffffffu, nfall, o);
     if ((tid & 31) == 0 && nfall) atomicAdd(&counters[0], nfall);
+  }
+}
+
+// FP64 keys of the queued uncertain samples (full warps on the FP64 pipe)
+__global__ void fixup_kernel(DevCfg c, const FallbackEntry *__restrict__ fq, const int *__restrict__ counters,
+                             long fq_cap, float *__restrict__ maps)
+{
+  const long cnt = min((long)*reinterpret_cast<const unsigned long long *>(&counters[2]), fq_cap);
+  const int nt = c.n / kTile;
+  for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < cnt; j += (long)gridDim.x * blockDim.x) {
+    const FallbackEntry e = fq[j];
+    const int bx = e.tile % nt, by = (e.tile / nt) % nt, bz = e.tile / (nt * nt);
+    const int lc = (int)(e.sub >> 4), is = (int)(e.sub & 15), k = lc / kProjThreads, t = lc % kProjThreads;
+    const int ix = bx * kTile + (t & 7), iy = by * kTile + ((t >> 3) & 7), iz = bz * kTile + (t >> 6) + 4 * k;
+    const uint32_t key = key_exact(c, ix, iy, iz, is, e.dz);
+    if (key != 0xFFFFFFFFu) atomicAdd(&maps[key], e.msub);
   }
 }
 
@@ -468,18 +526,34 @@ static FastConst fast_const(const DevCfg &c)
   }
   f.idr_cell = (float)(c.glob_idr * c.dx);
   f.half_n = (float)(c.n / 2);
+  f.nu_min = (float)c.nu_min;
+  f.inv_dnu = (float)c.inv_dnu;
   return f;
 }
 
+long fallback_queue_capacity(int n)
+{
+  long cap = (long)n * n * n * kNSUB / 128;
+  return cap < (1L << 20) ? (1L << 20) : cap;
+}
+size_t fallback_entry_bytes() { return sizeof(FallbackEntry); }
+
 cudaError_t project(const DevCfg &c, const double *stats, const float *a, const float *b, int fused, float *maps,
-                    int *counters, cudaStream_t st)
+                    int *counters, void *fq, long fq_cap, cudaStream_t st)
 {
   if (c.n % kTile) return cudaErrorInvalidValue;
   const long nt = c.n / kTile;
   const unsigned blocks = (unsigned)(nt * nt * nt);
   FastConst f = fast_const(c);
-  if (fused) project_kernel<true><<<blocks, kProjThreads, 0, st>>>(c, f, stats, a, b, maps, counters);
-  else project_kernel<false><<<blocks, kProjThreads, 0, st>>>(c, f, stats, a, b, maps, counters);
+  FallbackEntry *q = reinterpret_cast<FallbackEntry *>(fq);
+  if (fused) project_kernel<true><<<blocks, kProjThreads, 0, st>>>(c, f, stats, a, b, maps, counters, q, fq_cap);
+  else project_kernel<false><<<blocks, kProjThreads, 0, st>>>(c, f, stats, a, b, maps, counters, q, fq_cap);
+  return cudaGetLastError();
+}
+
+cudaError_t fixup(const DevCfg &c, const void *fq, const int *counters, long fq_cap, float *maps, cudaStream_t st)
+{
+  fixup_kernel<<<152 * 8, 256, 0, st>>>(c, reinterpret_cast<const FallbackEntry *>(fq), counters, fq_cap, maps);
   return cudaGetLastError();
 }
 

@@ -245,7 +245,7 @@ class GetHI:
         return out
 
     KERNEL_CLASSES = ("zpass", "ypass", "xpass", "xpass_vel", "nyq", "sigma", "fd_vel", "get_hi", "project",
-                      "scale", "zpass_raw")
+                      "scale", "zpass_raw", "fixup")
 
     def profile(self, on=True):
         _check(lib().gethi_gpu_profile(self._ctx, int(on)))

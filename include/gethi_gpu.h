@@ -145,7 +145,8 @@ int gethi_gpu_stage_times(const gethi_ctx *ctx, float *ms, int n);
 #define GETHI_KC_PROJECT 8
 #define GETHI_KC_SCALE 9
 #define GETHI_KC_ZPASS_RAW 10 /* Z pass of a velocity field from the stored modes */
-#define GETHI_NKCLASS 11
+#define GETHI_KC_FIXUP 11     /* FP64 keys of the samples the FP32 path left uncertain */
+#define GETHI_NKCLASS 12
 int gethi_gpu_profile(gethi_ctx *ctx, int on);
 /* accumulated ms and launch counts per class since profiling was switched on,
  * and the total number of kernels this context has launched */
