@@ -4,8 +4,9 @@
 // Device memory per context (N = n_grid, m = N/2):
 //   main  N^3 floats  : delta_k (split half spectrum) -> delta(x) -> HI mass
 //   nyq   N^2 complex : kx = N/2 plane of delta_k
-//   vmain N^3 floats  : velocity potential or one velocity component (scratch)
-//   vnyq  N^2 complex
+//   A, B, C N^3 floats (+ N^2 complex Nyquist planes each): phi after the Z
+//         pass, i kz phi, and v_x after the Y pass (spectral velocity); only A
+//         for the finite-difference velocity, none without RSD
 //   vr    N^3 floats  : radial velocity -> dz_rsd
 //   maps  n_nu 12 nside^2 floats
 //   plus FP64/FP32 tables, twiddles, per-block partial sums.
@@ -27,8 +28,8 @@ struct gethi_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
-  float2 *main = nullptr, *nyq = nullptr, *vmain = nullptr, *vnyq = nullptr, *modes = nullptr;
-  float2 *raw = nullptr, *rawnyq = nullptr;  // delta_k kept for the velocity fields
+  float2 *main = nullptr, *nyq = nullptr, *modes = nullptr;
+  float2 *bA = nullptr, *bAn = nullptr, *bB = nullptr, *bBn = nullptr, *bC = nullptr, *bCn = nullptr;
   float *vr = nullptr, *maps = nullptr;
   float2 *twN = nullptr, *twM = nullptr;
   double2 *partials = nullptr;
@@ -198,33 +199,102 @@ void collect_kernel_times(gethi_ctx *c)
 }
 
 // One field: Z pass (modes generated on the fly), Y pass, X pass with epilogue.
-// The first field (delta) draws the modes and keeps them in raw/rawnyq; later
-// fields read them back (zmode 2) instead of drawing again.
-int field_fft(gethi_ctx *c, float2 *main, float2 *nyq, int kind, const float2 *src, int epi, int comp, int first,
-              int zmode)
+// Geometries of the column sets (main block and Nyquist plane, Z and Y axes).
+struct Geoms {
+  ColGeom zm, zn, ym, yn;
+};
+Geoms geoms(float2 *main, float2 *nyq, long n, long m)
+{
+  return {geom(main, n * m, 0, 1, n * m, n * m), geom(nyq, n, 0, 1, n, n), geom(main, m, n * m, 1, m, n * m),
+          geom(nyq, n, 0, n, 1, n)};
+}
+
+// All Fourier-space work of one realisation: one Z pass drawing the modes and
+// transforming delta (+ phi, + i kz phi), Y passes, X passes.
+int fields_fft(gethi_ctx *c, const float2 *src)
 {
   const DevCfg &g = c->cfg;
+  const Setup &s = c->s;
   const long n = g.n, m = g.m;
   cudaStream_t st = c->stream;
+  const int nout = s.p.do_rsd ? (s.p.velocity_mode == 1 ? 3 : 2) : 1;
+  Geoms d = geoms(c->main, c->nyq, n, m), A = geoms(c->bA, c->bAn, n, m), B = geoms(c->bB, c->bBn, n, m),
+        C = geoms(c->bC, c->bCn, n, m);
   {
-    KTimer t(c, zmode == 1 ? KC_ZPASS : KC_ZPASS_RAW);
-    CK(col_pass(g, geom(main, n * m, 0, 1, n * m, n * m), 0, zmode, kind, src, c->twN, c->raw, st));
+    KTimer t(c, KC_ZPASS);
+    CK(col_pass(g, d.zm, 0, 1, nout, src, c->twN, c->bA, c->bB, st));
   }
   {
     KTimer t(c, KC_NYQ);
-    CK(col_pass(g, geom(nyq, n, 0, 1, n, n), 1, zmode, kind, src, c->twN, c->rawnyq, st));
+    CK(col_pass(g, d.zn, 1, 1, nout, src, c->twN, c->bAn, c->bBn, st));
   }
+  // density
   {
     KTimer t(c, KC_YPASS);
-    CK(col_pass(g, geom(main, m, n * m, 1, m, n * m), 0, 0, kind, nullptr, c->twN, nullptr, st));
+    CK(col_pass(g, d.ym, 0, 0, 0, nullptr, c->twN, nullptr, nullptr, st));
   }
   {
     KTimer t(c, KC_NYQ);
-    CK(col_pass(g, geom(nyq, n, 0, n, 1, n), 1, 0, kind, nullptr, c->twN, nullptr, st));
+    CK(col_pass(g, d.yn, 1, 0, 0, nullptr, c->twN, nullptr, nullptr, st));
+  }
+  RowIn in = {{c->main, nullptr, nullptr}, {c->nyq, nullptr, nullptr}};
+  {
+    KTimer t(c, KC_XPASS);
+    CK(row_pass(g, in, c->twN, c->twM, g.norm, 0, nullptr, c->partials, st));
   }
   {
-    KTimer t(c, epi ? KC_XPASS_VEL : KC_XPASS);
-    CK(row_pass(g, main, nyq, c->twN, c->twM, g.norm, epi, c->vr, comp, first, c->partials, st));
+    KTimer t(c, KC_SIGMA);
+    CK(finish_sigma(c->partials, (int)c->npartials, (double)n * n * n, c->stats, st));
+  }
+  if (!s.p.do_rsd) {
+    CK(cudaMemsetAsync(c->vr, 0, sizeof(float) * n * n * n, st));
+    return GETHI_OK;
+  }
+  if (s.p.velocity_mode == 1) {
+    // v_x = Y(i kx phi) -> C; v_y = Y(i ky phi) -> A; v_z = Y(i kz phi) in B
+    {
+      KTimer t(c, KC_YPASS);
+      CK(col_pass(g, A.ym, 0, 4, 0, nullptr, c->twN, c->bC, nullptr, st));
+    }
+    {
+      KTimer t(c, KC_NYQ);
+      CK(col_pass(g, A.yn, 1, 4, 0, nullptr, c->twN, c->bCn, nullptr, st));
+    }
+    {
+      KTimer t(c, KC_YPASS);
+      CK(col_pass(g, A.ym, 0, 5, 0, nullptr, c->twN, nullptr, nullptr, st));
+    }
+    {
+      KTimer t(c, KC_NYQ);
+      CK(col_pass(g, A.yn, 1, 5, 0, nullptr, c->twN, nullptr, nullptr, st));
+    }
+    {
+      KTimer t(c, KC_YPASS);
+      CK(col_pass(g, B.ym, 0, 0, 0, nullptr, c->twN, nullptr, nullptr, st));
+    }
+    {
+      KTimer t(c, KC_NYQ);
+      CK(col_pass(g, B.yn, 1, 0, 0, nullptr, c->twN, nullptr, nullptr, st));
+    }
+    RowIn v = {{c->bC, c->bA, c->bB}, {c->bCn, c->bAn, c->bBn}};
+    KTimer t(c, KC_XPASS_VEL);
+    CK(row_pass(g, v, c->twN, c->twM, g.norm, 2, c->vr, nullptr, st));
+  } else {
+    {
+      KTimer t(c, KC_YPASS);
+      CK(col_pass(g, A.ym, 0, 0, 0, nullptr, c->twN, nullptr, nullptr, st));
+    }
+    {
+      KTimer t(c, KC_NYQ);
+      CK(col_pass(g, A.yn, 1, 0, 0, nullptr, c->twN, nullptr, nullptr, st));
+    }
+    RowIn v = {{c->bA, nullptr, nullptr}, {c->bAn, nullptr, nullptr}};
+    {
+      KTimer t(c, KC_XPASS);
+      CK(row_pass(g, v, c->twN, c->twM, g.norm, 3, nullptr, nullptr, st));
+    }
+    KTimer t(c, KC_FDVEL);
+    CK(radial_velocity_fd(g, reinterpret_cast<const float *>(c->bA), c->vr, st));
   }
   return GETHI_OK;
 }
@@ -258,10 +328,12 @@ extern "C" int gethi_gpu_init(const gethi_params *p, int device, gethi_ctx **out
   const size_t ncell = (size_t)n * n * n;
   const long npix = 12 * s.p.n_side * s.p.n_side;
   c->npartials = row_pass_blocks((int)n);
+  const bool va = s.p.do_rsd, vbc = s.p.do_rsd && s.p.velocity_mode == 1;
   if ((rc = dalloc(&c->main, ncell / 2)) || (rc = dalloc(&c->nyq, (size_t)n * n)) ||
-      (rc = dalloc(&c->vmain, ncell / 2)) || (rc = dalloc(&c->vnyq, (size_t)n * n)) ||
+      (va && ((rc = dalloc(&c->bA, ncell / 2)) || (rc = dalloc(&c->bAn, (size_t)n * n)))) ||
+      (vbc && ((rc = dalloc(&c->bB, ncell / 2)) || (rc = dalloc(&c->bBn, (size_t)n * n)) ||
+               (rc = dalloc(&c->bC, ncell / 2)) || (rc = dalloc(&c->bCn, (size_t)n * n)))) ||
       (rc = dalloc(&c->vr, ncell)) || (rc = dalloc(&c->maps, (size_t)npix * s.p.n_nu)) ||
-      (s.p.do_rsd && ((rc = dalloc(&c->raw, ncell / 2)) || (rc = dalloc(&c->rawnyq, (size_t)n * n)))) ||
       (rc = dalloc(&c->twN, (size_t)n)) || (rc = dalloc(&c->twM, (size_t)m)) ||
       (rc = dalloc(&c->partials, (size_t)c->npartials)) || (rc = dalloc(&c->stats, 4)) ||
       (rc = dalloc(&c->pk_f, (size_t)s.d.numk)) || (rc = dalloc(&c->logk_f, (size_t)s.d.numk)) ||
@@ -327,7 +399,7 @@ extern "C" void gethi_gpu_free(gethi_ctx *c)
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  void *bufs[] = {c->main, c->nyq, c->vmain, c->vnyq, c->modes, c->raw, c->rawnyq, c->vr, c->maps, c->twN, c->twM, c->partials,
+  void *bufs[] = {c->main, c->nyq, c->bA, c->bAn, c->bB, c->bBn, c->bC, c->bCn, c->modes, c->vr, c->maps, c->twN, c->twM, c->partials,
                   c->stats, c->pk_f, c->logk_f, c->tab_f, c->tab_d, c->prefac, c->edges_f, c->edges_d, c->counters};
   for (void *b : bufs)
     if (b) cudaFree(b);
@@ -395,25 +467,8 @@ extern "C" int gethi_gpu_make_fields(gethi_ctx *c, const float *modes_k)
   }
   c->nev = 0;
   record(c);
-  int rc = field_fft(c, c->main, c->nyq, FIELD_DENS, src, 0, 0, 0, 1);
+  int rc = fields_fft(c, src);
   if (rc) return rc;
-  {
-    KTimer t(c, KC_SIGMA);
-    CK(finish_sigma(c->partials, (int)c->npartials, (double)n * n * n, c->stats, c->stream));
-  }
-  record(c);
-  if (s.p.do_rsd) {
-    if (s.p.velocity_mode == 1) {
-      for (int comp = 0; comp < 3; comp++)
-        if ((rc = field_fft(c, c->vmain, c->vnyq, FIELD_VX + comp, src, 1, comp, comp == 0, 2))) return rc;
-    } else {
-      if ((rc = field_fft(c, c->vmain, c->vnyq, FIELD_VPOT, src, 0, 0, 0, 2))) return rc;
-      KTimer t(c, KC_FDVEL);
-      CK(radial_velocity_fd(c->cfg, reinterpret_cast<const float *>(c->vmain), c->vr, c->stream));
-    }
-  } else {
-    CK(cudaMemsetAsync(c->vr, 0, sizeof(float) * n * n * n, c->stream));
-  }
   record(c);
   c->stage = 1;
   return GETHI_OK;

@@ -165,7 +165,13 @@ struct Radices {};
 template <int First, int... Rest>
 constexpr int first_radix() { return First; }
 
-template <int L, int P, int Ns, int R, int... Rest>
+// shared-memory slot of element n: n*ss, plus one skew slot per 16 elements
+// when SKEW (row transforms, ss = 1) so that the stride-R writes of the first
+// stage fall in different banks
+template <bool SKEW>
+__device__ __forceinline__ int sm_slot(int n, int ss) { return SKEW ? n + (n >> 4) : n * ss; }
+
+template <int L, int P, bool SKEW, int Ns, int R, int... Rest>
 __device__ __forceinline__ void stockham(float2 *v, float2 *sm, int ss, int t, const float2 *__restrict__ tw)
 {
   constexpr int T = L / P;
@@ -189,23 +195,27 @@ __device__ __forceinline__ void stockham(float2 *v, float2 *sm, int ss, int t, c
       const int b = t + T * j;
       const int base = (b / Ns) * Ns * R + (b % Ns);
 #pragma unroll
-      for (int r = 0; r < R; r++) sm[(base + r * Ns) * ss] = v[j * R + r];
+      for (int r = 0; r < R; r++) sm[sm_slot<SKEW>(base + r * Ns, ss)] = v[j * R + r];
     }
     __syncthreads();
 #pragma unroll
     for (int j = 0; j < P / R2; j++)
 #pragma unroll
-      for (int r = 0; r < R2; r++) v[j * R2 + r] = sm[(t + T * j + (L / R2) * r) * ss];
-    stockham<L, P, Ns * R, Rest...>(v, sm, ss, t, tw);
+      for (int r = 0; r < R2; r++) v[j * R2 + r] = sm[sm_slot<SKEW>(t + T * j + (L / R2) * r, ss)];
+    stockham<L, P, SKEW, Ns * R, Rest...>(v, sm, ss, t, tw);
   }
 }
 
-template <int L, int P, int... R>
+template <int L, int P, bool SKEW = false, int... R>
 __device__ __forceinline__ void stockham_run(float2 *v, float2 *sm, int ss, int t, const float2 *__restrict__ tw,
                                              Radices<R...>)
 {
-  stockham<L, P, 1, R...>(v, sm, ss, t, tw);
+  stockham<L, P, SKEW, 1, R...>(v, sm, ss, t, tw);
 }
+
+// shared-memory slots one transform of length L occupies
+template <int L, bool SKEW>
+constexpr int sm_len() { return SKEW ? L + L / 16 : L; }
 
 template <int... R>
 constexpr int radix_first(Radices<R...>) { return first_radix<R...>(); }

@@ -9,14 +9,19 @@
 // main[kz][ky][kx] (row length m = N/2 complex, rows 16-byte aligned); the
 // kx = N/2 (Nyquist) plane lives in nyq[kz][ky].  The transform is three
 // passes, each one read and one write of the field:
-//   pass Z: inverse c2c along kz of every (ky,kx) column; in the first pass the
-//           modes are produced on the fly (Philox or an uploaded spectrum), so
-//           the spectrum is never read from HBM;
-//   pass Y: inverse c2c along ky;
+//   pass Z: inverse c2c along kz of every (ky,kx) column.  The modes are drawn
+//           on the fly (Philox, or an uploaded spectrum) and, in the same
+//           kernel, up to three fields are transformed from them: delta,
+//           phi = delta f0 H0/k^2 and i k_z phi.  Along a z column k_x and k_y
+//           are constant, so the Z-transformed v_x and v_y are i k_x and i k_y
+//           times the Z-transformed phi and need no transform of their own;
+//   pass Y: inverse c2c along ky (v_x, v_y: phi times i k_x or i k_y on load);
 //   pass X: per (z,y) row the N-point c2r is an N/2-point complex FFT of
 //           Z[k] = (X_k + X*_{m-k}) + i e^{2 pi i k/N} (X_k - X*_{m-k}); the result
 //           (x[2j], x[2j+1]) overwrites the row in place, so the real field is a
-//           compact N^3 float grid with the same bytes as main.
+//           compact N^3 float grid with the same bytes as main.  For the
+//           spectral velocity one X kernel transforms v_x, v_y, v_z and writes
+//           v_r = v . (x - x_obs)/|x - x_obs| once.
 // Only Re X_0 and Re X_{N/2} enter the x c2r, i.e. the result is the real part
 // of the full inverse DFT of the Hermitian-extended spectrum (the reference
 // draws the kx=0 and kx=N/2 planes without Hermitian symmetry).
@@ -84,25 +89,24 @@ __device__ __forceinline__ float2 mode_value(const DevCfg &c, int ii, int jj, in
 // ---------------------------------------------------------------------------
 // column passes (Z and Y)
 // element (col, e) of a column set lives at base + (col/cpp) pstride + (col%cpp) cstride + e estride
+//   MODE 0: out = FFT(in)                   (in = g.base, out = out1 or in place)
+//   MODE 1: draw delta_k and write FFT(delta) to g.base, and (nout >= 2)
+//           FFT(phi) to out1, (nout == 3) FFT(i kz phi) to out2
+//   MODE 4: out = FFT(i kx in)  (kx of the column; 0 on the Nyquist plane)
+//   MODE 5: out = FFT(i ky in)  (ky of the element; 0 at the Nyquist index)
 // ---------------------------------------------------------------------------
-// kind transform of a stored delta_k (mode ii, jj, kk): FIELD_DENS, FIELD_VPOT or FIELD_V*
-__device__ __forceinline__ float2 field_from_delta(const DevCfg &c, float2 d, int ii, int jj, int kk, int kind)
+__device__ __forceinline__ float vfac_over_k2(const DevCfg &c, int ii, int jj, int kk)
 {
-  if (kind == FIELD_DENS) return d;
   const int n = c.n;
   float kz = kval(ii, n, c.dk), ky = kval(jj, n, c.dk), kx = kval(kk, n, c.dk);
   float k2 = kx * kx + ky * ky + kz * kz;
-  if (k2 <= 0.f) return make_float2(0.f, 0.f);
-  float f = c.vfac / k2;
-  if (kind == FIELD_VPOT) return cscale(d, f);
-  float kj = kind == FIELD_VX ? (2 * kk == n ? 0.f : kx) : kind == FIELD_VY ? (2 * jj == n ? 0.f : ky) : (2 * ii == n ? 0.f : kz);
-  return cmul_i(cscale(d, f * kj));
+  return k2 > 0.f ? __fdividef(c.vfac, k2) : 0.f;  // phi_k = delta_k f0 H0 / k^2, src/fourier.c:298
 }
 
 template <int L, int P, int TX, class Rad, int MODE>
-__global__ void __launch_bounds__(TX *(L / P)) col_pass_kernel(DevCfg c, ColGeom g, int nyq, int kind,
-                                                               const float2 *__restrict__ src,
-                                                               const float2 *__restrict__ tw, float2 *raw)
+__global__ void __launch_bounds__(TX *(L / P), MODE == 1 ? 1 : 2)
+    col_pass_kernel(DevCfg c, ColGeom g, int nyq, int nout, const float2 *__restrict__ src,
+                    const float2 *__restrict__ tw, float2 *out1, float2 *out2)
 {
   constexpr int T = L / P;
   constexpr int R0 = radix_first(Rad{}), RL = radix_last(Rad{});
@@ -111,70 +115,88 @@ __global__ void __launch_bounds__(TX *(L / P)) col_pass_kernel(DevCfg c, ColGeom
   const long col = (long)blockIdx.x * TX + cl;
   const bool active = col < g.ncols;
   const long cb = (col / g.cpp) * g.pstride + (col % g.cpp) * g.cstride;
+  const int ky = nyq ? (int)col : (int)(col / c.m), kx = nyq ? c.m : (int)(col % c.m);  // MODE 1 columns
   float2 v[P];
+  if constexpr (MODE == 1) {
+    float2 d[P];
 #pragma unroll
-  for (int j = 0; j < P / R0; j++)
+    for (int j = 0; j < P / R0; j++)
 #pragma unroll
-    for (int r = 0; r < R0; r++) {
-      const int e = t + T * j + (L / R0) * r;
-      float2 x = make_float2(0.f, 0.f);
+      for (int r = 0; r < R0; r++) {
+        const int e = t + T * j + (L / R0) * r;
+        d[j * R0 + r] = active ? mode_value(c, e, ky, kx, FIELD_DENS, src) : make_float2(0.f, 0.f);
+        v[j * R0 + r] = d[j * R0 + r];
+      }
+#pragma unroll 1
+    for (int f = 0; f < nout; f++) {
+      if (f > 0) {
+#pragma unroll
+        for (int j = 0; j < P / R0; j++)
+#pragma unroll
+          for (int r = 0; r < R0; r++) {
+            const int e = t + T * j + (L / R0) * r;
+            const float s = vfac_over_k2(c, e, ky, kx);
+            float2 x = cscale(d[j * R0 + r], s);
+            if (f == 2) x = cmul_i(cscale(x, 2 * e == c.n ? 0.f : kval(e, c.n, c.dk)));
+            v[j * R0 + r] = x;
+          }
+        __syncthreads();  // the previous transform's last shared-memory reads are done
+      }
+      stockham_run<L, P>(v, smem + cl, TX, t, tw, Rad{});
+      float2 *o = f == 0 ? g.base : (f == 1 ? out1 : out2);
       if (active) {
-        if constexpr (MODE == 1) {
-          int ky = nyq ? (int)col : (int)(col / c.m), kx = nyq ? c.m : (int)(col % c.m);
-          x = mode_value(c, e, ky, kx, FIELD_DENS, src);
-          if (raw) raw[cb + (long)e * g.estride] = x;
-          x = field_from_delta(c, x, e, ky, kx, kind);
-        } else if constexpr (MODE == 2) {
-          int ky = nyq ? (int)col : (int)(col / c.m), kx = nyq ? c.m : (int)(col % c.m);
-          x = field_from_delta(c, __ldg(&raw[cb + (long)e * g.estride]), e, ky, kx, kind);
-        } else {
-          x = g.base[cb + (long)e * g.estride];
-        }
+#pragma unroll
+        for (int j = 0; j < P / RL; j++)
+#pragma unroll
+          for (int r = 0; r < RL; r++) o[cb + (long)(t + T * j + (L / RL) * r) * g.estride] = v[j * RL + r];
       }
-      v[j * R0 + r] = x;
     }
-  stockham_run<L, P>(v, smem + cl, TX, t, tw, Rad{});
-  if (active) {
+  } else {
+    float2 *o = out1 ? out1 : g.base;
+    float fcol = 0.f;
+    if constexpr (MODE == 4) fcol = nyq ? 0.f : kval((int)(col % c.m), c.n, c.dk);
 #pragma unroll
-    for (int j = 0; j < P / RL; j++)
+    for (int j = 0; j < P / R0; j++)
 #pragma unroll
-      for (int r = 0; r < RL; r++) {
-        const int e = t + T * j + (L / RL) * r;
-        g.base[cb + (long)e * g.estride] = v[j * RL + r];
+      for (int r = 0; r < R0; r++) {
+        const int e = t + T * j + (L / R0) * r;
+        float2 x = active ? g.base[cb + (long)e * g.estride] : make_float2(0.f, 0.f);
+        if constexpr (MODE == 4) x = cmul_i(cscale(x, fcol));
+        if constexpr (MODE == 5) x = cmul_i(cscale(x, 2 * e == c.n ? 0.f : kval(e, c.n, c.dk)));
+        v[j * R0 + r] = x;
       }
+    stockham_run<L, P>(v, smem + cl, TX, t, tw, Rad{});
+    if (active) {
+#pragma unroll
+      for (int j = 0; j < P / RL; j++)
+#pragma unroll
+        for (int r = 0; r < RL; r++) o[cb + (long)(t + T * j + (L / RL) * r) * g.estride] = v[j * RL + r];
+    }
   }
 }
 
 // ---------------------------------------------------------------------------
-// row pass (X): c2r of every (z,y) row, fused epilogues
-//   EPI 0: write the real row in place (x scale) and accumulate sum, sum of squares
-//   EPI 1: add (x scale) * (cell_j - obs_j)/r into the radial-velocity grid
+// row pass (X): c2r of every (z,y) row
+//   EPI 0: write the real row in place (x scale), per-block sum and sum of squares
+//   EPI 3: write the real row in place (x scale)
+//   EPI 2: rows of v_x (in0), v_y (in1), v_z (in2) -> v_r = sum_j v_j u_j into vr
 // ---------------------------------------------------------------------------
-template <int M, int P, int RW, class Rad, int EPI>
-__global__ void __launch_bounds__(RW *(M / P)) row_pass_kernel(DevCfg c, float2 *main, const float2 *__restrict__ nyq,
-                                                               long nrows, const float2 *__restrict__ twN,
-                                                               const float2 *__restrict__ twM, float scale,
-                                                               float *vr, int comp, int first,
-                                                               double2 *partials)
+template <int M, int P, int RW, class Rad>
+__device__ __forceinline__ void row_c2r(float2 *v, float2 *srow, const float2 *__restrict__ grow, float2 xm,
+                                        bool active, int t, const float2 *__restrict__ twN,
+                                        const float2 *__restrict__ twM)
 {
   constexpr int T = M / P;
-  constexpr int R0 = radix_first(Rad{}), RL = radix_last(Rad{});
-  extern __shared__ float2 smem[];
-  const int tid = threadIdx.x, rl = tid / T, t = tid % T;
-  const long row = (long)blockIdx.x * RW + rl;
-  const bool active = row < nrows;
-  float2 *srow = smem + rl * M;
-  float2 *grow = main + row * (long)M;
-  for (int i = t; i < M; i += T) srow[i] = active ? grow[i] : make_float2(0.f, 0.f);
+  constexpr int R0 = radix_first(Rad{});
+  // row into shared memory (coalesced), then Z[k] at the first-stage positions
+  for (int i = t; i < M; i += T) srow[sm_slot<true>(i, 1)] = active ? grow[i] : make_float2(0.f, 0.f);
   __syncthreads();
-  const float2 xm = active ? nyq[row] : make_float2(0.f, 0.f);
-  float2 v[P];
 #pragma unroll
   for (int j = 0; j < P / R0; j++)
 #pragma unroll
     for (int r = 0; r < R0; r++) {
       const int k = t + T * j + (M / R0) * r;
-      float2 a = srow[k], b = k == 0 ? xm : srow[M - k];
+      float2 a = srow[sm_slot<true>(k, 1)], b = k == 0 ? xm : srow[sm_slot<true>(M - k, 1)];
       if (k == 0) {
         a.y = 0.f;
         b.y = 0.f;
@@ -183,73 +205,103 @@ __global__ void __launch_bounds__(RW *(M / P)) row_pass_kernel(DevCfg c, float2 
       float2 d = make_float2(a.x - b.x, a.y + b.y);  // a - conj(b)
       v[j * R0 + r] = cadd(s, cmul_i(cmul(__ldg(&twN[k]), d)));
     }
-  stockham_run<M, P>(v, srow, 1, t, twM, Rad{});
+  stockham_run<M, P, true>(v, srow, 1, t, twM, Rad{});
+}
 
-  double s1 = 0, s2 = 0;
-  if (active) {
-    if constexpr (EPI == 0) {
-      // per-thread sums in FP32 with Neumaier compensation (P values each),
-      // carried to FP64 for the block and grid reductions
+template <int M, int P, int RW, class Rad, int EPI>
+__global__ void __launch_bounds__(RW *(M / P), EPI == 2 ? 512 / (RW * (M / P)) : 1) row_pass_kernel(DevCfg c, RowIn in, long nrows,
+                                                               const float2 *__restrict__ twN,
+                                                               const float2 *__restrict__ twM, float scale,
+                                                               float *vr, double2 *partials)
+{
+  constexpr int T = M / P;
+  constexpr int RL = radix_last(Rad{});
+  extern __shared__ float2 smem[];
+  const int tid = threadIdx.x, rl = tid / T, t = tid % T;
+  const long row = (long)blockIdx.x * RW + rl;
+  const bool active = row < nrows;
+  float2 *srow = smem + rl * sm_len<M, true>();
+  float2 v[P];
+  if constexpr (EPI == 2) {
+    float2 acc[P];
+    const int iy = (int)(row % c.n), iz = (int)(row / c.n);
+    const float y = c.dxf * (iy + 0.5f) - c.pos_obsf, z = c.dxf * (iz + 0.5f) - c.pos_obsf;
+#pragma unroll 1
+    for (int comp = 0; comp < 3; comp++) {
+      if (comp) __syncthreads();  // shared row free again
+      row_c2r<M, P, RW, Rad>(v, srow, in.main[comp] + row * (long)M, active ? in.nyq[comp][row] : make_float2(0.f, 0.f),
+                             active, t, twN, twM);
+#pragma unroll
+      for (int j = 0; j < P / RL; j++)
+#pragma unroll
+        for (int r = 0; r < RL; r++) {
+          const int e = t + T * j + (M / RL) * r;
+          const float x0 = c.dxf * (2 * e + 0.5f) - c.pos_obsf, x1 = c.dxf * (2 * e + 1.5f) - c.pos_obsf;
+          const float i0 = rsqrtf(x0 * x0 + y * y + z * z), i1 = rsqrtf(x1 * x1 + y * y + z * z);
+          const float u0 = comp == 0 ? x0 * i0 : (comp == 1 ? y * i0 : z * i0);
+          const float u1 = comp == 0 ? x1 * i1 : (comp == 1 ? y * i1 : z * i1);
+          const float2 x = v[j * RL + r];
+          acc[j * RL + r] = comp == 0 ? make_float2(x.x * u0, x.y * u1)
+                                      : make_float2(fmaf(x.x, u0, acc[j * RL + r].x), fmaf(x.y, u1, acc[j * RL + r].y));
+        }
+    }
+    if (active) {
+      float2 *vrow = reinterpret_cast<float2 *>(vr + row * (long)c.n);
+#pragma unroll
+      for (int j = 0; j < P / RL; j++)
+#pragma unroll
+        for (int r = 0; r < RL; r++) vrow[t + T * j + (M / RL) * r] = cscale(acc[j * RL + r], scale);
+    }
+  } else {
+    float2 *grow = in.main[0] + row * (long)M;
+    row_c2r<M, P, RW, Rad>(v, srow, grow, active ? in.nyq[0][row] : make_float2(0.f, 0.f), active, t, twN, twM);
+    double s1 = 0, s2 = 0;
+    if (active) {
+      // per-thread sums in FP32 with Neumaier compensation, carried to FP64
       float a1 = 0.f, c1 = 0.f, a2 = 0.f, c2 = 0.f;
-      auto nsum = [](float &acc, float &comp, float v) {
-        float t = acc + v;
-        comp += fabsf(acc) >= fabsf(v) ? (acc - t) + v : (v - t) + acc;
-        acc = t;
+      auto nsum = [](float &acc, float &comp, float val) {
+        float s = acc + val;
+        comp += fabsf(acc) >= fabsf(val) ? (acc - s) + val : (val - s) + acc;
+        acc = s;
       };
 #pragma unroll
       for (int j = 0; j < P / RL; j++)
 #pragma unroll
         for (int r = 0; r < RL; r++) {
           const int e = t + T * j + (M / RL) * r;
-          float2 x = cscale(v[j * RL + r], scale);
+          const float2 x = cscale(v[j * RL + r], scale);
           grow[e] = x;
-          nsum(a1, c1, x.x);
-          nsum(a1, c1, x.y);
-          nsum(a2, c2, x.x * x.x);  // float squares, src/fourier.c:51
-          nsum(a2, c2, x.y * x.y);
+          if constexpr (EPI == 0) {
+            nsum(a1, c1, x.x);
+            nsum(a1, c1, x.y);
+            nsum(a2, c2, x.x * x.x);  // float squares, src/fourier.c:51
+            nsum(a2, c2, x.y * x.y);
+          }
         }
       s1 = (double)a1 + (double)c1;
       s2 = (double)a2 + (double)c2;
-    } else {
-      const int iy = (int)(row % c.n), iz = (int)(row / c.n);
-      const float y = c.dxf * (iy + 0.5f) - c.pos_obsf, z = c.dxf * (iz + 0.5f) - c.pos_obsf;
-      float *vrow = vr + row * (long)c.n;
-#pragma unroll
-      for (int j = 0; j < P / RL; j++)
-#pragma unroll
-        for (int r = 0; r < RL; r++) {
-          const int e = t + T * j + (M / RL) * r;
-          float2 x = cscale(v[j * RL + r], scale);
-          float x0 = c.dxf * (2 * e + 0.5f) - c.pos_obsf, x1 = c.dxf * (2 * e + 1.5f) - c.pos_obsf;
-          float i0 = rsqrtf(x0 * x0 + y * y + z * z), i1 = rsqrtf(x1 * x1 + y * y + z * z);
-          float u0 = comp == 0 ? x0 * i0 : (comp == 1 ? y * i0 : z * i0);
-          float u1 = comp == 0 ? x1 * i1 : (comp == 1 ? y * i1 : z * i1);
-          float2 old = first ? make_float2(0.f, 0.f) : *reinterpret_cast<float2 *>(vrow + 2 * e);
-          *reinterpret_cast<float2 *>(vrow + 2 * e) = make_float2(old.x + x.x * u0, old.y + x.y * u1);
-        }
     }
-  }
-  if constexpr (EPI == 0) {
-    // block reduction of the two sums -> partials[blockIdx.x]
-    __shared__ double red[2][32];
-    for (int o = 16; o > 0; o >>= 1) {
-      s1 += __shfl_xor_sync(0xffffffffu, s1, o);
-      s2 += __shfl_xor_sync(0xffffffffu, s2, o);
-    }
-    const int w = tid >> 5, lane = tid & 31, nw = (RW * T + 31) >> 5;
-    __syncthreads();
-    if (lane == 0) {
-      red[0][w] = s1;
-      red[1][w] = s2;
-    }
-    __syncthreads();
-    if (tid == 0) {
-      double a = 0, b = 0;
-      for (int i = 0; i < nw; i++) {
-        a += red[0][i];
-        b += red[1][i];
+    if constexpr (EPI == 0) {
+      __shared__ double red[2][32];
+      for (int o = 16; o > 0; o >>= 1) {
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
       }
-      partials[blockIdx.x] = make_double2(a, b);
+      const int w = tid >> 5, lane = tid & 31, nw = (RW * T + 31) >> 5;
+      __syncthreads();
+      if (lane == 0) {
+        red[0][w] = s1;
+        red[1][w] = s2;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        double a = 0, b = 0;
+        for (int i = 0; i < nw; i++) {
+          a += red[0][i];
+          b += red[1][i];
+        }
+        partials[blockIdx.x] = make_double2(a, b);
+      }
     }
   }
 }
@@ -277,21 +329,15 @@ __global__ void finish_sigma_kernel(const double2 *__restrict__ partials, int np
   if (threadIdx.x == 0) {
     double A = 0, CA = 0, B = 0, CB = 0;
     for (int i = 0; i < (int)blockDim.x; i++) {
-      double y = sh[0][i] - CA, t = A + y;
-      CA = (t - A) - y;
-      A = t;
-      y = sh[1][i] - CA;
-      t = A + y;
-      CA = (t - A) - y;
-      A = t;
-      y = sh[2][i] - CB;
-      t = B + y;
-      CB = (t - B) - y;
-      B = t;
-      y = sh[3][i] - CB;
-      t = B + y;
-      CB = (t - B) - y;
-      B = t;
+      for (int q = 0; q < 2; q++) {
+        double y = sh[q][i] - CA, t = A + y;
+        CA = (t - A) - y;
+        A = t;
+        y = sh[2 + q][i] - CB;
+        t = B + y;
+        CB = (t - B) - y;
+        B = t;
+      }
     }
     double mean = A / ncells;
     stats[0] = mean;
@@ -300,7 +346,7 @@ __global__ void finish_sigma_kernel(const double2 *__restrict__ partials, int np
 }
 
 // standalone mode generator (inspection): reference layout [kz][ky][N/2+1]
-__global__ void modes_kernel(DevCfg c, float2 *out, int kind)
+__global__ void modes_kernel(DevCfg c, float2 *out)
 {
   const long h = c.m + 1;
   const long total = (long)c.n * c.n * h;
@@ -308,17 +354,16 @@ __global__ void modes_kernel(DevCfg c, float2 *out, int kind)
     int kk = (int)(i % h);
     long rest = i / h;
     int jj = (int)(rest % c.n), ii = (int)(rest / c.n);
-    out[i] = mode_value(c, ii, jj, kk, kind, nullptr);
+    out[i] = mode_value(c, ii, jj, kk, FIELD_DENS, nullptr);
   }
 }
 
 // ---------------------------------------------------------------------------
 // launch plumbing
 // ---------------------------------------------------------------------------
-template <int L>
-struct ColPlan;
-template <int M>
-struct RowPlan;
+template <int L> struct ColPlan;
+template <int M> struct RowPlan;
+template <int M> struct RowPlanV;
 // columns: L = N; P points per thread, TX columns per block
 template <> struct ColPlan<2048> { static constexpr int P = 32, TX = 4; using R = Radices<32, 8, 8>; };
 template <> struct ColPlan<1024> { static constexpr int P = 32, TX = 8; using R = Radices<32, 32>; };
@@ -330,7 +375,7 @@ template <> struct ColPlan<64> { static constexpr int P = 8, TX = 16; using R = 
 template <> struct ColPlan<32> { static constexpr int P = 8, TX = 16; using R = Radices<8, 4>; };
 template <> struct ColPlan<24> { static constexpr int P = 12, TX = 16; using R = Radices<12, 2>; };
 template <> struct ColPlan<16> { static constexpr int P = 4, TX = 16; using R = Radices<4, 4>; };
-// rows: M = N/2
+// rows: M = N/2 (single field)
 template <> struct RowPlan<1024> { static constexpr int P = 32, RW = 4; using R = Radices<32, 8, 4>; };
 template <> struct RowPlan<512> { static constexpr int P = 32, RW = 16; using R = Radices<32, 16>; };
 template <> struct RowPlan<256> { static constexpr int P = 16, RW = 16; using R = Radices<16, 16>; };
@@ -341,41 +386,51 @@ template <> struct RowPlan<32> { static constexpr int P = 8, RW = 32; using R = 
 template <> struct RowPlan<16> { static constexpr int P = 4, RW = 32; using R = Radices<4, 4>; };
 template <> struct RowPlan<12> { static constexpr int P = 12, RW = 32; using R = Radices<12>; };
 template <> struct RowPlan<8> { static constexpr int P = 8, RW = 32; using R = Radices<8>; };
+// rows of the fused velocity pass (an accumulator per point: fewer points per thread)
+template <> struct RowPlanV<1024> { static constexpr int P = 16, RW = 2; using R = Radices<16, 16, 4>; };
+template <> struct RowPlanV<512> { static constexpr int P = 16, RW = 4; using R = Radices<16, 16, 2>; };
+template <> struct RowPlanV<256> { static constexpr int P = 16, RW = 8; using R = Radices<16, 16>; };
+template <> struct RowPlanV<192> { static constexpr int P = 24, RW = 16; using R = Radices<8, 8, 3>; };
+template <> struct RowPlanV<128> { static constexpr int P = 16, RW = 16; using R = Radices<16, 8>; };
+template <> struct RowPlanV<64> { static constexpr int P = 8, RW = 16; using R = Radices<8, 8>; };
+template <> struct RowPlanV<32> { static constexpr int P = 8, RW = 32; using R = Radices<8, 4>; };
+template <> struct RowPlanV<16> { static constexpr int P = 4, RW = 32; using R = Radices<4, 4>; };
+template <> struct RowPlanV<12> { static constexpr int P = 12, RW = 32; using R = Radices<12>; };
+template <> struct RowPlanV<8> { static constexpr int P = 8, RW = 32; using R = Radices<8>; };
 
-template <int L, int GEN>
-static cudaError_t launch_col(const DevCfg &c, const ColGeom &g, int nyq, int kind, const float2 *src,
-                              const float2 *tw, float2 *raw, cudaStream_t st)
+template <int L, int MODE>
+static cudaError_t launch_col(const DevCfg &c, const ColGeom &g, int nyq, int nout, const float2 *src,
+                              const float2 *tw, float2 *out1, float2 *out2, cudaStream_t st)
 {
   using PL = ColPlan<L>;
   constexpr int threads = PL::TX * (L / PL::P);
   const size_t sm = sizeof(float2) * PL::TX * L;
-  auto kern = col_pass_kernel<L, PL::P, PL::TX, typename PL::R, GEN>;
+  auto kern = col_pass_kernel<L, PL::P, PL::TX, typename PL::R, MODE>;
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     attr = true;
   }
   long blocks = (g.ncols + PL::TX - 1) / PL::TX;
-  kern<<<(unsigned)blocks, threads, sm, st>>>(c, g, nyq, kind, src, tw, raw);
+  kern<<<(unsigned)blocks, threads, sm, st>>>(c, g, nyq, nout, src, tw, out1, out2);
   return cudaGetLastError();
 }
 
-template <int M, int EPI>
-static cudaError_t launch_row(const DevCfg &c, float2 *main, const float2 *nyq, long nrows, const float2 *twN,
-                              const float2 *twM, float scale, float *vr, int comp, int first, double2 *partials,
-                              cudaStream_t st)
+template <int M, int EPI, class PL>
+static cudaError_t launch_row(const DevCfg &c, const RowIn &in, const float2 *twN, const float2 *twM, float scale,
+                              float *vr, double2 *partials, cudaStream_t st)
 {
-  using PL = RowPlan<M>;
   constexpr int threads = PL::RW * (M / PL::P);
-  const size_t sm = sizeof(float2) * PL::RW * M;
+  const size_t sm = sizeof(float2) * PL::RW * sm_len<M, true>();
   auto kern = row_pass_kernel<M, PL::P, PL::RW, typename PL::R, EPI>;
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     attr = true;
   }
+  const long nrows = (long)c.n * c.n;
   long blocks = (nrows + PL::RW - 1) / PL::RW;
-  kern<<<(unsigned)blocks, threads, sm, st>>>(c, main, nyq, nrows, twN, twM, scale, vr, comp, first, partials);
+  kern<<<(unsigned)blocks, threads, sm, st>>>(c, in, nrows, twN, twM, scale, vr, partials);
   return cudaGetLastError();
 }
 
@@ -407,56 +462,47 @@ bool fft_supported(int n)
   }
 }
 
-#define GETHI_COL_DISPATCH(GENV)                                                                    \
-  switch (c.n) {                                                                                    \
-    case 2048: return launch_col<2048, GENV>(c, g, nyq, kind, src, tw, raw, st);                        \
-    case 1024: return launch_col<1024, GENV>(c, g, nyq, kind, src, tw, raw, st);                        \
-    case 512: return launch_col<512, GENV>(c, g, nyq, kind, src, tw, raw, st);                          \
-    case 384: return launch_col<384, GENV>(c, g, nyq, kind, src, tw, raw, st);                          \
-    case 256: return launch_col<256, GENV>(c, g, nyq, kind, src, tw, raw, st);                          \
-    case 128: return launch_col<128, GENV>(c, g, nyq, kind, src, tw, raw, st);                          \
-    case 64: return launch_col<64, GENV>(c, g, nyq, kind, src, tw, raw, st);                            \
-    case 32: return launch_col<32, GENV>(c, g, nyq, kind, src, tw, raw, st);                            \
-    case 24: return launch_col<24, GENV>(c, g, nyq, kind, src, tw, raw, st);                            \
-    case 16: return launch_col<16, GENV>(c, g, nyq, kind, src, tw, raw, st);                            \
-    default: return cudaErrorInvalidValue;                                                          \
+#define GETHI_COL_CASE(LV, MV) \
+  case LV: return launch_col<LV, MV>(c, g, nyq, nout, src, tw, out1, out2, st);
+#define GETHI_COL_DISPATCH(MV)                                                                        \
+  switch (c.n) {                                                                                      \
+    GETHI_COL_CASE(2048, MV) GETHI_COL_CASE(1024, MV) GETHI_COL_CASE(512, MV) GETHI_COL_CASE(384, MV) \
+    GETHI_COL_CASE(256, MV) GETHI_COL_CASE(128, MV) GETHI_COL_CASE(64, MV) GETHI_COL_CASE(32, MV)     \
+    GETHI_COL_CASE(24, MV) GETHI_COL_CASE(16, MV)                                                     \
+    default: return cudaErrorInvalidValue;                                                            \
   }
 
-cudaError_t col_pass(const DevCfg &c, const ColGeom &g, int nyq, int mode, int kind, const float2 *src,
-                     const float2 *tw, float2 *raw, cudaStream_t st)
+cudaError_t col_pass(const DevCfg &c, const ColGeom &g, int nyq, int mode, int nout, const float2 *src,
+                     const float2 *tw, float2 *out1, float2 *out2, cudaStream_t st)
 {
-  if (mode == 1) {
-    GETHI_COL_DISPATCH(1)
-  } else if (mode == 2) {
-    GETHI_COL_DISPATCH(2)
-  } else {
-    GETHI_COL_DISPATCH(0)
+  switch (mode) {
+    case 0: GETHI_COL_DISPATCH(0)
+    case 1: GETHI_COL_DISPATCH(1)
+    case 4: GETHI_COL_DISPATCH(4)
+    case 5: GETHI_COL_DISPATCH(5)
+    default: return cudaErrorInvalidValue;
   }
 }
 
-#define GETHI_ROW_DISPATCH(EPIV)                                                                          \
-  switch (c.m) {                                                                                          \
-    case 1024: return launch_row<1024, EPIV>(c, main, nyq, nrows, twN, twM, scale, vr, comp, first, partials, st); \
-    case 512: return launch_row<512, EPIV>(c, main, nyq, nrows, twN, twM, scale, vr, comp, first, partials, st);   \
-    case 256: return launch_row<256, EPIV>(c, main, nyq, nrows, twN, twM, scale, vr, comp, first, partials, st);   \
-    case 192: return launch_row<192, EPIV>(c, main, nyq, nrows, twN, twM, scale, vr, comp, first, partials, st);   \
-    case 128: return launch_row<128, EPIV>(c, main, nyq, nrows, twN, twM, scale, vr, comp, first, partials, st);   \
-    case 64: return launch_row<64, EPIV>(c, main, nyq, nrows, twN, twM, scale, vr, comp, first, partials, st);     \
-    case 32: return launch_row<32, EPIV>(c, main, nyq, nrows, twN, twM, scale, vr, comp, first, partials, st);     \
-    case 16: return launch_row<16, EPIV>(c, main, nyq, nrows, twN, twM, scale, vr, comp, first, partials, st);     \
-    case 12: return launch_row<12, EPIV>(c, main, nyq, nrows, twN, twM, scale, vr, comp, first, partials, st);     \
-    case 8: return launch_row<8, EPIV>(c, main, nyq, nrows, twN, twM, scale, vr, comp, first, partials, st);       \
-    default: return cudaErrorInvalidValue;                                                                \
+#define GETHI_ROW_CASE(MV, EPIV, PLAN) \
+  case MV: return launch_row<MV, EPIV, PLAN<MV>>(c, in, twN, twM, scale, vr, partials, st);
+#define GETHI_ROW_DISPATCH(EPIV, PLAN)                                                                        \
+  switch (c.m) {                                                                                              \
+    GETHI_ROW_CASE(1024, EPIV, PLAN) GETHI_ROW_CASE(512, EPIV, PLAN) GETHI_ROW_CASE(256, EPIV, PLAN)          \
+    GETHI_ROW_CASE(192, EPIV, PLAN) GETHI_ROW_CASE(128, EPIV, PLAN) GETHI_ROW_CASE(64, EPIV, PLAN)            \
+    GETHI_ROW_CASE(32, EPIV, PLAN) GETHI_ROW_CASE(16, EPIV, PLAN) GETHI_ROW_CASE(12, EPIV, PLAN)              \
+    GETHI_ROW_CASE(8, EPIV, PLAN)                                                                             \
+    default: return cudaErrorInvalidValue;                                                                    \
   }
 
-cudaError_t row_pass(const DevCfg &c, float2 *main, const float2 *nyq, const float2 *twN, const float2 *twM,
-                     float scale, int epi, float *vr, int comp, int first, double2 *partials, cudaStream_t st)
+cudaError_t row_pass(const DevCfg &c, const RowIn &in, const float2 *twN, const float2 *twM, float scale, int epi,
+                     float *vr, double2 *partials, cudaStream_t st)
 {
-  const long nrows = (long)c.n * c.n;
-  if (epi == 0) {
-    GETHI_ROW_DISPATCH(0)
-  } else {
-    GETHI_ROW_DISPATCH(1)
+  switch (epi) {
+    case 0: GETHI_ROW_DISPATCH(0, RowPlan)
+    case 2: GETHI_ROW_DISPATCH(2, RowPlanV)
+    case 3: GETHI_ROW_DISPATCH(3, RowPlan)
+    default: return cudaErrorInvalidValue;
   }
 }
 
@@ -468,7 +514,8 @@ cudaError_t finish_sigma(const double2 *partials, int np, double ncells, double 
 
 cudaError_t gen_modes(const DevCfg &c, float2 *out, int kind, cudaStream_t st)
 {
-  modes_kernel<<<1024, 256, 0, st>>>(c, out, kind);
+  (void)kind;
+  modes_kernel<<<1024, 256, 0, st>>>(c, out);
   return cudaGetLastError();
 }
 

@@ -20,12 +20,18 @@ struct ColGeom {
 
 bool fft_supported(int n);
 long row_pass_blocks(int n);
-// mode 0: transform in place; 1: draw delta_k (Philox or src) and store it to raw
-// (if non-null) before transforming field `kind`; 2: read delta_k from raw
-cudaError_t col_pass(const DevCfg &c, const ColGeom &g, int nyq, int mode, int kind, const float2 *src,
-                     const float2 *tw, float2 *raw, cudaStream_t st);
-cudaError_t row_pass(const DevCfg &c, float2 *main, const float2 *nyq, const float2 *twN, const float2 *twM,
-                     float scale, int epi, float *vr, int comp, int first, double2 *partials, cudaStream_t st);
+struct RowIn {
+  float2 *main[3];
+  const float2 *nyq[3];
+};
+// mode 0: out1 (or in place) = FFT(g.base); 1: draw delta_k (Philox or src) and
+// write FFT(delta) to g.base, FFT(phi) to out1 (nout >= 2), FFT(i kz phi) to
+// out2 (nout == 3); 4: out = FFT(i kx in); 5: out = FFT(i ky in)
+cudaError_t col_pass(const DevCfg &c, const ColGeom &g, int nyq, int mode, int nout, const float2 *src,
+                     const float2 *tw, float2 *out1, float2 *out2, cudaStream_t st);
+// epi 0: real row in place + sigma partials; 3: real row in place; 2: v_r from three rows
+cudaError_t row_pass(const DevCfg &c, const RowIn &in, const float2 *twN, const float2 *twM, float scale, int epi,
+                     float *vr, double2 *partials, cudaStream_t st);
 cudaError_t finish_sigma(const double2 *partials, int np, double ncells, double *stats, cudaStream_t st);
 cudaError_t gen_modes(const DevCfg &c, float2 *out, int kind, cudaStream_t st);
 
