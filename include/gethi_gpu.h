@@ -132,6 +132,30 @@ int gethi_gpu_download_modes(gethi_ctx *ctx, float *modes_k);
 /* per-stage device times of the last run, in ms (up to n entries) */
 int gethi_gpu_stage_times(const gethi_ctx *ctx, float *ms, int n);
 
+/* ---- projection without device allocation ----
+ * No counterpart in the reference.  mk_T_maps (src/pixelize.c:303-417) for
+ * callers that cannot let a library call cudaMalloc: they own all device
+ * memory through their own allocator or arena, or may not allocate once a run
+ * has started.  mass and dz are the caller's device grids (N^3 floats,
+ * [z][y][x], the HI mass and dz_rsd of get_HI); maps is the caller's device
+ * output [n_nu][12 n_side^2] (overwritten).  d, tables, offsets and prefac are
+ * the outputs of gethi_host_setup for the same parameters; nu_edges holds the
+ * n_nu+1 shell edges of a frequency file (NULL for a regular table).  stream is
+ * a cudaStream_t (NULL: default stream); the work is enqueued on it.
+ * The call allocates nothing: its scratch (a 16 MiB queue of samples whose
+ * FP32 key needs the FP64 check, counters, distance tables and shell edges,
+ * about 16.4 MiB in all) is a set of file-scope device arrays that every GPU
+ * loading the library holds until the process exits.  Limits: n_nu <= 4096,
+ * n_grid one of the supported sizes; larger requests return GETHI_E_ARG.  The
+ * first call on a device looks the arrays' addresses up (cudaGetSymbolAddress
+ * with that device current), so make that first call before any stream
+ * capture.  All calls share the arrays; the counters are cleared at the start
+ * of every call, and calls that overlap on the GPU (other streams, other host
+ * threads) race on them. */
+int gethi_project_noalloc(const gethi_params *p, const gethi_derived *d, const double *tables,
+                          const double *offsets, const double *prefac, const double *nu_edges,
+                          const float *mass, const float *dz, float *maps, void *stream);
+
 /* ---- measurement ---- */
 /* kernel classes timed when profiling is on (events around each launch) */
 #define GETHI_KC_ZPASS 0      /* Z pass drawing the modes on the fly (main block) */
