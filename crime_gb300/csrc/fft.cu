@@ -26,6 +26,7 @@
 // of the full inverse DFT of the Hermitian-extended spectrum (the reference
 // draws the kx=0 and kx=N/2 planes without Hermitian symmetry).
 #include <cstdio>
+#include <type_traits>
 
 #include "common.cuh"
 #include "fft.h"
@@ -104,7 +105,7 @@ __device__ __forceinline__ float vfac_over_k2(const DevCfg &c, int ii, int jj, i
 }
 
 template <int L, int P, int TX, class Rad, int MODE>
-__global__ void __launch_bounds__(TX *(L / P), MODE == 1 ? 1 : 2)
+__global__ void __launch_bounds__(TX *(L / P), 2)
     col_pass_kernel(DevCfg c, ColGeom g, int nyq, int nout, const float2 *__restrict__ src,
                     const float2 *__restrict__ tw, float2 *out1, float2 *out2)
 {
@@ -181,16 +182,15 @@ __global__ void __launch_bounds__(TX *(L / P), MODE == 1 ? 1 : 2)
 //   EPI 3: write the real row in place (x scale)
 //   EPI 2: rows of v_x (in0), v_y (in1), v_z (in2) -> v_r = sum_j v_j u_j into vr
 // ---------------------------------------------------------------------------
-template <int M, int P, int RW, class Rad>
-__device__ __forceinline__ void row_c2r(float2 *v, float2 *srow, const float2 *__restrict__ grow, float2 xm,
-                                        bool active, int t, const float2 *__restrict__ twN,
-                                        const float2 *__restrict__ twM)
+// c2r of one row held in shared memory (srow, skewed slots): Z[k] at the
+// first-stage positions, then the M-point inverse FFT; srow is reused as the
+// exchange buffer
+template <int M, int P, class Rad>
+__device__ __forceinline__ void row_c2r_smem(float2 *v, float2 *srow, float2 xm, int t, const float2 *__restrict__ twN,
+                                             const float2 *__restrict__ twM)
 {
   constexpr int T = M / P;
   constexpr int R0 = radix_first(Rad{});
-  // row into shared memory (coalesced), then Z[k] at the first-stage positions
-  for (int i = t; i < M; i += T) srow[sm_slot<true>(i, 1)] = active ? grow[i] : make_float2(0.f, 0.f);
-  __syncthreads();
 #pragma unroll
   for (int j = 0; j < P / R0; j++)
 #pragma unroll
@@ -208,8 +208,19 @@ __device__ __forceinline__ void row_c2r(float2 *v, float2 *srow, const float2 *_
   stockham_run<M, P, true>(v, srow, 1, t, twM, Rad{});
 }
 
+template <int M, int P, int RW, class Rad>
+__device__ __forceinline__ void row_c2r(float2 *v, float2 *srow, const float2 *__restrict__ grow, float2 xm,
+                                        bool active, int t, const float2 *__restrict__ twN,
+                                        const float2 *__restrict__ twM)
+{
+  constexpr int T = M / P;
+  for (int i = t; i < M; i += T) srow[sm_slot<true>(i, 1)] = active ? grow[i] : make_float2(0.f, 0.f);
+  __syncthreads();
+  row_c2r_smem<M, P, Rad>(v, srow, xm, t, twN, twM);
+}
+
 template <int M, int P, int RW, class Rad, int EPI>
-__global__ void __launch_bounds__(RW *(M / P), EPI == 2 ? 512 / (RW * (M / P)) : 1) row_pass_kernel(DevCfg c, RowIn in, long nrows,
+__global__ void __launch_bounds__(RW *(M / P), EPI == 2 ? 512 / (RW * (M / P)) : 3) row_pass_kernel(DevCfg c, RowIn in, long nrows,
                                                                const float2 *__restrict__ twN,
                                                                const float2 *__restrict__ twM, float scale,
                                                                float *vr, double2 *partials)
@@ -223,14 +234,24 @@ __global__ void __launch_bounds__(RW *(M / P), EPI == 2 ? 512 / (RW * (M / P)) :
   float2 *srow = smem + rl * sm_len<M, true>();
   float2 v[P];
   if constexpr (EPI == 2) {
+    // the three component rows of this row index go to three shared-memory
+    // regions at once, so all their loads are in flight together
+    float2 *sr[3];
+    float2 xm[3];
+#pragma unroll
+    for (int comp = 0; comp < 3; comp++) {
+      sr[comp] = smem + (comp * RW + rl) * sm_len<M, true>();
+      const float2 *grow = in.main[comp] + row * (long)M;
+      for (int i = t; i < M; i += T) sr[comp][sm_slot<true>(i, 1)] = active ? grow[i] : make_float2(0.f, 0.f);
+      xm[comp] = active ? in.nyq[comp][row] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
     float2 acc[P];
     const int iy = (int)(row % c.n), iz = (int)(row / c.n);
     const float y = c.dxf * (iy + 0.5f) - c.pos_obsf, z = c.dxf * (iz + 0.5f) - c.pos_obsf;
 #pragma unroll 1
     for (int comp = 0; comp < 3; comp++) {
-      if (comp) __syncthreads();  // shared row free again
-      row_c2r<M, P, RW, Rad>(v, srow, in.main[comp] + row * (long)M, active ? in.nyq[comp][row] : make_float2(0.f, 0.f),
-                             active, t, twN, twM);
+      row_c2r_smem<M, P, Rad>(v, sr[comp], xm[comp], t, twN, twM);
 #pragma unroll
       for (int j = 0; j < P / RL; j++)
 #pragma unroll
@@ -375,6 +396,11 @@ template <> struct ColPlan<64> { static constexpr int P = 8, TX = 16; using R = 
 template <> struct ColPlan<32> { static constexpr int P = 8, TX = 16; using R = Radices<8, 4>; };
 template <> struct ColPlan<24> { static constexpr int P = 12, TX = 16; using R = Radices<12, 2>; };
 template <> struct ColPlan<16> { static constexpr int P = 4, TX = 16; using R = Radices<4, 4>; };
+// columns of the drawing Z pass (modes kept in registers for up to three transforms)
+template <int L> struct ColPlanGen : ColPlan<L> {};
+template <> struct ColPlanGen<2048> { static constexpr int P = 16, TX = 2; using R = Radices<16, 16, 8>; };
+template <> struct ColPlanGen<1024> { static constexpr int P = 16, TX = 4; using R = Radices<16, 16, 4>; };
+template <> struct ColPlanGen<512> { static constexpr int P = 16, TX = 8; using R = Radices<16, 16, 2>; };
 // rows: M = N/2 (single field)
 template <> struct RowPlan<1024> { static constexpr int P = 32, RW = 4; using R = Radices<32, 8, 4>; };
 template <> struct RowPlan<512> { static constexpr int P = 32, RW = 16; using R = Radices<32, 16>; };
@@ -402,7 +428,7 @@ template <int L, int MODE>
 static cudaError_t launch_col(const DevCfg &c, const ColGeom &g, int nyq, int nout, const float2 *src,
                               const float2 *tw, float2 *out1, float2 *out2, cudaStream_t st)
 {
-  using PL = ColPlan<L>;
+  using PL = typename std::conditional<MODE == 1, ColPlanGen<L>, ColPlan<L>>::type;
   constexpr int threads = PL::TX * (L / PL::P);
   const size_t sm = sizeof(float2) * PL::TX * L;
   auto kern = col_pass_kernel<L, PL::P, PL::TX, typename PL::R, MODE>;
@@ -421,7 +447,7 @@ static cudaError_t launch_row(const DevCfg &c, const RowIn &in, const float2 *tw
                               float *vr, double2 *partials, cudaStream_t st)
 {
   constexpr int threads = PL::RW * (M / PL::P);
-  const size_t sm = sizeof(float2) * PL::RW * sm_len<M, true>();
+  const size_t sm = sizeof(float2) * PL::RW * sm_len<M, true>() * (EPI == 2 ? 3 : 1);
   auto kern = row_pass_kernel<M, PL::P, PL::RW, typename PL::R, EPI>;
   static bool attr = false;
   if (!attr) {

@@ -384,30 +384,39 @@ __global__ void __launch_bounds__(kProjThreads) project_kernel(DevCfg c, FastCon
     const float Xc = (float)ix - f.half_n, Yc = (float)iy - f.half_n, Zc = (float)iz - f.half_n;
     uint32_t cur = 0xFFFFFFFFu;
     float acc = 0.f;
+    // two sub-samples per iteration: independent FP32 chains for the scheduler
 #pragma unroll 1
-    for (int is = 0; is < kNSUB; is++) {
-      uint32_t key;
-      if (!key_fast(c, f, ef, Xc + f.xsp[is], Yc + f.ysp[is], Zc + f.zsp[is], dz, key)) {
-        const int slot = atomicAdd(&q_n, 1);
-        if (slot < kQueueCap) {
-          q_cell[slot] = (uint32_t)(tid + kProjThreads * k);
-          q_sub[slot] = (uint8_t)is;
-          q_val[slot] = msub;
-          q_dz[slot] = dz;
-        } else {
-          key = key_exact(c, ix, iy, iz, is, dz);
-          if (key != 0xFFFFFFFFu) tile_add(hkey, hval, maps, key, msub);
+    for (int is = 0; is < kNSUB; is += 2) {
+      uint32_t kk[2];
+      bool okk[2];
+#pragma unroll
+      for (int u = 0; u < 2; u++)
+        okk[u] = key_fast(c, f, ef, Xc + f.xsp[is + u], Yc + f.ysp[is + u], Zc + f.zsp[is + u], dz, kk[u]);
+#pragma unroll
+      for (int u = 0; u < 2; u++) {
+        uint32_t key = kk[u];
+        if (!okk[u]) {
+          const int slot = atomicAdd(&q_n, 1);
+          if (slot < kQueueCap) {
+            q_cell[slot] = (uint32_t)(tid + kProjThreads * k);
+            q_sub[slot] = (uint8_t)(is + u);
+            q_val[slot] = msub;
+            q_dz[slot] = dz;
+          } else {
+            key = key_exact(c, ix, iy, iz, is + u, dz);
+            if (key != 0xFFFFFFFFu) tile_add(hkey, hval, maps, key, msub);
+          }
+          nfall++;
+          continue;
         }
-        nfall++;
-        continue;
-      }
-      if (key == 0xFFFFFFFFu) continue;
-      if (key == cur) {
-        acc += msub;
-      } else {
-        if (cur != 0xFFFFFFFFu) tile_add(hkey, hval, maps, cur, acc);
-        cur = key;
-        acc = msub;
+        if (key == 0xFFFFFFFFu) continue;
+        if (key == cur) {
+          acc += msub;
+        } else {
+          if (cur != 0xFFFFFFFFu) tile_add(hkey, hval, maps, cur, acc);
+          cur = key;
+          acc = msub;
+        }
       }
     }
     if (cur != 0xFFFFFFFFu) tile_add(hkey, hval, maps, cur, acc);
