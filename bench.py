@@ -123,7 +123,7 @@ def algorithmic_bytes(cls, n, npix, n_nu):
         "zpass_raw": 8 * n3,        # read the raw modes, write the transformed column
         "ypass": 8 * n3,            # read + write 8 B/mode
         "xpass": 8 * n3,            # read 8 B/mode, write 4 B/cell
-        "xpass_vel": 32.0 / 3 * n3,  # read 8 B/mode, read (2 of 3 comps) + write v_r 4 B/cell
+        "xpass_vel": 16 * n3,       # read v_x, v_y, v_z (8 B/mode each), write v_r 4 B/cell
         "project": 8 * n3 + 4.0 * npix * n_nu,  # read delta, v_r; write the maps once
         "scale": 8.0 * npix * n_nu,
     }.get(cls)

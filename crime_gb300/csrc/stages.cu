@@ -205,15 +205,20 @@ __device__ __forceinline__ float atan01(float t)
 //   1+z from the FP32 table: |z1-z0| tr 3.7e-7 + 4 ulp(1+z); nu (approximate division): +2.7e-7 rel
 //   octant angle: atan01 8.6e-8 + ratio (2 ulp) 9e-8; w = 2a/pi or 1-2a/pi: 2.05e-7
 //   floor arguments: nside (dw + 6e-8 + 0.75 dcos) + 4 half-ulps at 1.5 nside
-__device__ __forceinline__ bool key_fast(const DevCfg &c, const FastConst &f, const float *ef, float X, float Y,
-                                         float Z, float dz, uint32_t &key)
+constexpr uint32_t kKeyInvalid = 0xFFFFFFFFu;    // outside the shells
+constexpr uint32_t kKeyUncertain = 0xFFFFFFFEu;  // FP32 cannot decide: use key_exact
+// (valid keys are < n_nu * 12 nside^2 <= 2^32 - 2, checked at set-up)
+
+__device__ __forceinline__ uint32_t key_fast(const DevCfg &c, const FastConst &f, const float *ef, int log2nn, float X,
+                                             float Y, float Z, float dz)
 {
   const float rho2 = fmaf(Y, Y, X * X);
   const float R2 = fmaf(Z, Z, rho2);
   const float iR = rsqrtf(R2);
   const float R = R2 * iR;
-  const float tr = R * f.idr_cell;
-  if (!(tr < (float)(kNZ - 2)) || !(rho2 > 0.f)) return false;
+  float tr = R * f.idr_cell;
+  const bool bad = !(tr < (float)(kNZ - 2)) || !(rho2 > 0.f);
+  tr = bad ? 0.f : tr;
   const int ir = (int)tr;
   const float fr = tr - (float)ir;
   const float z0 = __ldg(&c.z_r2z_f[ir]), z1 = __ldg(&c.z_r2z_f[ir + 1]);
@@ -221,41 +226,33 @@ __device__ __forceinline__ bool key_fast(const DevCfg &c, const FastConst &f, co
   const float nu = __fdividef(1420.40575177f, zz);
   const float mnu = 2.f * nu * (__fdividef(fabsf(z1 - z0) * tr * 3.7e-7f, zz) + 4.8e-7f + 2.7e-7f);
   int inu;
+  bool unc;
   if (c.regular_nu) {
     const float t = (nu - f.nu_min) * f.inv_dnu;
-    if (near_int(t, (mnu + 1.2e-7f * nu) * f.inv_dnu + 4e-7f * fabsf(t) + 1e-6f)) return false;
+    unc = near_int(t, (mnu + 1.2e-7f * nu) * f.inv_dnu + 4e-7f * fabsf(t) + 1e-6f);
     inu = (int)t;  // truncation, src/pixelize.c:369
   } else {
+    // edges ef[0..nn]: branch-free search for the last edge <= nu (inu = -1 below ef[0], nn at/above ef[nn])
     const int nn = c.n_nu;
-    const float e0 = ef[0], en = ef[nn];
-    if (nu < e0) {
-      if (e0 - nu < mnu) return false;
-      inu = -1;
-    } else if (nu >= en) {
-      if (nu - en < mnu) return false;
-      inu = nn;
-    } else {
-      int lo = 0, hi = nn;
-      while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (nu >= ef[mid]) lo = mid;
-        else hi = mid;
-      }
-      if (nu - ef[lo] < mnu || ef[lo + 1] - nu < mnu) return false;
-      inu = lo;
+    int lo = -1;
+#pragma unroll 1
+    for (int step = 1 << log2nn; step > 0; step >>= 1) {
+      const int cand = lo + step;
+      lo = (cand <= nn && nu >= ef[cand]) ? cand : lo;
     }
+    inu = lo;
+    const float below = lo >= 0 ? nu - ef[lo] : 1e30f;
+    const float above = lo < nn ? ef[lo + 1] - nu : 1e30f;
+    unc = below < mnu || above < mnu;
   }
-  if (inu < 0 || inu >= c.n_nu) {
-    key = 0xFFFFFFFFu;
-    return true;
-  }
+  if (bad || unc) return kKeyUncertain;
+  if (inu < 0 || inu >= c.n_nu) return kKeyInvalid;
   // ---- pixel (RING scheme)
   const int nside = (int)c.nside;
   const float fn = (float)nside;
   const float cth = Z * iR;
   const float za = fabsf(cth);
   const float dcos = 3.7e-7f;
-  if (fabsf(za - 0.6666667f) < 2.f * dcos + 6e-8f) return false;
   // octant decomposition: a = atan(min/max) in [0, pi/4]; tt = 2 phi/pi = q + w
   const float ax = fabsf(X), ay = fabsf(Y);
   const bool swap = ay > ax;
@@ -263,26 +260,26 @@ __device__ __forceinline__ bool key_fast(const DevCfg &c, const FastConst &f, co
   const bool upper = Y >= 0.f, right = X >= 0.f;
   int q = upper ? (right ? 0 : 1) : (right ? 3 : 2);
   // w = a2 when the octant runs counter-clockwise from the quadrant start, else 1 - a2
-  const bool ccw = (q == 0 || q == 2) ? !swap : swap;
+  const bool ccw = ((q & 1) == 0) ? !swap : swap;
   float w = ccw ? a2 : 1.f - a2;
-  if (w >= 1.f) {
-    w -= 1.f;
-    q = (q + 1) & 3;
-  }
+  const bool wrap = w >= 1.f;
+  w = wrap ? w - 1.f : w;
+  q = wrap ? ((q + 1) & 3) : q;
   const float dw = 2.05e-7f;
   const int npix = (int)c.npix;
+  if (fabsf(za - 0.6666667f) < 2.f * dcos + 6e-8f) return kKeyUncertain;
   int pix;
   if (za <= 0.6666667f) {
     const float t2 = fn * cth * 0.75f;
     const float v = fn * (0.5f + w);
     const float v1 = v - t2, v2 = v + t2;
     const float mu = 2.f * (fn * (dw + 6e-8f + 0.75f * dcos) + 2.f * 1.2e-7f * (1.5f * fn + 1.f));
-    if (near_int(v1, mu) || near_int(v2, mu)) return false;
-    const int jp = (int)floorf(v1) + q * nside, jm = (int)floorf(v2) + q * nside;
-    const int ring = nside + 1 + jp - jm;
-    const int num = jp + jm - nside + (1 - (ring & 1)) + 1;  // >= -1
-    int ip = (num + (num < 0)) >> 1;                          // C division by 2 (toward zero)
-    if (ip >= 4 * nside) ip -= 4 * nside;
+    if (near_int(v1, mu) || near_int(v2, mu)) return kKeyUncertain;
+    const int f1 = (int)floorf(v1), f2 = (int)floorf(v2);
+    const int ring = nside + 1 + f1 - f2;  // jp - jm: the q nside terms cancel
+    const int num = f1 + f2 + (2 * q - 1) * nside + (1 - (ring & 1)) + 1;  // jp + jm - nside + kshift + 1 >= -1
+    int ip = (num + (num < 0)) >> 1;                                        // C division by 2
+    ip = ip >= 4 * nside ? ip - 4 * nside : ip;
     pix = 2 * nside * (nside - 1) + (ring - 1) * 4 * nside + ip;
   } else {
     // polar caps: nside sqrt(3(1-|z|)) = nside (rho/R) / sqrt((1+|z|)/3)
@@ -290,16 +287,16 @@ __device__ __forceinline__ bool key_fast(const DevCfg &c, const FastConst &f, co
     const float tmp = fn * st * rsqrtf((1.f + za) * (1.f / 3.f));
     const float u3 = w * tmp, u4 = (1.f - w) * tmp;
     const float mu = 2.f * (tmp * (dw + 1e-6f) + 2.f * 1.2e-7f * (tmp + 1.f));
-    if (near_int(u3, mu) || near_int(u4, mu) || w < 2.f * dw || 1.f - w < 2.f * dw) return false;
     const int jp = (int)u3, jm = (int)u4;
     const int ring = jp + jm + 1;
     const float u5 = w * (float)ring;
-    if (near_int(u5, 2.f * ((float)ring * dw + 2.4e-7f * (u5 + 1.f)))) return false;
+    if (near_int(u3, mu) || near_int(u4, mu) || w < 2.f * dw || 1.f - w < 2.f * dw ||
+        near_int(u5, 2.f * ((float)ring * dw + 2.4e-7f * (u5 + 1.f))))
+      return kKeyUncertain;
     const int ip = q * ring + (int)u5;  // floor(tt ring) < 4 ring
     pix = (cth > 0) ? 2 * ring * (ring - 1) + ip : npix - 2 * ring * (ring + 1) + ip;
   }
-  key = (uint32_t)pix + (uint32_t)npix * (uint32_t)inu;
-  return true;
+  return (uint32_t)pix + (uint32_t)npix * (uint32_t)inu;
 }
 
 // ---------------------------------------------------------------------------
@@ -363,6 +360,8 @@ __global__ void __launch_bounds__(kProjThreads) project_kernel(DevCfg c, FastCon
   if (tid == 0) q_n = 0;
   __syncthreads();
   const float *ef = smem_edges ? sef : c.nu_edges_f;
+  int log2nn = 0;
+  while ((1 << (log2nn + 1)) - 2 < c.n_nu) log2nn++;  // steps 2^L..1 from -1 reach index n_nu
   const int n = c.n, nt = n / kTile;
   const int bx = blockIdx.x % nt, by = (blockIdx.x / nt) % nt, bz = blockIdx.x / (nt * nt);
   const float sigma2 = FUSED ? (float)stats[1] : 0.f;
@@ -382,34 +381,28 @@ __global__ void __launch_bounds__(kProjThreads) project_kernel(DevCfg c, FastCon
     }
     const float msub = mass / 10.f;  // src/pixelize.c:356
     const float Xc = (float)ix - f.half_n, Yc = (float)iy - f.half_n, Zc = (float)iz - f.half_n;
+    uint32_t keys[kNSUB];
+#pragma unroll
+    for (int is = 0; is < kNSUB; is++)
+      keys[is] = key_fast(c, f, ef, log2nn, Xc + f.xsp[is], Yc + f.ysp[is], Zc + f.zsp[is], dz);
     uint32_t cur = 0xFFFFFFFFu;
     float acc = 0.f;
-    // two sub-samples per iteration: independent FP32 chains for the scheduler
-#pragma unroll 1
-    for (int is = 0; is < kNSUB; is += 2) {
-      uint32_t kk[2];
-      bool okk[2];
 #pragma unroll
-      for (int u = 0; u < 2; u++)
-        okk[u] = key_fast(c, f, ef, Xc + f.xsp[is + u], Yc + f.ysp[is + u], Zc + f.zsp[is + u], dz, kk[u]);
-#pragma unroll
-      for (int u = 0; u < 2; u++) {
-        uint32_t key = kk[u];
-        if (!okk[u]) {
-          const int slot = atomicAdd(&q_n, 1);
-          if (slot < kQueueCap) {
-            q_cell[slot] = (uint32_t)(tid + kProjThreads * k);
-            q_sub[slot] = (uint8_t)(is + u);
-            q_val[slot] = msub;
-            q_dz[slot] = dz;
-          } else {
-            key = key_exact(c, ix, iy, iz, is + u, dz);
-            if (key != 0xFFFFFFFFu) tile_add(hkey, hval, maps, key, msub);
-          }
-          nfall++;
-          continue;
+    for (int is = 0; is < kNSUB; is++) {
+      const uint32_t key = keys[is];
+      if (key == kKeyUncertain) {
+        nfall++;
+        const int slot = atomicAdd(&q_n, 1);
+        if (slot < kQueueCap) {
+          q_cell[slot] = (uint32_t)(tid + kProjThreads * k);
+          q_sub[slot] = (uint8_t)is;
+          q_val[slot] = msub;
+          q_dz[slot] = dz;
+        } else {
+          const uint32_t ke = key_exact(c, ix, iy, iz, is, dz);
+          if (ke != 0xFFFFFFFFu) tile_add(hkey, hval, maps, ke, msub);
         }
-        if (key == 0xFFFFFFFFu) continue;
+      } else if (key != kKeyInvalid) {
         if (key == cur) {
           acc += msub;
         } else {
@@ -484,6 +477,8 @@ __global__ void sample_keys_kernel(DevCfg c, FastConst f, const float *__restric
   const int n = c.n;
   const long total = (long)n * n * n;
   int nfall = 0;
+  int log2nn = 0;
+  while ((1 << (log2nn + 1)) - 2 < c.n_nu) log2nn++;  // steps 2^L..1 from -1 reach index n_nu
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
     const int ix = (int)(i % n);
     const long rest = i / n;
@@ -491,10 +486,9 @@ __global__ void sample_keys_kernel(DevCfg c, FastConst f, const float *__restric
     const float dz = dzg[i];
     const float Xc = (float)ix - f.half_n, Yc = (float)iy - f.half_n, Zc = (float)iz - f.half_n;
     for (int is = 0; is < kNSUB; is++) {
-      uint32_t key;
-      bool ok = false;
-      if (!exact) ok = key_fast(c, f, c.nu_edges_f, Xc + f.xsp[is], Yc + f.ysp[is], Zc + f.zsp[is], dz, key);
-      if (!ok) {
+      uint32_t key = kKeyUncertain;
+      if (!exact) key = key_fast(c, f, c.nu_edges_f, log2nn, Xc + f.xsp[is], Yc + f.ysp[is], Zc + f.zsp[is], dz);
+      if (key == kKeyUncertain) {
         key = key_exact(c, ix, iy, iz, is, dz);
         nfall++;
       }
