@@ -309,11 +309,16 @@ __device__ __forceinline__ uint32_t key_fast(const DevCfg &c, const FastConst &f
 // whole block at the end of the tile.
 // ---------------------------------------------------------------------------
 constexpr int kProjThreads = 256;
-constexpr int kTile = 8;
+constexpr int kTile = 8;  // tiles are 8 x 8 x (4 zsteps) cells: 256 threads cover 8 x 8 x 4 cells per step
+__host__ __device__ inline int tile_zsteps(int n) { return n % 16 == 0 ? 4 : 2; }
 constexpr int kQueueCap = 1024;
 constexpr int kHash = 4096;
 constexpr int kProbe = 16;
 constexpr int kEdgesSmem = 516;
+#ifndef PROJ_UNROLL
+#define PROJ_UNROLL 2
+#endif
+constexpr int kProjUnroll = PROJ_UNROLL;  // sub-samples per loop iteration
 
 __device__ __forceinline__ void tile_add(uint32_t *hkey, float *hval, float *maps, uint32_t key, float val)
 {
@@ -362,13 +367,13 @@ __global__ void __launch_bounds__(kProjThreads) project_kernel(DevCfg c, FastCon
   const float *ef = smem_edges ? sef : c.nu_edges_f;
   int log2nn = 0;
   while ((1 << (log2nn + 1)) - 2 < c.n_nu) log2nn++;  // steps 2^L..1 from -1 reach index n_nu
-  const int n = c.n, nt = n / kTile;
+  const int n = c.n, nt = n / kTile, zsteps = tile_zsteps(n);
   const int bx = blockIdx.x % nt, by = (blockIdx.x / nt) % nt, bz = blockIdx.x / (nt * nt);
   const float sigma2 = FUSED ? (float)stats[1] : 0.f;
   int nfall = 0;
 #pragma unroll 1
-  for (int k = 0; k < 2; k++) {
-    const int ix = bx * kTile + (tid & 7), iy = by * kTile + ((tid >> 3) & 7), iz = bz * kTile + (tid >> 6) + 4 * k;
+  for (int k = 0; k < zsteps; k++) {
+    const int ix = bx * kTile + (tid & 7), iy = by * kTile + ((tid >> 3) & 7), iz = bz * 4 * zsteps + (tid >> 6) + 4 * k;
     const long i = ((long)iz * n + iy) * n + ix;
     float mass, dz;
     if (FUSED) {
@@ -381,15 +386,11 @@ __global__ void __launch_bounds__(kProjThreads) project_kernel(DevCfg c, FastCon
     }
     const float msub = mass / 10.f;  // src/pixelize.c:356
     const float Xc = (float)ix - f.half_n, Yc = (float)iy - f.half_n, Zc = (float)iz - f.half_n;
-    uint32_t keys[kNSUB];
-#pragma unroll
-    for (int is = 0; is < kNSUB; is++)
-      keys[is] = key_fast(c, f, ef, log2nn, Xc + f.xsp[is], Yc + f.ysp[is], Zc + f.zsp[is], dz);
     uint32_t cur = 0xFFFFFFFFu;
     float acc = 0.f;
-#pragma unroll
+#pragma unroll kProjUnroll
     for (int is = 0; is < kNSUB; is++) {
-      const uint32_t key = keys[is];
+      const uint32_t key = key_fast(c, f, ef, log2nn, Xc + f.xsp[is], Yc + f.ysp[is], Zc + f.zsp[is], dz);
       if (key == kKeyUncertain) {
         nfall++;
         const int slot = atomicAdd(&q_n, 1);
@@ -433,7 +434,7 @@ __global__ void __launch_bounds__(kProjThreads) project_kernel(DevCfg c, FastCon
       continue;
     }
     const int lc = (int)q_cell[j], k = lc / kProjThreads, t = lc % kProjThreads;
-    const int ix = bx * kTile + (t & 7), iy = by * kTile + ((t >> 3) & 7), iz = bz * kTile + (t >> 6) + 4 * k;
+    const int ix = bx * kTile + (t & 7), iy = by * kTile + ((t >> 3) & 7), iz = bz * 4 * zsteps + (t >> 6) + 4 * k;
     const uint32_t key = key_exact(c, ix, iy, iz, q_sub[j], q_dz[j]);
     if (key != 0xFFFFFFFFu) tile_add(hkey, hval, maps, key, q_val[j]);
   }
@@ -451,12 +452,12 @@ __global__ void fixup_kernel(DevCfg c, const FallbackEntry *__restrict__ fq, con
                              long fq_cap, float *__restrict__ maps)
 {
   const long cnt = min((long)*reinterpret_cast<const unsigned long long *>(&counters[2]), fq_cap);
-  const int nt = c.n / kTile;
+  const int nt = c.n / kTile, zsteps = tile_zsteps(c.n);
   for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < cnt; j += (long)gridDim.x * blockDim.x) {
     const FallbackEntry e = fq[j];
     const int bx = e.tile % nt, by = (e.tile / nt) % nt, bz = e.tile / (nt * nt);
     const int lc = (int)(e.sub >> 4), is = (int)(e.sub & 15), k = lc / kProjThreads, t = lc % kProjThreads;
-    const int ix = bx * kTile + (t & 7), iy = by * kTile + ((t >> 3) & 7), iz = bz * kTile + (t >> 6) + 4 * k;
+    const int ix = bx * kTile + (t & 7), iy = by * kTile + ((t >> 3) & 7), iz = bz * 4 * zsteps + (t >> 6) + 4 * k;
     const uint32_t key = key_exact(c, ix, iy, iz, is, e.dz);
     if (key != 0xFFFFFFFFu) atomicAdd(&maps[key], e.msub);
   }
@@ -544,9 +545,10 @@ size_t fallback_entry_bytes() { return sizeof(FallbackEntry); }
 cudaError_t project(const DevCfg &c, const double *stats, const float *a, const float *b, int fused, float *maps,
                     int *counters, void *fq, long fq_cap, cudaStream_t st)
 {
-  if (c.n % kTile) return cudaErrorInvalidValue;
+  const int tz = 4 * tile_zsteps(c.n);
+  if (c.n % kTile || c.n % tz) return cudaErrorInvalidValue;
   const long nt = c.n / kTile;
-  const unsigned blocks = (unsigned)(nt * nt * nt);
+  const unsigned blocks = (unsigned)(nt * nt * (c.n / tz));
   FastConst f = fast_const(c);
   FallbackEntry *q = reinterpret_cast<FallbackEntry *>(fq);
   if (fused) project_kernel<true><<<blocks, kProjThreads, 0, st>>>(c, f, stats, a, b, maps, counters, q, fq_cap);
