@@ -49,42 +49,51 @@ __device__ __forceinline__ float pk_lookup(const DevCfg &c, float lgk)  // src/c
 }
 
 // Production draw: amplitude law of src/fourier.c:292-298 with Philox4x32-10.
-// ctr = (mode id lo, hi, 0, 0), key = (seed, 0x4352494D); phase from out.x,
-// modulus from w = 1 - out.y/2^32 (never 0).
-__device__ __forceinline__ float2 philox_mode(const DevCfg &c, int ii, int jj, int kk, float k2)
+// One Philox call serves the modes kz and kz + N/2 (same ky, kx):
+// ctr = (id lo, id hi, 0, 0) with id = kx + (N/2+1)(ky + N (kz mod N/2)),
+// key = (seed, 0x4352494D); the lower mode uses words (x, y), the upper (z, w).
+// Phase = 2 pi word0/2^32; modulus from ln(1 - word1/2^32).
+__device__ __forceinline__ uint4 philox_for_pair(const DevCfg &c, int ii0, int jj, int kk)
 {
+  uint64_t id = (uint64_t)kk + (uint64_t)(c.m + 1) * ((uint64_t)jj + (uint64_t)c.n * ii0);
+  return philox4x32_10(make_uint4((uint32_t)id, (uint32_t)(id >> 32), 0u, 0u), make_uint2(c.seed, 0x4352494Du));
+}
+
+__device__ __forceinline__ float2 mode_from_words(const DevCfg &c, int ii, int jj, int kk, uint32_t wph, uint32_t wmod)
+{
+  const int n = c.n;
+  float kz = kval(ii, n, c.dk), ky = kval(jj, n, c.dk), kx = kval(kk, n, c.dk);
+  float k2 = kx * kx + ky * ky + kz * kz;
+  if (k2 <= 0.f) return make_float2(0.f, 0.f);
   float lgk = 0.5f * log10f(k2);
   float sigma2 = pk_lookup(c, lgk) * c.idk3;
   if (c.do_smoothing) sigma2 *= expf(-c.r2_smooth * k2);
-  uint64_t id = (uint64_t)kk + (uint64_t)(c.m + 1) * ((uint64_t)jj + (uint64_t)c.n * ii);
-  uint4 o = philox4x32_10(make_uint4((uint32_t)id, (uint32_t)(id >> 32), 0u, 0u), make_uint2(c.seed, 0x4352494Du));
-  float u = (float)o.x * 2.3283064365386963e-10f;
-  // ln(1 - u2), u2 = out.y/2^32: log1p keeps the relative accuracy for small u2,
-  // the direct log of the exact remainder 2^32 - out.y for u2 >= 1/2
-  float lnw = o.y < 0x80000000u ? log1pf(-(float)o.y * 2.3283064365386963e-10f)
-                                : logf((float)(0u - o.y) * 2.3283064365386963e-10f);
+  float u = (float)wph * 2.3283064365386963e-10f;
+  // ln(1 - u2): log1p keeps the relative accuracy for small u2, the direct log of
+  // the exact remainder 2^32 - word for u2 >= 1/2
+  float lnw = wmod < 0x80000000u ? log1pf(-(float)wmod * 2.3283064365386963e-10f)
+                                 : logf((float)(0u - wmod) * 2.3283064365386963e-10f);
   float amp = sqrtf(-sigma2 * lnw);
   float s, co;
   sincospif(2.f * u, &s, &co);
   return make_float2(amp * co, amp * s);
 }
 
-// Mode (kz index ii, ky index jj, kx index kk) of field `kind`.
-// src != nullptr: delta_k from a host spectrum in the reference layout.
+// delta_k of mode (kz index ii, ky index jj, kx index kk); src != nullptr: a
+// host spectrum in the reference layout [kz][ky][N/2+1]
 __device__ __forceinline__ float2 mode_value(const DevCfg &c, int ii, int jj, int kk, int kind,
                                              const float2 *__restrict__ src)
 {
+  (void)kind;
   const int n = c.n;
-  float kz = kval(ii, n, c.dk), ky = kval(jj, n, c.dk), kx = kval(kk, n, c.dk);
-  float k2 = kx * kx + ky * ky + kz * kz;
-  if (k2 <= 0.f) return make_float2(0.f, 0.f);
-  float2 d = src ? __ldg(&src[((size_t)ii * n + jj) * (size_t)(c.m + 1) + kk]) : philox_mode(c, ii, jj, kk, k2);
-  if (kind == FIELD_DENS) return d;
-  float f = c.vfac / k2;  // phi_k = delta_k f0 H0 / k^2, src/fourier.c:298
-  if (kind == FIELD_VPOT) return cscale(d, f);
-  // v_j = i k_j phi_k; the derivative of a Nyquist component is set to zero
-  float kj = kind == FIELD_VX ? (2 * kk == n ? 0.f : kx) : kind == FIELD_VY ? (2 * jj == n ? 0.f : ky) : (2 * ii == n ? 0.f : kz);
-  return cmul_i(cscale(d, f * kj));
+  if (src) {
+    float kz = kval(ii, n, c.dk), ky = kval(jj, n, c.dk), kx = kval(kk, n, c.dk);
+    if (kx * kx + ky * ky + kz * kz <= 0.f) return make_float2(0.f, 0.f);
+    return __ldg(&src[((size_t)ii * n + jj) * (size_t)(c.m + 1) + kk]);
+  }
+  const int half = 2 * ii >= n ? 1 : 0;
+  const uint4 o = philox_for_pair(c, ii - half * (n / 2), jj, kk);
+  return half ? mode_from_words(c, ii, jj, kk, o.z, o.w) : mode_from_words(c, ii, jj, kk, o.x, o.y);
 }
 
 // ---------------------------------------------------------------------------
@@ -120,14 +129,28 @@ __global__ void __launch_bounds__(TX *(L / P), 2)
   float2 v[P];
   if constexpr (MODE == 1) {
     float2 d[P];
+    static_assert(R0 % 2 == 0, "modes kz and kz + N/2 sit in first-stage slots r and r + R0/2");
 #pragma unroll
     for (int j = 0; j < P / R0; j++)
 #pragma unroll
-      for (int r = 0; r < R0; r++) {
-        const int e = t + T * j + (L / R0) * r;
-        d[j * R0 + r] = active ? mode_value(c, e, ky, kx, FIELD_DENS, src) : make_float2(0.f, 0.f);
-        v[j * R0 + r] = d[j * R0 + r];
+      for (int r = 0; r < R0 / 2; r++) {
+        const int e = t + T * j + (L / R0) * r;  // e < N/2; its partner e + N/2 is slot r + R0/2
+        float2 lo = make_float2(0.f, 0.f), hi = lo;
+        if (active) {
+          if (src) {
+            lo = mode_value(c, e, ky, kx, FIELD_DENS, src);
+            hi = mode_value(c, e + L / 2, ky, kx, FIELD_DENS, src);
+          } else {
+            const uint4 o = philox_for_pair(c, e, ky, kx);
+            lo = mode_from_words(c, e, ky, kx, o.x, o.y);
+            hi = mode_from_words(c, e + L / 2, ky, kx, o.z, o.w);
+          }
+        }
+        d[j * R0 + r] = lo;
+        d[j * R0 + r + R0 / 2] = hi;
       }
+#pragma unroll
+    for (int i = 0; i < P; i++) v[i] = d[i];
 #pragma unroll 1
     for (int f = 0; f < nout; f++) {
       if (f > 0) {
@@ -214,7 +237,11 @@ __device__ __forceinline__ void row_c2r(float2 *v, float2 *srow, const float2 *_
                                         const float2 *__restrict__ twM)
 {
   constexpr int T = M / P;
-  for (int i = t; i < M; i += T) srow[sm_slot<true>(i, 1)] = active ? grow[i] : make_float2(0.f, 0.f);
+  float2 ld[P];
+#pragma unroll
+  for (int j = 0; j < P; j++) ld[j] = active ? grow[t + T * j] : make_float2(0.f, 0.f);
+#pragma unroll
+  for (int j = 0; j < P; j++) srow[sm_slot<true>(t + T * j, 1)] = ld[j];
   __syncthreads();
   row_c2r_smem<M, P, Rad>(v, srow, xm, t, twN, twM);
 }
@@ -242,7 +269,11 @@ __global__ void __launch_bounds__(RW *(M / P), EPI == 2 ? 512 / (RW * (M / P)) :
     for (int comp = 0; comp < 3; comp++) {
       sr[comp] = smem + (comp * RW + rl) * sm_len<M, true>();
       const float2 *grow = in.main[comp] + row * (long)M;
-      for (int i = t; i < M; i += T) sr[comp][sm_slot<true>(i, 1)] = active ? grow[i] : make_float2(0.f, 0.f);
+      float2 ld[P];
+#pragma unroll
+      for (int j = 0; j < P; j++) ld[j] = active ? grow[t + T * j] : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int j = 0; j < P; j++) sr[comp][sm_slot<true>(t + T * j, 1)] = ld[j];
       xm[comp] = active ? in.nyq[comp][row] : make_float2(0.f, 0.f);
     }
     __syncthreads();

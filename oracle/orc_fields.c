@@ -73,8 +73,10 @@ void orc_modes_mt(const orc_config *c, const orc_derived *d, const double *logk,
 }
 
 /* Production modes: the same amplitude law with counter-based draws.
- * ctr = (mode id lo, mode id hi, 0, 0), key = (seed, 0x4352494D); the phase
- * uses out[0]/2^32 and the modulus w = (2^32 - out[1])/2^32 = 1 - u. */
+ * One Philox4x32-10 call serves the modes kz and kz + N/2 (same ky, kx):
+ * ctr = (id lo, id hi, 0, 0), id = kx + (N/2+1)(ky + N (kz mod N/2)),
+ * key = (seed, 0x4352494D); the lower mode uses words 0,1, the upper 2,3.
+ * Phase = 2 pi w0/2^32; modulus w = (2^32 - w1)/2^32 = 1 - u. */
 void orc_modes_philox(const orc_config *c, const orc_derived *d, const double *logk,
                       const double *pk, float *dens_k)
 {
@@ -84,6 +86,7 @@ void orc_modes_philox(const orc_config *c, const orc_derived *d, const double *l
 #pragma omp parallel for schedule(static)
   for (int ii = 0; ii < n; ii++) {
     double kz = kval(ii, n, dk);
+    int half = 2 * ii >= n, ii0 = ii - half * (n / 2);
     for (int jj = 0; jj < n; jj++) {
       double ky = kval(jj, n, dk);
       for (int kk = 0; kk <= n / 2; kk++) {
@@ -94,11 +97,13 @@ void orc_modes_philox(const orc_config *c, const orc_derived *d, const double *l
         double lgk = 0.5 * log10(k_mod2);
         double sigma2 = orc_pk_linear0(d, logk, pk, lgk) * idk3;
         if (d->do_smoothing) sigma2 *= exp(-d->r2_smooth * k_mod2);
-        uint32_t ctr[4] = {(uint32_t)index, (uint32_t)((uint64_t)index >> 32), 0, 0};
+        uint64_t id = (uint64_t)kk + (uint64_t)h * ((uint64_t)jj + (uint64_t)n * ii0);
+        uint32_t ctr[4] = {(uint32_t)id, (uint32_t)(id >> 32), 0, 0};
         uint32_t key[2] = {c->seed, 0x4352494Du}, o[4];
         orc_philox4x32_10(ctr, key, o);
-        double phase = 2 * M_PI * (o[0] * (1.0 / 4294967296.0));
-        double w = (4294967296.0 - (double)o[1]) * (1.0 / 4294967296.0);
+        uint32_t w0 = half ? o[2] : o[0], w1 = half ? o[3] : o[1];
+        double phase = 2 * M_PI * (w0 * (1.0 / 4294967296.0));
+        double w = (4294967296.0 - (double)w1) * (1.0 / 4294967296.0);
         double mod = sqrt(-sigma2 * log(w));
         dens_k[2 * index] = (float)(mod * cos(phase));
         dens_k[2 * index + 1] = (float)(mod * sin(phase));
