@@ -371,18 +371,28 @@ __global__ void __launch_bounds__(kProjThreads) project_kernel(DevCfg c, FastCon
   const int bx = blockIdx.x % nt, by = (blockIdx.x / nt) % nt, bz = blockIdx.x / (nt * nt);
   const float sigma2 = FUSED ? (float)stats[1] : 0.f;
   int nfall = 0;
+  // all of this thread's cells are loaded up front (up to 4 load pairs in flight)
+  const int ix = bx * kTile + (tid & 7), iy = by * kTile + ((tid >> 3) & 7), iz0 = bz * 4 * zsteps + (tid >> 6);
+  float va[4], vb[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const long i = ((long)(iz0 + 4 * k) * n + iy) * n + ix;
+    va[k] = k < zsteps ? a[i] : 0.f;
+    vb[k] = k < zsteps ? b[i] : 0.f;
+  }
 #pragma unroll 1
   for (int k = 0; k < zsteps; k++) {
-    const int ix = bx * kTile + (tid & 7), iy = by * kTile + ((tid >> 3) & 7), iz = bz * 4 * zsteps + (tid >> 6) + 4 * k;
-    const long i = ((long)iz * n + iy) * n + ix;
+    const int iz = iz0 + 4 * k;
+    const float ak = k == 0 ? va[0] : k == 1 ? va[1] : k == 2 ? va[2] : va[3];
+    const float bk = k == 0 ? vb[0] : k == 1 ? vb[1] : k == 2 ? vb[2] : vb[3];
     float mass, dz;
     if (FUSED) {
-      CellHI h = cell_hi(c, sigma2, ix, iy, iz, a[i], b[i]);
+      CellHI h = cell_hi(c, sigma2, ix, iy, iz, ak, bk);
       mass = h.mass;
       dz = h.dz;
     } else {
-      mass = a[i];
-      dz = b[i];
+      mass = ak;
+      dz = bk;
     }
     const float msub = mass / 10.f;  // src/pixelize.c:356
     const float Xc = (float)ix - f.half_n, Yc = (float)iy - f.half_n, Zc = (float)iz - f.half_n;
