@@ -30,13 +30,13 @@ NU21 = 1420.40575177
 # Synthetic configurations (seeded; the P(k) is the built-in EH no-wiggle table).
 CONFIGS = {
     "c0": dict(n_grid=128, l_box=1500.0, zmin=0.5, zmax=1.0, n_nu=30, n_side=64, seed=1001, do_rsd=0,
-               bias_model="const", b_HI=1.0, velocity_mode="spectral"),
+               bias_model="const", b_HI=1.0, velocity_mode="spectral", gaussianise=1),
     "c1": dict(n_grid=512, l_box=2500.0, zmin=0.3, zmax=2.0, n_nu=150, n_side=256, seed=2001, do_rsd=1,
-               velocity_mode="spectral"),
+               velocity_mode="spectral", gaussianise=1),
     "c2": dict(n_grid=1024, l_box=4000.0, zmin=0.3, zmax=2.0, n_nu=150, n_side=512, seed=3001, do_rsd=1,
-               velocity_mode="spectral"),
+               velocity_mode="spectral", gaussianise=1),
     "c4": dict(n_grid=2048, l_box=6000.0, zmin=0.2, zmax=2.5, n_nu=256, n_side=1024, seed=5001, do_rsd=1,
-               velocity_mode="spectral"),
+               velocity_mode="spectral", gaussianise=1),
 }
 COSMO = dict(omega_M=0.315, omega_L=0.685, omega_B=0.049, h=0.67, w=-1.0, ns=0.96, sigma_8=0.83)
 

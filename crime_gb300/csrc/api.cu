@@ -54,6 +54,7 @@ struct gethi_ctx {
   void *staging = nullptr;  // pinned host copy of the per-realisation inputs
   void *fq = nullptr;       // queue of samples whose FP32 key is uncertain
   long fq_cap = 0;
+  float2 *pg = nullptr, *pgn = nullptr;  // Gaussianised spectrum (gaussianise=1)
 };
 
 namespace {
@@ -199,6 +200,7 @@ void collect_kernel_times(gethi_ctx *c)
 }
 
 // One field: Z pass (modes generated on the fly), Y pass, X pass with epilogue.
+
 // Geometries of the column sets (main block and Nyquist plane, Z and Y axes).
 struct Geoms {
   ColGeom zm, zn, ym, yn;
@@ -207,6 +209,55 @@ Geoms geoms(float2 *main, float2 *nyq, long n, long m)
 {
   return {geom(main, n * m, 0, 1, n * m, n * m), geom(nyq, n, 0, 1, n, n), geom(main, m, n * m, 1, m, n * m),
           geom(nyq, n, 0, n, 1, n)};
+}
+
+int plain_c2r(gethi_ctx *c, float2 *main, float2 *nyq, float scale)
+{
+  const DevCfg &g = c->cfg;
+  const long n = g.n, m = g.m;
+  cudaStream_t st = c->stream;
+  Geoms d = geoms(main, nyq, n, m);
+  CK(col_pass(g, d.zm, 0, 0, 0, nullptr, c->twN, nullptr, nullptr, st));
+  CK(col_pass(g, d.zn, 1, 0, 0, nullptr, c->twN, nullptr, nullptr, st));
+  CK(col_pass(g, d.ym, 0, 0, 0, nullptr, c->twN, nullptr, nullptr, st));
+  CK(col_pass(g, d.yn, 1, 0, 0, nullptr, c->twN, nullptr, nullptr, st));
+  RowIn in = {{main, nullptr, nullptr}, {nyq, nullptr, nullptr}};
+  CK(row_pass(g, in, c->twN, c->twM, scale, 3, nullptr, nullptr, st));
+  c->launches += 5;
+  return GETHI_OK;
+}
+
+// Gaussianised spectrum P_G on the grid, once per context (pg holds N^3 floats,
+// main/nyq serve as scratch for xi).  src/fourier.c has no counterpart: the
+// reference draws the modes from P(k) itself.
+int make_pg(gethi_ctx *c)
+{
+  const DevCfg &g = c->cfg;
+  const long n = g.n;
+  const double vol = c->s.d.l_box * c->s.d.l_box * c->s.d.l_box;
+  cudaStream_t st = c->stream;
+  CK(pack_pk(g, c->main, c->nyq, (float)(1.0 / vol), st));
+  int rc = plain_c2r(c, c->main, c->nyq, 1.f);  // xi(x), compact N^3 in main
+  if (rc) return rc;
+  CK(log_xi(g, reinterpret_cast<const float *>(c->main), c->pg, c->pgn, st));
+  rc = plain_c2r(c, c->pg, c->pgn, (float)(vol / ((double)n * n * n)));  // P_G(k) on the full grid
+  if (rc) return rc;
+  c->launches += 2;
+  c->cfg.pg = reinterpret_cast<const float *>(c->pg);
+  return GETHI_OK;
+}
+
+// P_G for drawing the modes when gaussianise=1 (built on first use)
+int ensure_pg(gethi_ctx *c)
+{
+  if (!c->s.p.gaussianise || c->cfg.pg) return GETHI_OK;
+  const size_t n = c->s.p.n_grid;
+  if (!c->pg) {
+    int rc = dalloc(&c->pg, n * n * n / 2);
+    if (!rc) rc = dalloc(&c->pgn, n * n);
+    if (rc) return rc;
+  }
+  return make_pg(c);
 }
 
 // All Fourier-space work of one realisation: one Z pass drawing the modes and
@@ -399,7 +450,7 @@ extern "C" void gethi_gpu_free(gethi_ctx *c)
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  void *bufs[] = {c->main, c->nyq, c->bA, c->bAn, c->bB, c->bBn, c->bC, c->bCn, c->modes, c->vr, c->maps, c->twN, c->twM, c->partials,
+  void *bufs[] = {c->main, c->nyq, c->bA, c->bAn, c->bB, c->bBn, c->bC, c->bCn, c->modes, c->vr, c->pg, c->pgn, c->maps, c->twN, c->twM, c->partials,
                   c->stats, c->pk_f, c->logk_f, c->tab_f, c->tab_d, c->prefac, c->edges_f, c->edges_d, c->counters};
   for (void *b : bufs)
     if (b) cudaFree(b);
@@ -466,6 +517,10 @@ extern "C" int gethi_gpu_make_fields(gethi_ctx *c, const float *modes_k)
     src = c->modes;
   }
   c->nev = 0;
+  if (!src) {
+    int rc = ensure_pg(c);
+    if (rc) return rc;
+  }
   record(c);
   int rc = fields_fft(c, src);
   if (rc) return rc;
@@ -607,8 +662,10 @@ extern "C" int gethi_gpu_download_modes(gethi_ctx *c, float *modes_k)
 {
   if (!c || !modes_k) return GETHI_E_ARG;
   const long n = c->s.p.n_grid, h = n / 2 + 1;
+  int rc = ensure_pg(c);
+  if (rc) return rc;
   float2 *d = nullptr;
-  int rc = dalloc(&d, (size_t)n * n * h);
+  rc = dalloc(&d, (size_t)n * n * h);
   if (rc) return rc;
   cudaError_t e = gen_modes(c->cfg, d, FIELD_DENS, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);

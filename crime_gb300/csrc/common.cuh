@@ -278,6 +278,9 @@ struct DevCfg {
   float b_HI;
   float sigma2;    // Gaussian variance (after the density FFT)
   float mass_prefac;
+  // Gaussianised spectrum on the grid (gaussianise=1): P_G of mode (kz,ky,kx)
+  // at pg[(kz n + ky) n + kx], smoothing included; nullptr = table lookup
+  const float *pg;
 };
 
 // wave number of grid index i (src/fourier.c:264-283): Nyquist is +n/2

@@ -65,9 +65,14 @@ __device__ __forceinline__ float2 mode_from_words(const DevCfg &c, int ii, int j
   float kz = kval(ii, n, c.dk), ky = kval(jj, n, c.dk), kx = kval(kk, n, c.dk);
   float k2 = kx * kx + ky * ky + kz * kz;
   if (k2 <= 0.f) return make_float2(0.f, 0.f);
-  float lgk = 0.5f * log10f(k2);
-  float sigma2 = pk_lookup(c, lgk) * c.idk3;
-  if (c.do_smoothing) sigma2 *= expf(-c.r2_smooth * k2);
+  float sigma2;
+  if (c.pg) {
+    sigma2 = fmaxf(__ldg(&c.pg[((size_t)ii * n + jj) * n + kk]), 0.f) * c.idk3;
+  } else {
+    float lgk = 0.5f * log10f(k2);
+    sigma2 = pk_lookup(c, lgk) * c.idk3;
+    if (c.do_smoothing) sigma2 *= expf(-c.r2_smooth * k2);
+  }
   float u = (float)wph * 2.3283064365386963e-10f;
   // ln(1 - u2): log1p keeps the relative accuracy for small u2, the direct log of
   // the exact remainder 2^32 - word for u2 >= 1/2
@@ -397,6 +402,49 @@ __global__ void finish_sigma_kernel(const double2 *__restrict__ partials, int np
   }
 }
 
+// ---------------------------------------------------------------------------
+// Gaussianised spectrum on the grid (gaussianise=1):
+//   xi(x) = c2r(P~/V), xi_G = ln(1 + xi) in FP64, P_G = (V/N^3) c2r(xi_G),
+// where c2r(xi_G) is the forward DFT because xi_G is real and even.
+// ---------------------------------------------------------------------------
+// P~(|k|)/V on the split half spectrum (imaginary parts zero)
+__global__ void pack_pk_kernel(DevCfg c, float2 *main, float2 *nyq, float inv_vol)
+{
+  const int n = c.n, m = c.m;
+  const long total = (long)n * n * (m + 1);
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    const int kk = (int)(i % (m + 1));
+    const long rest = i / (m + 1);
+    const int jj = (int)(rest % n), ii = (int)(rest / n);
+    float kz = kval(ii, n, c.dk), ky = kval(jj, n, c.dk), kx = kval(kk, n, c.dk);
+    float k2 = kx * kx + ky * ky + kz * kz;
+    float p = 0.f;
+    if (k2 > 0.f) {
+      p = pk_lookup(c, 0.5f * log10f(k2));
+      if (c.do_smoothing) p *= expf(-c.r2_smooth * k2);  // src/fourier.c:294-295
+    }
+    const float2 v = make_float2(p * inv_vol, 0.f);
+    if (kk < m) main[rest * m + kk] = v;
+    else nyq[rest] = v;
+  }
+}
+
+// xi (real, compact N^3) -> half grid of ln(1 + xi) packed as a half spectrum
+__global__ void log_xi_kernel(DevCfg c, const float *__restrict__ xi, float2 *main, float2 *nyq)
+{
+  const int n = c.n, m = c.m;
+  const long total = (long)n * n * (m + 1);
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % (m + 1));
+    const long row = i / (m + 1);
+    double v = (double)xi[row * n + x];
+    v = v > -1.0 + 1e-12 ? v : -1.0 + 1e-12;
+    const float2 g = make_float2((float)log1p(v), 0.f);  // the log transform in FP64
+    if (x < m) main[row * m + x] = g;
+    else nyq[row] = g;
+  }
+}
+
 // standalone mode generator (inspection): reference layout [kz][ky][N/2+1]
 __global__ void modes_kernel(DevCfg c, float2 *out)
 {
@@ -566,6 +614,18 @@ cudaError_t row_pass(const DevCfg &c, const RowIn &in, const float2 *twN, const 
 cudaError_t finish_sigma(const double2 *partials, int np, double ncells, double *stats, cudaStream_t st)
 {
   finish_sigma_kernel<<<1, 256, 0, st>>>(partials, np, ncells, stats);
+  return cudaGetLastError();
+}
+
+cudaError_t pack_pk(const DevCfg &c, float2 *main, float2 *nyq, float inv_vol, cudaStream_t st)
+{
+  pack_pk_kernel<<<152 * 16, 256, 0, st>>>(c, main, nyq, inv_vol);
+  return cudaGetLastError();
+}
+
+cudaError_t log_xi(const DevCfg &c, const float *xi, float2 *main, float2 *nyq, cudaStream_t st)
+{
+  log_xi_kernel<<<152 * 16, 256, 0, st>>>(c, xi, main, nyq);
   return cudaGetLastError();
 }
 

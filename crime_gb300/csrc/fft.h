@@ -34,6 +34,8 @@ cudaError_t row_pass(const DevCfg &c, const RowIn &in, const float2 *twN, const 
                      float *vr, double2 *partials, cudaStream_t st);
 cudaError_t finish_sigma(const double2 *partials, int np, double ncells, double *stats, cudaStream_t st);
 cudaError_t gen_modes(const DevCfg &c, float2 *out, int kind, cudaStream_t st);
+cudaError_t pack_pk(const DevCfg &c, float2 *main, float2 *nyq, float inv_vol, cudaStream_t st);
+cudaError_t log_xi(const DevCfg &c, const float *xi, float2 *main, float2 *nyq, cudaStream_t st);
 
 // stages.cu
 cudaError_t radial_velocity_fd(const DevCfg &c, const float *vpot, float *rvel, cudaStream_t st);

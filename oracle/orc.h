@@ -88,6 +88,10 @@ void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t ou
 void orc_modes_mt(const orc_config *c, const orc_derived *d, const double *logk,
                   const double *pk, int nthreads, float *dens_k, float *vpot_k);
 /* Counter-based production modes (same amplitude law, Philox4x32-10 draws). */
+void orc_pk_grid(const orc_config *c, const orc_derived *d, const double *logk, const double *pk,
+                 double *out);
+void orc_modes_philox_pg(const orc_config *c, const orc_derived *d, const double *logk,
+                         const double *pk, const double *pg, float *dens_k);
 void orc_modes_philox(const orc_config *c, const orc_derived *d, const double *logk,
                       const double *pk, float *dens_k);
 

@@ -56,6 +56,8 @@ def lib():
             getattr(L, fn).restype = C.c_double
         L.orc_modes_mt.argtypes = [P(Config), P(Derived), f64p, f64p, C.c_int, f32p, C.c_void_p]
         L.orc_modes_philox.argtypes = [P(Config), P(Derived), f64p, f64p, f32p]
+        L.orc_modes_philox_pg.argtypes = [P(Config), P(Derived), f64p, f64p, f64p, f32p]
+        L.orc_pk_grid.argtypes = [P(Config), P(Derived), f64p, f64p, f64p]
         L.orc_c2r_inplace.argtypes = [C.c_int, f32p]
         L.orc_c2r_to_double.argtypes = [C.c_int, f32p, f64p]
         L.orc_normalize.argtypes = [C.c_int, C.c_double, f32p]
@@ -124,6 +126,27 @@ class Oracle:
     def modes_philox(self):
         dk = np.zeros(self.spec_shape(), np.complex64)
         lib().orc_modes_philox(C.byref(self.c), C.byref(self.d), self.logk, self.pk, dk.view(np.float32))
+        return dk
+
+    def pk_grid(self):
+        out = np.zeros((self.n,) * 3, np.float64)
+        lib().orc_pk_grid(C.byref(self.c), C.byref(self.d), self.logk, self.pk, out.reshape(-1))
+        return out
+
+    def gaussianised_pk(self):
+        """P_G on the grid, all in FP64: xi = sum_k P(k)/V e^{ikx}, xi_G = ln(1 + xi),
+        P_G = V/N^3 sum_x xi_G e^{-ikx} (the periodic-box form of the lognormal
+        Gaussianisation, e.g. Coles & Jones 1991; Agrawal et al. 2017, sec. 2)."""
+        n, vol = self.n, self.d.l_box ** 3
+        xi = np.fft.ifftn(self.pk_grid() / vol).real * n ** 3
+        xg = np.log1p(np.maximum(xi, -1 + 1e-12))
+        return np.ascontiguousarray(np.fft.fftn(xg).real * (vol / n ** 3))
+
+    def modes_philox_gaussianised(self, pg=None):
+        pg = self.gaussianised_pk() if pg is None else np.ascontiguousarray(pg, np.float64)
+        dk = np.zeros(self.spec_shape(), np.complex64)
+        lib().orc_modes_philox_pg(C.byref(self.c), C.byref(self.d), self.logk, self.pk, pg.reshape(-1),
+                                  dk.view(np.float32))
         return dk
 
     def c2r(self, spec):

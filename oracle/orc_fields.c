@@ -80,6 +80,34 @@ void orc_modes_mt(const orc_config *c, const orc_derived *d, const double *logk,
 void orc_modes_philox(const orc_config *c, const orc_derived *d, const double *logk,
                       const double *pk, float *dens_k)
 {
+  orc_modes_philox_pg(c, d, logk, pk, NULL, dens_k);
+}
+
+/* Smoothed P(k) of every grid mode, [kz][ky][kx] over the full n^3 grid, zero at k=0
+ * (the amplitude law of src/fourier.c:288-296 without the 1/dk^3 factor). */
+void orc_pk_grid(const orc_config *c, const orc_derived *d, const double *logk, const double *pk,
+                 double *out)
+{
+  int n = c->n_grid;
+  double dk = 2 * M_PI / d->l_box;
+  for (int ii = 0; ii < n; ii++)
+    for (int jj = 0; jj < n; jj++)
+      for (int kk = 0; kk < n; kk++) {
+        double kz = kval(ii, n, dk), ky = kval(jj, n, dk), kx = kval(kk, n, dk);
+        double k2 = kx * kx + ky * ky + kz * kz, p = 0;
+        if (k2 > 0) {
+          p = orc_pk_linear0(d, logk, pk, 0.5 * log10(k2));
+          if (d->do_smoothing) p *= exp(-d->r2_smooth * k2);
+        }
+        out[((long)ii * n + jj) * n + kk] = p;
+      }
+}
+
+/* Production modes; pg (full n^3 grid [kz][ky][kx], or NULL) replaces the smoothed
+ * table P(k) by a Gaussianised spectrum, negative values clipped to zero. */
+void orc_modes_philox_pg(const orc_config *c, const orc_derived *d, const double *logk,
+                         const double *pk, const double *pg, float *dens_k)
+{
   int n = c->n_grid, h = n / 2 + 1;
   double dk = 2 * M_PI / d->l_box;
   double idk3 = 1. / (dk * dk * dk);
@@ -94,9 +122,15 @@ void orc_modes_philox(const orc_config *c, const orc_derived *d, const double *l
         long index = kk + (long)h * (jj + (long)n * ii);
         double k_mod2 = kx * kx + ky * ky + kz * kz;
         if (k_mod2 <= 0) { dens_k[2 * index] = dens_k[2 * index + 1] = 0; continue; }
-        double lgk = 0.5 * log10(k_mod2);
-        double sigma2 = orc_pk_linear0(d, logk, pk, lgk) * idk3;
-        if (d->do_smoothing) sigma2 *= exp(-d->r2_smooth * k_mod2);
+        double sigma2;
+        if (pg) {
+          double p = pg[((long)ii * n + jj) * n + kk];
+          sigma2 = (p > 0 ? p : 0) * idk3;
+        } else {
+          double lgk = 0.5 * log10(k_mod2);
+          sigma2 = orc_pk_linear0(d, logk, pk, lgk) * idk3;
+          if (d->do_smoothing) sigma2 *= exp(-d->r2_smooth * k_mod2);
+        }
         uint64_t id = (uint64_t)kk + (uint64_t)h * ((uint64_t)jj + (uint64_t)n * ii0);
         uint32_t ctr[4] = {(uint32_t)id, (uint32_t)(id >> 32), 0, 0};
         uint32_t key[2] = {c->seed, 0x4352494Du}, o[4];

@@ -21,14 +21,16 @@ def load_case(name):
     return {k: z[k] for k in z.files}
 
 
-def oracle_for_case(case):
-    """Oracle configured like the reference run that produced a golden case."""
+def oracle_for_case(case, **over):
+    """Oracle configured like the reference run that produced a golden case
+    (keyword arguments override oracle configuration fields)."""
     from oracle import orc
     k, pk = orc.load_pk(os.path.join(GOLDEN, "pk_eh_nowiggle.txt"))
     reg = int(case["cfg_regular_nu"])
     cfg = dict(COSMO, r_smooth=float(case["cfg_r_smooth"]) if "cfg_r_smooth" in case else 2.0,
                n_grid=int(case["cfg_n_grid"]), n_side=int(case["cfg_n_side"]), seed=int(case["cfg_seed"]),
                regular_nu=reg)
+    cfg.update(over)
     if reg:
         cfg.update(nu_min=float(case["cfg_nu_min"]), nu_max=float(case["cfg_nu_max"]),
                    n_nu=int(case["cfg_n_nu"]))

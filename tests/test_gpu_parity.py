@@ -113,6 +113,24 @@ def test_philox_modes_vs_oracle(gh):
     assert np.all(np.abs(dm - om) <= 3e-5 * amp + 1e-30)
 
 
+@pytest.mark.parametrize("l_box,effect", [(None, 1e-3), (400.0, 0.1)])
+def test_gaussianised_modes_vs_oracle(gh, l_box, effect):
+    """gaussianise=1: P_G from xi_G = ln(1 + xi) on the grid (FP32 FFTs, FP64 log)
+    against the all-FP64 oracle; the modes share the Philox draws, so they
+    differ only through P_G.  The 400 Mpc/h box has xi(0) = 0.82."""
+    g = load_case("case_irr32")
+    extra = {} if l_box is None else dict(l_box=l_box)
+    ctx = gh.GetHI(params_for_case(gh, g, gaussianise=1, **extra))
+    dm = ctx.device_modes()
+    ctx.free()
+    orc = oracle_for_case(g, **({} if l_box is None else dict(l_box_override=l_box)))
+    om = orc.modes_philox_gaussianised()
+    assert np.linalg.norm(dm - om) / np.linalg.norm(om) < 1e-4
+    # P_G differs from P(k) by more than the tolerance at this variance
+    pm = orc.modes_philox()
+    assert np.linalg.norm(om - pm) / np.linalg.norm(pm) > effect
+
+
 def test_spectral_velocity_vs_oracle(gh):
     g = load_case("case_irr32")
     n = int(g["cfg_n_grid"])

@@ -139,6 +139,10 @@ def test_setup_rejects_bad_configs(gh):
         gh.host_setup(gh.make_params(n_grid=33, pk_filename="EH", frequencies_filename=""))
     with pytest.raises(gh.GetHIError):
         gh.host_setup(gh.make_params(do_psources=1, pk_filename="EH", frequencies_filename=""))
+    with pytest.raises(gh.GetHIError) as e:  # Gaussianised draws are Philox draws
+        gh.host_setup(gh.make_params(gaussianise=1, rng="mt_validation", pk_filename="EH", frequencies_filename=""))
+    assert e.value.code == -1
+    gh.host_setup(gh.make_params(gaussianise=1, n_grid=16, pk_filename="EH", frequencies_filename=""))
     with pytest.raises(gh.GetHIError) as e:
         gh.host_setup(gh.make_params(pk_filename="/nonexistent", frequencies_filename=""))
     assert e.value.code == -2
