@@ -129,6 +129,110 @@ def algorithmic_bytes(cls, n, npix, n_nu):
     }.get(cls)
 
 
+def fp64_planes(modes, zs, n, l_box, vfac, pos_obs):
+    """delta(x, y, z0) and v_r(x, y, z0) on whole z planes in FP64 from a half spectrum
+    [kz][ky][kx <= n/2]: separable sums (kz at z0, an FP64 inverse FFT over ky, the
+    c2r over kx taking Re of the kx = 0 and n/2 terms), the spectral velocity
+    v_j = c2r(i k_j delta_k f0 H0 / k^2) with derivatives of Nyquist indices set to
+    zero, and v_r = v . (x - x_obs)/|x - x_obs| at cell centres."""
+    m = n // 2
+    dk = 2 * np.pi / l_box
+    idx = np.arange(n)
+    kv = np.where(2 * idx <= n, idx, idx - n) * dk
+    kd = kv.copy()
+    kd[m] = 0.0
+    kx, kdx = kv[:m + 1], kd[:m + 1]
+    norm = (np.sqrt(2 * np.pi) / l_box) ** 3
+    cc = (idx + 0.5) * (l_box / n) - pos_obs
+    out = []
+    for z0 in zs:
+        ph = np.exp(2j * np.pi * idx * z0 / n)
+        acc = [np.zeros((n, m + 1), np.complex128) for _ in range(4)]
+        for a in range(0, n, 16):
+            blk = modes[a:a + 16].astype(np.complex128)
+            k2 = kv[a:a + 16, None, None] ** 2 + kv[None, :, None] ** 2 + kx[None, None, :] ** 2
+            with np.errstate(divide="ignore", invalid="ignore"):
+                phi = blk * np.where(k2 > 0, vfac / k2, 0.0)
+            p = ph[a:a + 16]
+            acc[0] += np.tensordot(p, blk, axes=(0, 0))
+            acc[1] += np.tensordot(p, phi, axes=(0, 0)) * (1j * kdx[None, :])
+            acc[2] += np.tensordot(p, phi, axes=(0, 0)) * (1j * kd[:, None])
+            acc[3] += np.tensordot(p * (1j * kd[a:a + 16]), phi, axes=(0, 0))
+        pl = [np.fft.irfft(np.fft.ifft(s, axis=0) * n, n=n, axis=1) * n * norm for s in acc]
+        x, y, z = cc[None, :], cc[:, None], cc[z0]
+        r = np.sqrt(x * x + y * y + z * z)
+        out.append((pl[0], (pl[1] * x + pl[2] * y + pl[3] * z) / r))
+    return out
+
+
+def fft_precision_compare(args, cfg, ctx32, stream, local, steps, ms32, ktimes32):
+    """The same workload with the tensor-core split-precision column passes: time per
+    realisation, column-pass time, and the error of delta and v_r of both paths against
+    FP64 on two z planes (same Philox seed)."""
+    import torch
+
+    import crime_gb300 as gh
+    n = cfg["n_grid"]
+    ctx = gh.GetHI(params_for(dict(cfg, fft_precision="tc_split")), device=local)
+    ctx.set_stream(stream.cuda_stream)
+    for i in range(2):
+        ctx.set_seed(cfg["seed"] + 1000 * (i + 1))
+        ctx.run_into(0)
+    torch.cuda.synchronize()
+    ctx.profile(True)
+    ctx.kernel_times()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for i in range(steps):
+        ctx.set_seed(cfg["seed"] + 7919 * i)
+        ctx.run_into(0)
+    b.record(stream)
+    torch.cuda.synchronize()
+    mstc = a.elapsed_time(b)
+    kttc, _ = ctx.kernel_times()
+    ctx.profile(False)
+
+    def col_ms(kt):
+        return sum(kt[k][0] for k in ("zpass", "ypass", "nyq") if k in kt) / steps
+
+    # errors on one seed
+    seed = cfg["seed"]
+    npix, n_nu = ctx.npix, ctx.n_nu
+    res = {}
+    maps = {}
+    for name, c in (("fp32", ctx32), ("tc_split", ctx)):
+        c.set_seed(seed)
+        maps[name] = c.run()
+        c.create_d_and_vr_fields()
+        res[name] = c.grids()
+    modes = ctx32.device_modes()
+    d = ctx32.derived()
+    zs = (0, 517 % n)
+    planes = fp64_planes(modes, zs, n, d.l_box, d.fgrowth_0 * d.hubble_0, d.pos_obs)
+    del modes
+
+    def rel(x, y):
+        x = np.asarray(x, np.float64)
+        y = np.asarray(y, np.float64)
+        return float(np.linalg.norm(x - y) / np.linalg.norm(y))
+
+    out = {"fft": "column passes (Z, Y) of the 1024-point c2r; the X (row) passes are FP32 in both",
+           "error_vs_fp64": "relative L2 on the z planes %s against an FP64 separable evaluation of the same "
+                            "modes" % (list(zs),)}
+    for name, ms_, kt in (("fp32", ms32, ktimes32), ("tc_split", mstc, kttc)):
+        dd, vv = res[name]
+        out[name] = {"ms_per_step": round(ms_ / steps, 3), "voxels_per_s": float(n) ** 3 * steps / (ms_ / 1e3),
+                     "column_pass_ms_per_step": round(col_ms(kt), 3),
+                     "delta_rel_l2_vs_fp64": max(rel(dd[z], p[0]) for z, p in zip(zs, planes)),
+                     "v_r_rel_l2_vs_fp64": max(rel(vv[z], p[1]) for z, p in zip(zs, planes))}
+    out["maps_rel_l2_tc_vs_fp32"] = rel(maps["tc_split"], maps["fp32"])
+    out["speedup_tc_over_fp32"] = round(out["fp32"]["ms_per_step"] / out["tc_split"]["ms_per_step"], 3)
+    out["column_pass_speedup_tc_over_fp32"] = round(out["fp32"]["column_pass_ms_per_step"] /
+                                                    out["tc_split"]["column_pass_ms_per_step"], 3)
+    ctx.free()
+    return out
+
+
 def bench_ours(args):
     import torch
 
@@ -249,6 +353,8 @@ def bench_ours(args):
         "wall_s": wall,
         "filled_fraction": ctx.derived().filled_fraction,
     }
+    if ws == 1 and n == 1024 and not args.no_fft_compare:
+        line["fft_precision_compare"] = fft_precision_compare(args, cfg, ctx, stream, local, args.steps, ms, ktimes)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args)
     if rank == 0:
@@ -341,6 +447,8 @@ def main():
     ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
     ap.add_argument("--cpu-sample", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fft-compare", action="store_true",
+                    help="skip the tensor-core split-precision FFT comparison (1024^3 workloads)")
     args = ap.parse_args()
     if args.impl == "reference":
         bench_reference(args)

@@ -55,6 +55,9 @@ struct gethi_ctx {
   void *fq = nullptr;       // queue of samples whose FP32 key is uncertain
   long fq_cap = 0;
   float2 *pg = nullptr, *pgn = nullptr;  // Gaussianised spectrum (gaussianise=1)
+  uint4 *tc_bmat = nullptr;                // fft_precision=tc_split tables and error flag
+  float2 *tc_tw = nullptr;
+  int *tc_err = nullptr;
 };
 
 namespace {
@@ -149,6 +152,9 @@ void fill_cfg(gethi_ctx *c)
   g.b_HI = (float)s.p.b_HI;
   g.do_rsd = s.p.do_rsd;
   g.mass_prefac = (float)(g.dx * g.dx * g.dx);  // src/grid_tools.c:122
+  g.tc_bmat = c->tc_bmat;
+  g.tc_tw = c->tc_tw;
+  g.tc_err = c->tc_err;
 }
 
 ColGeom geom(float2 *base, long cpp, long pstride, long cstride, long estride, long ncols)
@@ -213,7 +219,8 @@ Geoms geoms(float2 *main, float2 *nyq, long n, long m)
 
 int plain_c2r(gethi_ctx *c, float2 *main, float2 *nyq, float scale)
 {
-  const DevCfg &g = c->cfg;
+  DevCfg g = c->cfg;
+  g.tc_bmat = nullptr;  // FP32 passes: P_G spans many decades and is shared by both FFT precisions
   const long n = g.n, m = g.m;
   cudaStream_t st = c->stream;
   Geoms d = geoms(main, nyq, n, m);
@@ -394,6 +401,23 @@ extern "C" int gethi_gpu_init(const gethi_params *p, int device, gethi_ctx **out
     gethi_gpu_free(c);
     return rc;
   }
+  if (s.p.fft_precision == 1) {
+    std::vector<uint16_t> bm;
+    std::vector<float2> tw;
+    if (!tc_tables((int)n, bm, tw)) {
+      set_error("fft_precision=tc_split needs n_grid=1024");
+      gethi_gpu_free(c);
+      return GETHI_E_ARG;
+    }
+    if ((rc = dalloc(&c->tc_bmat, tc_table_bytes() / sizeof(uint4))) || (rc = dalloc(&c->tc_tw, tw.size())) ||
+        (rc = dalloc(&c->tc_err, 1))) {
+      gethi_gpu_free(c);
+      return rc;
+    }
+    cudaMemcpy(c->tc_bmat, bm.data(), tc_table_bytes(), cudaMemcpyHostToDevice);
+    cudaMemcpy(c->tc_tw, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice);
+    cudaMemset(c->tc_err, 0, sizeof(int));
+  }
   // tables
   std::vector<float2> t;
   twiddles(t, (int)n);
@@ -450,7 +474,8 @@ extern "C" void gethi_gpu_free(gethi_ctx *c)
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  void *bufs[] = {c->main, c->nyq, c->bA, c->bAn, c->bB, c->bBn, c->bC, c->bCn, c->modes, c->vr, c->pg, c->pgn, c->maps, c->twN, c->twM, c->partials,
+  void *bufs[] = {c->main, c->nyq, c->bA, c->bAn, c->bB, c->bBn, c->bC, c->bCn, c->modes, c->vr, c->pg, c->pgn,
+                  c->tc_bmat, c->tc_tw, c->tc_err, c->maps, c->twN, c->twM, c->partials,
                   c->stats, c->pk_f, c->logk_f, c->tab_f, c->tab_d, c->prefac, c->edges_f, c->edges_d, c->counters};
   for (void *b : bufs)
     if (b) cudaFree(b);
@@ -545,6 +570,19 @@ extern "C" int gethi_gpu_get_hi(gethi_ctx *c)
   return GETHI_OK;
 }
 
+// the tensor-core passes record an expired wait in tc_err (after a synchronize)
+static int check_tc(const gethi_ctx *c)
+{
+  if (!c->tc_err) return GETHI_OK;
+  int flag = 0;
+  CK(cudaMemcpy(&flag, c->tc_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (flag) {
+    set_error("tensor-core FFT: an MMA completion wait expired");
+    return GETHI_E_CUDA;
+  }
+  return GETHI_OK;
+}
+
 static int maps_common(gethi_ctx *c, float *maps_out, int fused)
 {
   const Setup &s = c->s;
@@ -576,6 +614,8 @@ static int maps_common(gethi_ctx *c, float *maps_out, int fused)
     record(c);
   }
   CK(cudaStreamSynchronize(c->stream));
+  int rc = check_tc(c);
+  if (rc) return rc;
   for (int i = 0; i + 1 < c->nev && i < 7; i++) cudaEventElapsedTime(&c->times[i], c->ev[i], c->ev[i + 1]);
   collect_kernel_times(c);
   return GETHI_OK;
@@ -626,6 +666,8 @@ extern "C" int gethi_gpu_download_grids(const gethi_ctx *c, float *dens, float *
   if (!c) return GETHI_E_ARG;
   const long n = c->s.p.n_grid;
   CK(cudaStreamSynchronize(c->stream));
+  int rc = check_tc(c);
+  if (rc) return rc;
   if (dens) CK(cudaMemcpy(dens, c->main, sizeof(float) * n * n * n, cudaMemcpyDeviceToHost));
   if (rvel) CK(cudaMemcpy(rvel, c->vr, sizeof(float) * n * n * n, cudaMemcpyDeviceToHost));
   return GETHI_OK;

@@ -281,6 +281,11 @@ struct DevCfg {
   // Gaussianised spectrum on the grid (gaussianise=1): P_G of mode (kz,ky,kx)
   // at pg[(kz n + ky) n + kx], smoothing included; nullptr = table lookup
   const float *pg;
+  // tensor-core split-precision column passes (fft_precision=tc_split): DFT
+  // operand tables, twiddles, error flag; tc_bmat == nullptr selects FP32
+  const uint4 *tc_bmat;
+  const float2 *tc_tw;
+  int *tc_err;
 };
 
 // wave number of grid index i (src/fourier.c:264-283): Nyquist is +n/2

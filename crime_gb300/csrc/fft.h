@@ -2,6 +2,9 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cstdint>
+#include <vector>
+
 #include "common.cuh"
 
 namespace gethi {
@@ -36,6 +39,13 @@ cudaError_t finish_sigma(const double2 *partials, int np, double ncells, double 
 cudaError_t gen_modes(const DevCfg &c, float2 *out, int kind, cudaStream_t st);
 cudaError_t pack_pk(const DevCfg &c, float2 *main, float2 *nyq, float inv_vol, cudaStream_t st);
 cudaError_t log_xi(const DevCfg &c, const float *xi, float2 *main, float2 *nyq, cudaStream_t st);
+
+// tcfft.cu: split-precision tensor-core column passes (n = 1024, main block)
+bool tc_col_supported(const DevCfg &c, const ColGeom &g, int nyq);
+cudaError_t tc_col_pass(const DevCfg &c, const ColGeom &g, int mode, int nout, const float2 *src, float2 *out1,
+                        float2 *out2, cudaStream_t st);
+bool tc_tables(int n, std::vector<uint16_t> &bmat, std::vector<float2> &tw);
+size_t tc_table_bytes();
 
 // stages.cu
 cudaError_t radial_velocity_fd(const DevCfg &c, const float *vpot, float *rvel, cudaStream_t st);

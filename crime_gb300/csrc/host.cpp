@@ -397,6 +397,10 @@ int setup_build(const gethi_params &p, Setup &s, std::string &err)
   if (p.n_grid < 4 || (p.n_grid & 1)) { err = "n_grid must be even and >= 4"; return GETHI_E_ARG; }
   if (p.n_side < 1 || p.n_side > 8192) { err = "n_side out of range"; return GETHI_E_ARG; }
   if (p.do_psources) { err = "do_psources=1: point sources are not part of this path"; return GETHI_E_ARG; }
+  if (p.fft_precision == 1 && p.n_grid != 1024) {
+    err = "fft_precision=tc_split: the tensor-core column transform is built for n_grid=1024";
+    return GETHI_E_ARG;
+  }
   if (p.gaussianise && p.rng != 0) {
     err = "gaussianise=1 draws its modes with rng=philox (the validation draws follow P(k) as the reference does)";
     return GETHI_E_ARG;

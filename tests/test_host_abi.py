@@ -143,6 +143,10 @@ def test_setup_rejects_bad_configs(gh):
         gh.host_setup(gh.make_params(gaussianise=1, rng="mt_validation", pk_filename="EH", frequencies_filename=""))
     assert e.value.code == -1
     gh.host_setup(gh.make_params(gaussianise=1, n_grid=16, pk_filename="EH", frequencies_filename=""))
+    with pytest.raises(gh.GetHIError) as e:  # the tensor-core column transform is 1024-point
+        gh.host_setup(gh.make_params(fft_precision="tc_split", n_grid=512, pk_filename="EH", frequencies_filename=""))
+    assert e.value.code == -1
+    gh.host_setup(gh.make_params(fft_precision="tc_split", n_grid=1024, pk_filename="EH", frequencies_filename=""))
     with pytest.raises(gh.GetHIError) as e:
         gh.host_setup(gh.make_params(pk_filename="/nonexistent", frequencies_filename=""))
     assert e.value.code == -2
