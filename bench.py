@@ -39,6 +39,9 @@ CONFIGS = {
                velocity_mode="spectral", gaussianise=1),
 }
 COSMO = dict(omega_M=0.315, omega_L=0.685, omega_B=0.049, h=0.67, w=-1.0, ns=0.96, sigma_8=0.83)
+# ensemble: (n_grid, box, realisations, lanes = concurrent contexts of that size); seeds 4000.. in order
+ENSEMBLE = dict(members=[(128, 1000.0, 32, 4), (256, 2000.0, 24, 3), (384, 3000.0, 8, 2)], seed=4000, zmin=0.5,
+                zmax=1.5, n_nu=64, n_side=128, do_rsd=1, velocity_mode="spectral", gaussianise=1)
 
 
 def params_for(cfg, seed_offset=0):
@@ -231,6 +234,91 @@ def fft_precision_compare(args, cfg, ctx32, stream, local, steps, ms32, ktimes32
                                                     out["tc_split"]["column_pass_ms_per_step"], 3)
     ctx.free()
     return out
+
+
+def bench_ensemble(args):
+    """The batched ensemble: every member's realisations in one CUDA-graph launch per
+    step (run_batch), contexts of one size run as concurrent lanes, launch shapes
+    from the autotuner.  value = voxels/s of the device-resident batch; e2e = the
+    same through run_batch with the maps copied to host memory and the graph
+    captured and instantiated inside the timed region."""
+    import torch
+
+    import crime_gb300 as gh
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    E = ENSEMBLE
+    ctxs, jobs, tuned, filled = [], [], {}, {}
+    seed = E["seed"] + 1000 * rank
+    for n, box, count, lanes in E["members"]:
+        first = len(ctxs)
+        for ln in range(lanes):
+            cfg = dict(n_grid=n, l_box=box, zmin=E["zmin"], zmax=E["zmax"], n_nu=E["n_nu"], n_side=E["n_side"],
+                       seed=seed, do_rsd=E["do_rsd"], velocity_mode=E["velocity_mode"], gaussianise=E["gaussianise"])
+            c = gh.GetHI(params_for(cfg), device=local)
+            t = c.autotune()
+            tuned.setdefault(n, []).append(t)
+            ctxs.append(c)
+        filled[n] = ctxs[first].derived().filled_fraction
+        for i in range(count):
+            jobs.append((first + i % lanes, seed))
+            seed += 1
+    voxels = float(sum(float(n) ** 3 * count for n, _, count, _ in E["members"]))
+    for _ in range(args.warmup):
+        gh.run_batch(ctxs, jobs, download=False, graph=True)
+    torch.cuda.synchronize()
+    dev_ms, stats = [], None
+    clk = ClockSampler(local)
+    with clk:
+        for _ in range(args.steps):
+            _, stats = gh.run_batch(ctxs, jobs, download=False, graph=True)
+            dev_ms.append(stats["device_ms"])
+    ms = sum(dev_ms)
+    # end to end: capture + instantiate + run + maps to the host, wall clock
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        maps, st_e2e = gh.run_batch(ctxs, jobs, download=True, graph=True)
+    e2e_s = time.perf_counter() - t0
+    assert all(np.isfinite(m).all() for m in maps)
+    d2h = int(sum(4 * m.size for m in maps))
+    # the same batch without the graph, and one realisation at a time through gethi_gpu_run
+    _, st_ng = gh.run_batch(ctxs, jobs, download=False, graph=False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k, s in jobs:
+        ctxs[k].set_seed(s)
+        ctxs[k].run_into(0)
+    torch.cuda.synchronize()
+    seq_s = time.perf_counter() - t0
+    line = {
+        "metric": "GetHI batched ensemble throughput (voxels/s): %s" % " + ".join(
+            "%dx%d^3" % (cnt, n) for n, _, cnt, _ in E["members"]),
+        "value": voxels * args.steps / (ms / 1e3), "unit": "voxels/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic (Philox modes from an EH no-wiggle P(k))",
+        "realisations_per_s": len(jobs) * args.steps / (ms / 1e3),
+        "config": {"workload": "c3: " + ", ".join("%d x %d^3 (box %g Mpc/h, %d lanes)" % (cnt, n, box, ln)
+                                                  for n, box, cnt, ln in E["members"]) +
+                   "; seeds %d-%d; Nside %d x %d shells, z %.1f-%.1f; spectral RSD; Gaussianised P(k)" % (
+                       E["seed"], E["seed"] + len(jobs) - 1, E["n_side"], E["n_nu"], E["zmin"], E["zmax"]),
+                   "graph_nodes": stats["graph_nodes"], "kernel_launches_per_step": stats["kernel_launches"],
+                   "autotuned": {str(n): v[0] for n, v in tuned.items()},
+                   "filled_fraction": {str(n): f for n, f in filled.items()},
+                   "l2": "the batch's working set (%.1f GB of fields) exceeds L2" % (
+                       sum(6 * 4 * float(n) ** 3 * ln for n, _, _, ln in E["members"]) / 1e9)},
+        "e2e": {"value": voxels * args.steps / e2e_s, "unit": "voxels/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": d2h, "includes": "graph capture + instantiate (%.1f ms) + run + maps to "
+                                                      "host" % st_e2e["capture_ms"]},
+        "gpu_launches": stats["kernel_launches"] * args.steps,
+        "compare": {"batch_no_graph_ms": round(st_ng["device_ms"], 3),
+                    "one_at_a_time_ms": round(1e3 * seq_s, 3),
+                    "graph_ms": round(ms / args.steps, 3)},
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    for c in ctxs:
+        c.free()
 
 
 def bench_ours(args):
@@ -444,7 +532,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS) + ["c3"])
     ap.add_argument("--cpu-sample", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fft-compare", action="store_true",
@@ -452,6 +540,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         bench_reference(args)
+    elif args.config == "c3":
+        bench_ensemble(args)
     else:
         bench_ours(args)
 

@@ -12,6 +12,7 @@
 //   plus FP64/FP32 tables, twiddles, per-block partial sums.
 #include <cmath>
 #include <cstdio>
+#include <chrono>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -570,6 +571,17 @@ extern "C" int gethi_gpu_get_hi(gethi_ctx *c)
   return GETHI_OK;
 }
 
+// queue of the samples whose FP32 key needs the FP64 decision (first projection)
+static int ensure_fq(gethi_ctx *c)
+{
+  if (c->fq) return GETHI_OK;
+  const long cap = fallback_queue_capacity((int)c->s.p.n_grid);
+  int rc = dalloc(reinterpret_cast<char **>(&c->fq), (size_t)cap * fallback_entry_bytes());
+  if (rc) return rc;
+  c->fq_cap = cap;
+  return GETHI_OK;
+}
+
 // the tensor-core passes record an expired wait in tc_err (after a synchronize)
 static int check_tc(const gethi_ctx *c)
 {
@@ -589,12 +601,8 @@ static int maps_common(gethi_ctx *c, float *maps_out, int fused)
   const long npix = 12 * s.p.n_side * s.p.n_side;
   CK(cudaMemsetAsync(c->maps, 0, sizeof(float) * npix * s.p.n_nu, c->stream));
   CK(cudaMemsetAsync(c->counters, 0, sizeof(int) * 16, c->stream));
-  if (!c->fq) {
-    long cap = fallback_queue_capacity((int)s.p.n_grid);
-    int rc = dalloc(reinterpret_cast<char **>(&c->fq), (size_t)cap * fallback_entry_bytes());
-    if (rc) return rc;
-    c->fq_cap = cap;
-  }
+  int rq = ensure_fq(c);
+  if (rq) return rq;
   {
     KTimer t(c, KC_PROJECT);
     CK(project(c->cfg, c->stats, reinterpret_cast<const float *>(c->main), c->vr, fused, c->maps, c->counters,
@@ -643,6 +651,220 @@ extern "C" int gethi_gpu_run(gethi_ctx *c, float *maps_out)
   c->stage = 3;  // mass is not materialised by the fused path
   if (c->s.p.write_maps && maps_out) return gethi_gpu_write_maps(c, maps_out);
   return GETHI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batches of realisations: enqueue-only realisations (no host synchronisation,
+// no allocation), captured into one CUDA graph
+// ---------------------------------------------------------------------------
+
+// every lazily allocated buffer and the per-configuration set-up, so that a
+// realisation only enqueues work
+static int prepare(gethi_ctx *c)
+{
+  CK(cudaSetDevice(c->device));
+  int rc = ensure_fq(c);
+  if (!rc) rc = ensure_pg(c);
+  if (!rc) CK(cudaStreamSynchronize(c->stream));
+  return rc;
+}
+
+// one Philox realisation on stream st (fields, fused get_HI + projection, FP64
+// key fix-up, channel scaling) and, maps_out != NULL, the maps copied to
+// maps_out (device or page-locked host memory)
+static int enqueue_realisation(gethi_ctx *c, unsigned int seed, float *maps_out, cudaStream_t st)
+{
+  const Setup &s = c->s;
+  const size_t bytes = sizeof(float) * 12 * (size_t)s.p.n_side * s.p.n_side * s.p.n_nu;
+  const cudaStream_t s0 = c->stream;
+  const int prof = c->prof;
+  const unsigned int seed0 = c->cfg.seed;
+  c->stream = st;
+  c->prof = 0;
+  c->cfg.seed = seed;
+  int rc = fields_fft(c, nullptr);
+  auto step = [&](cudaError_t e, const char *what) {
+    if (!rc && e != cudaSuccess) rc = cuda_fail(e, what);
+  };
+  step(cudaMemsetAsync(c->maps, 0, bytes, st), "memset maps");
+  step(cudaMemsetAsync(c->counters, 0, sizeof(int) * 16, st), "memset counters");
+  if (!rc)
+    step(project(c->cfg, c->stats, reinterpret_cast<const float *>(c->main), c->vr, 1, c->maps, c->counters, c->fq,
+                 c->fq_cap, st),
+         "project");
+  if (!rc) step(fixup(c->cfg, c->fq, c->counters, c->fq_cap, c->maps, st), "fixup");
+  if (!rc) step(scale_maps(c->cfg, c->maps, st), "scale_maps");
+  if (!rc && maps_out) step(cudaMemcpyAsync(maps_out, c->maps, bytes, cudaMemcpyDefault, st), "maps copy");
+  c->launches += 3;
+  c->stream = s0;
+  c->prof = prof;
+  c->cfg.seed = seed0;
+  return rc;
+}
+
+extern "C" int gethi_gpu_run_batch(gethi_ctx *const *ctxs, int nctx, const int *job_ctx, const unsigned int *seeds,
+                                   int njobs, float *const *maps_out, int use_graph, double *stats)
+{
+  if (!ctxs || nctx < 1 || !job_ctx || !seeds || njobs < 0) return GETHI_E_ARG;
+  for (int k = 0; k < nctx; k++)
+    if (!ctxs[k] || ctxs[k]->device != ctxs[0]->device || ctxs[k]->s.p.rng != 0) {
+      set_error("run_batch: contexts must be valid, on one device, with rng=philox");
+      return GETHI_E_ARG;
+    }
+  for (int i = 0; i < njobs; i++)
+    if (job_ctx[i] < 0 || job_ctx[i] >= nctx) {
+      set_error("run_batch: job_ctx out of range");
+      return GETHI_E_ARG;
+    }
+  CK(cudaSetDevice(ctxs[0]->device));
+  for (int k = 0; k < nctx; k++) {
+    int rc = prepare(ctxs[k]);
+    if (rc) return rc;
+  }
+  // page-lock pageable host outputs for the duration of the call
+  std::vector<void *> registered;
+  if (maps_out)
+    for (int i = 0; i < njobs; i++) {
+      if (!maps_out[i]) continue;
+      cudaPointerAttributes at;
+      if (cudaPointerGetAttributes(&at, maps_out[i]) == cudaSuccess && at.type != cudaMemoryTypeUnregistered) continue;
+      cudaGetLastError();
+      const Setup &s = ctxs[job_ctx[i]]->s;
+      const size_t bytes = sizeof(float) * 12 * (size_t)s.p.n_side * s.p.n_side * s.p.n_nu;
+      if (cudaHostRegister(maps_out[i], bytes, cudaHostRegisterDefault) == cudaSuccess)
+        registered.push_back(maps_out[i]);
+      else
+        cudaGetLastError();  // already page-locked
+    }
+  auto unregister = [&]() {
+    for (void *p : registered) cudaHostUnregister(p);
+  };
+  long launches0 = 0;
+  for (int k = 0; k < nctx; k++) launches0 += ctxs[k]->launches;
+
+  cudaStream_t origin = nullptr;
+  cudaEvent_t fork = nullptr, t0 = nullptr, t1 = nullptr;
+  std::vector<cudaEvent_t> joins(nctx, nullptr);
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int rc = GETHI_OK;
+  auto cu = [&](cudaError_t e, const char *what) {
+    if (!rc && e != cudaSuccess) rc = cuda_fail(e, what);
+  };
+  cu(cudaStreamCreateWithFlags(&origin, cudaStreamNonBlocking), "stream");
+  cu(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "event");
+  cu(cudaEventCreate(&t0), "event");
+  cu(cudaEventCreate(&t1), "event");
+  for (int k = 0; k < nctx; k++) cu(cudaEventCreateWithFlags(&joins[k], cudaEventDisableTiming), "event");
+  const auto c0 = std::chrono::steady_clock::now();
+  double capture_ms = 0, nodes = 0;
+  if (!rc) {
+    if (use_graph) cu(cudaStreamBeginCapture(origin, cudaStreamCaptureModeThreadLocal), "begin capture");
+    else cu(cudaEventRecord(t0, origin), "event");
+    cu(cudaEventRecord(fork, origin), "fork");
+    for (int k = 0; k < nctx; k++) cu(cudaStreamWaitEvent(ctxs[k]->stream, fork, 0), "fork wait");
+    for (int i = 0; i < njobs && !rc; i++) {
+      gethi_ctx *c = ctxs[job_ctx[i]];
+      rc = enqueue_realisation(c, seeds[i], maps_out ? maps_out[i] : nullptr, c->stream);
+    }
+    for (int k = 0; k < nctx; k++) {
+      cu(cudaEventRecord(joins[k], ctxs[k]->stream), "join");
+      cu(cudaStreamWaitEvent(origin, joins[k], 0), "join wait");
+    }
+    if (use_graph) {
+      cudaError_t e = cudaStreamEndCapture(origin, &graph);
+      if (!rc && e != cudaSuccess) rc = cuda_fail(e, "end capture");
+      if (!rc) cu(cudaGraphInstantiate(&exec, graph, 0), "instantiate");
+      size_t nn = 0;
+      if (!rc && cudaGraphGetNodes(graph, nullptr, &nn) == cudaSuccess) nodes = (double)nn;
+      capture_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - c0).count();
+      cu(cudaEventRecord(t0, origin), "event");
+      if (!rc) cu(cudaGraphLaunch(exec, origin), "graph launch");
+    }
+    cu(cudaEventRecord(t1, origin), "event");
+    cu(cudaStreamSynchronize(origin), "synchronize");
+  }
+  float run_ms = 0;
+  if (!rc) cudaEventElapsedTime(&run_ms, t0, t1);
+  for (int k = 0; k < nctx && !rc; k++) rc = check_tc(ctxs[k]);
+  long launches1 = 0;
+  for (int k = 0; k < nctx; k++) launches1 += ctxs[k]->launches;
+  if (stats) {
+    stats[0] = capture_ms;
+    stats[1] = run_ms;
+    stats[2] = nodes;
+    stats[3] = (double)(launches1 - launches0);
+  }
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  for (cudaEvent_t e : joins)
+    if (e) cudaEventDestroy(e);
+  if (fork) cudaEventDestroy(fork);
+  if (t0) cudaEventDestroy(t0);
+  if (t1) cudaEventDestroy(t1);
+  if (origin) cudaStreamDestroy(origin);
+  unregister();
+  for (int k = 0; k < nctx; k++) ctxs[k]->stage = 3;
+  return rc;
+}
+
+// Launch-shape autotuner: times each candidate (projection tile depth, column
+// tile width) on this context's own workload and keeps the fastest.
+extern "C" int gethi_gpu_autotune(gethi_ctx *c, int *choice, float *ms_out)
+{
+  if (!c) return GETHI_E_ARG;
+  if (c->s.p.rng != 0) {
+    set_error("autotune: needs rng=philox");
+    return GETHI_E_ARG;
+  }
+  int rc = prepare(c);
+  if (rc) return rc;
+  const int n = c->s.p.n_grid;
+  std::vector<std::pair<int, int>> cand;
+  for (int zs : {4, 2, 1})
+    if (n % (4 * zs) == 0 && n % 8 == 0)
+      for (int cv : {0, 1})
+        if (cv == 0 || n == 128 || n == 256 || n == 384) cand.push_back({zs, cv});
+  if (cand.empty()) return GETHI_OK;
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  const int zs0 = c->cfg.proj_zsteps, cv0 = c->cfg.col_variant;
+  float best = 1e30f;
+  std::pair<int, int> pick = cand[0];
+  const int reps = n >= 768 ? 1 : 3;
+  for (auto &cd : cand) {
+    c->cfg.proj_zsteps = cd.first;
+    c->cfg.col_variant = cd.second;
+    rc = enqueue_realisation(c, c->cfg.seed, nullptr, c->stream);  // warm-up
+    if (!rc) CK(cudaEventRecord(a, c->stream));
+    for (int r = 0; r < reps && !rc; r++) rc = enqueue_realisation(c, c->cfg.seed + 1 + r, nullptr, c->stream);
+    if (!rc) CK(cudaEventRecord(b, c->stream));
+    if (!rc) CK(cudaEventSynchronize(b));
+    if (rc) break;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    ms /= reps;
+    if (ms < best) {
+      best = ms;
+      pick = cd;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc) {
+    c->cfg.proj_zsteps = zs0;
+    c->cfg.col_variant = cv0;
+    return rc;
+  }
+  c->cfg.proj_zsteps = pick.first;
+  c->cfg.col_variant = pick.second;
+  if (choice) {
+    choice[0] = pick.first;
+    choice[1] = pick.second;
+  }
+  if (ms_out) *ms_out = best;
+  return check_tc(c);
 }
 
 extern "C" int gethi_gpu_write_maps(const gethi_ctx *c, const float *maps)

@@ -286,6 +286,10 @@ struct DevCfg {
   const uint4 *tc_bmat;
   const float2 *tc_tw;
   int *tc_err;
+  // launch shapes chosen by the autotuner (0 = built-in choice): cells per
+  // projection tile along z / 4, and the half-width column tile of the FP32 passes
+  int proj_zsteps;
+  int col_variant;
 };
 
 // wave number of grid index i (src/fourier.c:264-283): Nyquist is +n/2

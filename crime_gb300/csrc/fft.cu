@@ -400,6 +400,12 @@ template <> struct ColPlan<64> { static constexpr int P = 8, TX = 16; using R = 
 template <> struct ColPlan<32> { static constexpr int P = 8, TX = 16; using R = Radices<8, 4>; };
 template <> struct ColPlan<24> { static constexpr int P = 12, TX = 16; using R = Radices<12, 2>; };
 template <> struct ColPlan<16> { static constexpr int P = 4, TX = 16; using R = Radices<4, 4>; };
+// half-width column tiles (a second launch shape for the autotuner) at the ensemble sizes
+template <int L> struct ColPlanNarrow;
+template <> struct ColPlanNarrow<384> { static constexpr int P = 24, TX = 8; using R = Radices<8, 8, 6>; };
+template <> struct ColPlanNarrow<256> { static constexpr int P = 16, TX = 8; using R = Radices<16, 16>; };
+template <> struct ColPlanNarrow<128> { static constexpr int P = 16, TX = 8; using R = Radices<16, 8>; };
+template <int L> constexpr bool has_narrow() { return L == 128 || L == 256 || L == 384; }
 // columns of the drawing Z pass (modes kept in registers for up to three transforms)
 template <int L> struct ColPlanGen : ColPlan<L> {};
 template <> struct ColPlanGen<2048> { static constexpr int P = 16, TX = 2; using R = Radices<16, 16, 8>; };
@@ -428,11 +434,10 @@ template <> struct RowPlanV<16> { static constexpr int P = 4, RW = 32; using R =
 template <> struct RowPlanV<12> { static constexpr int P = 12, RW = 32; using R = Radices<12>; };
 template <> struct RowPlanV<8> { static constexpr int P = 8, RW = 32; using R = Radices<8>; };
 
-template <int L, int MODE>
-static cudaError_t launch_col(const DevCfg &c, const ColGeom &g, int nyq, int nout, const float2 *src,
-                              const float2 *tw, float2 *out1, float2 *out2, cudaStream_t st)
+template <int L, int MODE, class PL>
+static cudaError_t launch_col_plan(const DevCfg &c, const ColGeom &g, int nyq, int nout, const float2 *src,
+                                   const float2 *tw, float2 *out1, float2 *out2, cudaStream_t st)
 {
-  using PL = typename std::conditional<MODE == 1, ColPlanGen<L>, ColPlan<L>>::type;
   constexpr int threads = PL::TX * (L / PL::P);
   const size_t sm = sizeof(float2) * PL::TX * L;
   auto kern = col_pass_kernel<L, PL::P, PL::TX, typename PL::R, MODE>;
@@ -444,6 +449,17 @@ static cudaError_t launch_col(const DevCfg &c, const ColGeom &g, int nyq, int no
   long blocks = (g.ncols + PL::TX - 1) / PL::TX;
   kern<<<(unsigned)blocks, threads, sm, st>>>(c, g, nyq, nout, src, tw, out1, out2);
   return cudaGetLastError();
+}
+
+template <int L, int MODE>
+static cudaError_t launch_col(const DevCfg &c, const ColGeom &g, int nyq, int nout, const float2 *src,
+                              const float2 *tw, float2 *out1, float2 *out2, cudaStream_t st)
+{
+  if constexpr (has_narrow<L>()) {
+    if (c.col_variant == 1) return launch_col_plan<L, MODE, ColPlanNarrow<L>>(c, g, nyq, nout, src, tw, out1, out2, st);
+  }
+  using PL = typename std::conditional<MODE == 1, ColPlanGen<L>, ColPlan<L>>::type;
+  return launch_col_plan<L, MODE, PL>(c, g, nyq, nout, src, tw, out1, out2, st);
 }
 
 template <int M, int EPI, class PL>

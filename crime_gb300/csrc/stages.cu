@@ -310,7 +310,12 @@ __device__ __forceinline__ uint32_t key_fast(const DevCfg &c, const FastConst &f
 // ---------------------------------------------------------------------------
 constexpr int kProjThreads = 256;
 constexpr int kTile = 8;  // tiles are 8 x 8 x (4 zsteps) cells: 256 threads cover 8 x 8 x 4 cells per step
-__host__ __device__ inline int tile_zsteps(int n) { return n % 16 == 0 ? 4 : 2; }
+// projection tile = 8 x 8 x (4 zsteps) cells; zsteps from the autotuner when it divides the grid
+__host__ __device__ inline int tile_zsteps(const DevCfg &c)
+{
+  if (c.proj_zsteps >= 1 && c.proj_zsteps <= 4 && c.n % (4 * c.proj_zsteps) == 0) return c.proj_zsteps;
+  return c.n % 16 == 0 ? 4 : 2;
+}
 constexpr int kQueueCap = 1024;
 constexpr int kHash = 4096;
 constexpr int kProbe = 16;
@@ -367,7 +372,7 @@ __global__ void __launch_bounds__(kProjThreads) project_kernel(DevCfg c, FastCon
   const float *ef = smem_edges ? sef : c.nu_edges_f;
   int log2nn = 0;
   while ((1 << (log2nn + 1)) - 2 < c.n_nu) log2nn++;  // steps 2^L..1 from -1 reach index n_nu
-  const int n = c.n, nt = n / kTile, zsteps = tile_zsteps(n);
+  const int n = c.n, nt = n / kTile, zsteps = tile_zsteps(c);
   const int bx = blockIdx.x % nt, by = (blockIdx.x / nt) % nt, bz = blockIdx.x / (nt * nt);
   const float sigma2 = FUSED ? (float)stats[1] : 0.f;
   int nfall = 0;
@@ -462,7 +467,7 @@ __global__ void fixup_kernel(DevCfg c, const FallbackEntry *__restrict__ fq, con
                              long fq_cap, float *__restrict__ maps)
 {
   const long cnt = min((long)*reinterpret_cast<const unsigned long long *>(&counters[2]), fq_cap);
-  const int nt = c.n / kTile, zsteps = tile_zsteps(c.n);
+  const int nt = c.n / kTile, zsteps = tile_zsteps(c);
   for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < cnt; j += (long)gridDim.x * blockDim.x) {
     const FallbackEntry e = fq[j];
     const int bx = e.tile % nt, by = (e.tile / nt) % nt, bz = e.tile / (nt * nt);
@@ -555,7 +560,7 @@ size_t fallback_entry_bytes() { return sizeof(FallbackEntry); }
 cudaError_t project(const DevCfg &c, const double *stats, const float *a, const float *b, int fused, float *maps,
                     int *counters, void *fq, long fq_cap, cudaStream_t st)
 {
-  const int tz = 4 * tile_zsteps(c.n);
+  const int tz = 4 * tile_zsteps(c);
   if (c.n % kTile || c.n % tz) return cudaErrorInvalidValue;
   const long nt = c.n / kTile;
   const unsigned blocks = (unsigned)(nt * nt * (c.n / tz));

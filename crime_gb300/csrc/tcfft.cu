@@ -46,10 +46,6 @@ constexpr float kStage2Scale = 1.f / 32.f;      // folded into the twiddle table
 
 __device__ __forceinline__ uint32_t core_off(int r, int j) { return (r >> 3) * kSBO + j * kLBO + (r & 7) * 16; }
 
-__device__ __forceinline__ uint32_t pack_half2(__half a, __half b)
-{
-  return (uint32_t)__half_as_ushort(a) | ((uint32_t)__half_as_ushort(b) << 16);
-}
 
 // element (column, e): input with the per-mode factor of the pass
 template <int MODE>

@@ -92,6 +92,8 @@ def lib():
         L.gethi_gpu_upload_inputs.restype = C.c_long
         L.gethi_gpu_kernel_times.argtypes = [vp, vp, vp, vp]
         L.gethi_gpu_fallback_count.argtypes = [vp, vp]
+        L.gethi_gpu_run_batch.argtypes = [vp, C.c_int, vp, vp, C.c_int, vp, C.c_int, vp]
+        L.gethi_gpu_autotune.argtypes = [vp, vp, vp]
         _lib = L
     return _lib
 
@@ -262,10 +264,42 @@ class GetHI:
         _check(lib().gethi_gpu_fallback_count(self._ctx, _ptr(v)))
         return int(v[0])
 
+    def autotune(self):
+        """Pick the fastest projection tile depth / column tile width for this
+        configuration (kept for the context's later work)."""
+        ch = np.zeros(2, np.int32)
+        ms = np.zeros(1, np.float32)
+        _check(lib().gethi_gpu_autotune(self._ctx, _ptr(ch), _ptr(ms)))
+        return {"tile_depth": 4 * int(ch[0]), "column_variant": int(ch[1]), "ms_per_realisation": float(ms[0])}
+
     def stage_times(self):
         ms = np.zeros(8, np.float32)
         k = lib().gethi_gpu_stage_times(self._ctx, _ptr(ms), 8)
         return ms[:max(k, 0)]
+
+
+def run_batch(contexts, jobs, download=True, graph=True):
+    """A batch of Philox realisations: jobs = [(context index, seed), ...].  Jobs of
+    one context run in order, contexts run concurrently; graph=True captures the
+    whole batch into one CUDA graph.  Returns (maps per job or None, stats dict)."""
+    nctx = len(contexts)
+    ctx_arr = (C.c_void_p * nctx)(*[c._ctx.value for c in contexts])
+    job_ctx = np.ascontiguousarray([j[0] for j in jobs], np.int32)
+    seeds = np.ascontiguousarray([j[1] & 0xFFFFFFFF for j in jobs], np.uint32)
+    maps = None
+    ptrs = None
+    if download:
+        sizes = [contexts[j[0]].n_nu * contexts[j[0]].npix for j in jobs]
+        buf = np.empty(sum(sizes), np.float32)
+        offs = np.concatenate([[0], np.cumsum(sizes)])
+        maps = [buf[offs[i]:offs[i + 1]].reshape(contexts[j[0]].n_nu, contexts[j[0]].npix)
+                for i, j in enumerate(jobs)]
+        ptrs = (C.c_void_p * len(jobs))(*[m.ctypes.data for m in maps])
+    st = np.zeros(4)
+    _check(lib().gethi_gpu_run_batch(ctx_arr, nctx, _ptr(job_ctx), _ptr(seeds), len(jobs), ptrs, int(bool(graph)),
+                                     _ptr(st)))
+    return maps, {"capture_ms": float(st[0]), "device_ms": float(st[1]), "graph_nodes": int(st[2]),
+                  "kernel_launches": int(st[3])}
 
 
 def read_run_params(fname, device=0):

@@ -122,6 +122,29 @@ int gethi_gpu_set_seed(gethi_ctx *ctx, unsigned int seed);
  * byte count (>= 0) or an error code. */
 long gethi_gpu_upload_inputs(gethi_ctx *ctx);
 
+/* ---- ensembles ----
+ * The reference runs one realisation per process (src/main_gh.c:24-80); an
+ * ensemble is many runs of GetHI with different seed= values.  This runs a
+ * batch of Philox realisations in one call: job i uses context ctx[job_ctx[i]]
+ * (one configuration: grid, box, shells) with seed seeds[i] and, maps_out !=
+ * NULL and maps_out[i] != NULL, copies its maps [n_nu][12 n_side^2] (mK) to
+ * maps_out[i] (device memory, page-locked host memory, or pageable host memory,
+ * which is page-locked for the duration of the call).  Jobs of one context run
+ * in order on its stream; different contexts run concurrently.  use_graph != 0:
+ * the whole batch is captured into one CUDA graph and launched once.
+ * stats (may be NULL) receives {capture + instantiate ms, device ms of the
+ * batch, graph nodes, kernel launches}.  Contexts must be on one device with
+ * rng=philox. */
+int gethi_gpu_run_batch(gethi_ctx *const *ctx, int nctx, const int *job_ctx, const unsigned int *seeds, int njobs,
+                        float *const *maps_out, int use_graph, double *stats);
+/* Launch-shape autotuner (no counterpart in the reference): times each
+ * candidate projection tile depth (8 x 8 x {16, 8, 4} cells) and, for n_grid
+ * 128/256/384, the half-width column tile of the FP32 passes on this context's
+ * own realisations, and keeps the fastest for the context's later work.
+ * choice (may be NULL) = {tile depth / 4, column variant}; ms = best time per
+ * realisation. */
+int gethi_gpu_autotune(gethi_ctx *ctx, int *choice, float *ms);
+
 /* ---- validation / inspection (compact [z][y][x] float grids, N^3) ---- */
 int gethi_gpu_download_grids(const gethi_ctx *ctx, float *dens, float *rvel);
 int gethi_gpu_upload_grids(gethi_ctx *ctx, const float *dens, const float *rvel, int stage);
