@@ -44,7 +44,7 @@ namespace gethi {
 //   MODE 5: out = FFT(i ky in)  (ky of the element; 0 at the Nyquist index)
 // ---------------------------------------------------------------------------
 template <int L, int P, int TX, class Rad, int MODE>
-__global__ void __launch_bounds__(TX *(L / P), 2)
+__global__ void __launch_bounds__(TX *(L / P), TX *(L / P) >= 512 ? 1 : 2)
     col_pass_kernel(DevCfg c, ColGeom g, int nyq, int nout, const float2 *__restrict__ src,
                     const float2 *__restrict__ tw, float2 *out1, float2 *out2)
 {
@@ -389,8 +389,9 @@ __global__ void modes_kernel(DevCfg c, float2 *out)
 template <int L> struct ColPlan;
 template <int M> struct RowPlan;
 template <int M> struct RowPlanV;
-// columns: L = N; P points per thread, TX columns per block
-template <> struct ColPlan<2048> { static constexpr int P = 32, TX = 4; using R = Radices<32, 8, 8>; };
+// columns: L = N; P points per thread, TX columns per block.  At 2048 points a column of the
+// spectrum steps 16 MB per element, so wide tiles (512 threads) keep the pages touched per byte low
+template <> struct ColPlan<2048> { static constexpr int P = 32, TX = 8; using R = Radices<32, 8, 8>; };
 template <> struct ColPlan<1024> { static constexpr int P = 32, TX = 8; using R = Radices<32, 32>; };
 template <> struct ColPlan<512> { static constexpr int P = 32, TX = 16; using R = Radices<32, 16>; };
 template <> struct ColPlan<384> { static constexpr int P = 24, TX = 16; using R = Radices<8, 8, 6>; };
@@ -408,7 +409,7 @@ template <> struct ColPlanNarrow<128> { static constexpr int P = 16, TX = 8; usi
 template <int L> constexpr bool has_narrow() { return L == 128 || L == 256 || L == 384; }
 // columns of the drawing Z pass (modes kept in registers for up to three transforms)
 template <int L> struct ColPlanGen : ColPlan<L> {};
-template <> struct ColPlanGen<2048> { static constexpr int P = 16, TX = 2; using R = Radices<16, 16, 8>; };
+template <> struct ColPlanGen<2048> { static constexpr int P = 16, TX = 4; using R = Radices<16, 16, 8>; };
 template <> struct ColPlanGen<1024> { static constexpr int P = 16, TX = 4; using R = Radices<16, 16, 4>; };
 template <> struct ColPlanGen<512> { static constexpr int P = 16, TX = 8; using R = Radices<16, 16, 2>; };
 // rows: M = N/2 (single field)
