@@ -26,6 +26,8 @@
 #define ORC_NU21 1420.40575177 /* src/common.h:38 */
 #define ORC_NSUB 10          /* src/pixelize.c:25 */
 #define ORC_HMPC 2997.92458  /* src/cosmo_mad.h:35 */
+#define ORC_NZ_PS 256        /* src/common_gh.h:35 */
+#define ORC_NL_PS 256        /* src/psources.c:24 */
 
 #ifdef __cplusplus
 extern "C" {
@@ -124,6 +126,20 @@ void orc_channel_prefactors(const orc_config *c, const orc_derived *d, const dou
 /* ---- whole realisation (CPU baseline) ---- */
 int orc_num_threads(void);
 void orc_set_threads(int t);
+
+/* Point sources (src/psources.c, grid_tools.c:24-101, pixelize.c:58-148); orc_psources.c */
+void orc_setup_psources(double z_max, double *nz_arr, double *maxpdf, double *glob_dz);
+double orc_n_of_z_psources(const double *nz_arr, double glob_dz, double z);
+long orc_poisson_small(orc_mt *r, double mu);
+double orc_temp_of_l(double hhub, double L0, double nu_obs, double z, double r, double dOmega);
+long orc_point_sources(const orc_config *c, const orc_derived *d, const double *nz_arr, double glob_dz,
+                       const float *dens, double sigma2, int nthreads, int *nsources);
+void orc_psources_maps(const orc_config *c, const orc_derived *d, const double *nu0, const double *nuf,
+                       const double *nz_arr, const double *maxpdf, double glob_dz, const int *nsources,
+                       const float *dz, int nthreads, float *maps_ps);
+void orc_psources_maps_catalogue(const orc_config *c, const orc_derived *d, const double *nu0, const double *nuf,
+                                 long ns, const int64_t *cell, const double *u, const double *L0,
+                                 const double *dzs, double *maps_ps, int64_t *pix);
 
 #ifdef __cplusplus
 }

@@ -72,6 +72,17 @@ def lib():
         L.orc_mk_T_maps.argtypes = [P(Config), P(Derived), f64p, f64p, f32p, f32p, f32p, C.c_void_p]
         L.orc_channel_prefactors.argtypes = [P(Config), P(Derived), f64p, f64p, f64p]
         L.orc_philox4x32_10.argtypes = [u32p, u32p, u32p]
+        i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+        i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+        L.orc_setup_psources.argtypes = [C.c_double, f64p, f64p, P(C.c_double)]
+        L.orc_point_sources.argtypes = [P(Config), P(Derived), f64p, C.c_double, f32p, C.c_double, C.c_int, i32p]
+        L.orc_point_sources.restype = C.c_long
+        L.orc_psources_maps.argtypes = [P(Config), P(Derived), f64p, f64p, f64p, f64p, C.c_double, i32p, f32p,
+                                        C.c_int, f32p]
+        L.orc_psources_maps_catalogue.argtypes = [P(Config), P(Derived), f64p, f64p, C.c_long, i64p, f64p, f64p,
+                                                  f64p, f64p, i64p]
+        L.orc_n_of_z_psources.argtypes = [f64p, C.c_double, C.c_double]
+        L.orc_n_of_z_psources.restype = C.c_double
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_num_threads.restype = C.c_int
         _lib = L
@@ -148,6 +159,44 @@ class Oracle:
         lib().orc_modes_philox_pg(C.byref(self.c), C.byref(self.d), self.logk, self.pk, pg.reshape(-1),
                                   dk.view(np.float32))
         return dk
+
+    # ---- point sources (src/psources.c, grid_tools.c:24-101, pixelize.c:58-148)
+    def setup_psources(self):
+        nz, mp, gdz = np.zeros(256), np.zeros(256), C.c_double()
+        lib().orc_setup_psources(self.d.z_max, nz, mp, C.byref(gdz))
+        return nz, mp, gdz.value
+
+    def point_sources(self, dens_padded, sigma2, nthreads=1):
+        nz, _, gdz = self.setup_psources()
+        ns = np.zeros(self.real_pad_shape(), np.int32)
+        tot = lib().orc_point_sources(C.byref(self.c), C.byref(self.d), nz, gdz,
+                                      np.ascontiguousarray(dens_padded, np.float32).reshape(-1), sigma2, nthreads,
+                                      ns.reshape(-1))
+        if tot < 0:
+            raise ValueError("a cell's Poisson mean exceeds the restated range (<= 10)")
+        return ns
+
+    def psources_maps(self, nsources_padded, dz_padded, nthreads=1):
+        nz, mp, gdz = self.setup_psources()
+        npix = 12 * self.c.n_side ** 2
+        maps = np.zeros((self.c.n_nu, npix), np.float32)
+        lib().orc_psources_maps(C.byref(self.c), C.byref(self.d), self.nu0, self.nuf, nz, mp, gdz,
+                                np.ascontiguousarray(nsources_padded, np.int32).reshape(-1),
+                                np.ascontiguousarray(dz_padded, np.float32).reshape(-1), nthreads, maps.reshape(-1))
+        return maps
+
+    def psources_maps_catalogue(self, cells, u, L0, dz):
+        """FP64 maps and pixels of a given source catalogue."""
+        ns = len(cells)
+        npix = 12 * self.c.n_side ** 2
+        maps = np.zeros((self.c.n_nu, npix))
+        pix = np.zeros(ns, np.int64)
+        lib().orc_psources_maps_catalogue(C.byref(self.c), C.byref(self.d), self.nu0, self.nuf, ns,
+                                          np.ascontiguousarray(cells, np.int64),
+                                          np.ascontiguousarray(u, np.float64).reshape(-1),
+                                          np.ascontiguousarray(L0, np.float64),
+                                          np.ascontiguousarray(dz, np.float64), maps.reshape(-1), pix)
+        return maps, pix
 
     def c2r(self, spec):
         """In-place padded c2r of a half spectrum, float32 result (FFTW layout)."""

@@ -1,6 +1,6 @@
 /*
  * Test-infrastructure driver: runs the reference's GetHI stages
- * (src/main_gh.c:24-80 minus point sources and FITS output) and dumps every
+ * (src/main_gh.c:24-80 minus FITS output) and dumps every
  * stage's buffers as raw files, so the fixture script can turn them into
  * golden vectors.  Usage: gethi_ref <param.ini> <outdir>
  */
@@ -58,6 +58,14 @@ int main(int argc, char **argv)
 
   create_d_and_vr_fields(par);
   fprintf(f, "sigma2_gauss %.17g\n", par->sigma2_gauss);
+  if (par->do_psources) {  /* src/main_gh.c:55-58 */
+    setup_psources(par);
+    get_point_sources(par);
+    fprintf(f, "glob_dz %.17g\n", par->glob_dz);
+    dump(od, "ps_nz.f64", par->nz_psources_arr, sizeof(double) * NZ_PSOURCES);
+    dump(od, "ps_maxpdf.f64", par->max_Lpdf_arr, sizeof(double) * NZ_PSOURCES);
+    dump(od, "nsources.i32", par->nsources, ngrid * sizeof(int));
+  }
   fclose(f);
   size_t nspec = (size_t)n * n * (n / 2 + 1) * 2 * sizeof(float);
   dump(od, "dens_k.f32", shim_captured[0], nspec);
@@ -72,5 +80,9 @@ int main(int argc, char **argv)
 
   mk_T_maps(par);
   dump(od, "maps.f32", par->maps_HI, sizeof(float) * par->n_nu * 12 * par->n_side * par->n_side);
+  if (par->do_psources) {  /* src/main_gh.c:63-64 */
+    mk_psources_maps(par);
+    dump(od, "maps_ps.f32", par->maps_PS, sizeof(float) * par->n_nu * 12 * par->n_side * par->n_side);
+  }
   return 0;
 }

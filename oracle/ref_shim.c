@@ -25,7 +25,17 @@ gsl_rng *gsl_rng_alloc(const gsl_rng_type *T) { (void)T; return (gsl_rng *)callo
 void gsl_rng_set(const gsl_rng *r, unsigned long int s) { orc_mt_seed((orc_mt *)&r->mt, (uint32_t)s); }
 double gsl_rng_uniform(const gsl_rng *r) { return orc_mt_uniform((orc_mt *)&r->mt); }
 void gsl_rng_free(gsl_rng *r) { free(r); }
-unsigned int gsl_ran_poisson(const gsl_rng *r, double mu) { (void)r; (void)mu; abort(); }
+/* GSL's gsl_ran_poisson for mu <= 10 (Knuth's multiplication method, restated in
+ * orc_psources.c); the golden cases keep every cell's mean below 10 */
+unsigned int gsl_ran_poisson(const gsl_rng *r, double mu)
+{
+  long k = orc_poisson_small((orc_mt *)&r->mt, mu);
+  if (k < 0) {
+    fprintf(stderr, "shim: gsl_ran_poisson with mu = %g > 10 is not restated\n", mu);
+    abort();
+  }
+  return (unsigned int)k;
+}
 
 /* ---- GSL errors / quadrature ---- */
 gsl_error_handler_t *gsl_set_error_handler_off(void) { return NULL; }
@@ -97,12 +107,6 @@ void fftwf_cleanup_threads(void) {}
 void vec2pix_ring(long nside, const double *vec, long *ipix) { *ipix = orc_vec2pix_ring(nside, vec); }
 long nside2npix(long nside) { return 12 * nside * nside; }
 
-/* ---- healpix_extra.c / psources.c entry points (not on the tested path) ---- */
+/* ---- healpix_extra.c entry point (FITS output is not on the tested path) ---- */
 void he_write_healpix_map(float **tmap, int nfields, long nside, char *fname)
 { (void)tmap; (void)nfields; (void)nside; (void)fname; }
-void setup_psources(ParamGetHI *par) { (void)par; abort(); }
-double n_of_z_psources(ParamGetHI *par, double z) { (void)par; (void)z; abort(); }
-double bias_psources(double z) { (void)z; abort(); }
-double draw_luminosity(ParamGetHI *par, double redshift, gsl_rng *rng) { (void)par; (void)redshift; (void)rng; abort(); }
-double temp_of_l(ParamGetHI *par, double L0, double nu_obs, double z, double r, double dOmega)
-{ (void)par; (void)L0; (void)nu_obs; (void)z; (void)r; (void)dOmega; abort(); }

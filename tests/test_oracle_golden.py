@@ -75,3 +75,40 @@ def test_maps_bitexact(case):
     maps = o.mk_T_maps(g["mass"], g["dz"])
     np.testing.assert_array_equal(maps.reshape(-1), g["maps"])
     assert np.count_nonzero(maps) > 0.5 * maps.size
+
+
+# ---- point sources (src/psources.c, grid_tools.c:24-101, pixelize.c:58-148)
+@pytest.fixture(scope="module")
+def ps_case(oracle_lib):
+    oracle_lib.set_threads(1)
+    g = load_case("case_ps32")
+    return g, oracle_for_case(g)
+
+
+def test_psources_tables_bitexact(ps_case):
+    g, o = ps_case
+    nz, mp, gdz = o.setup_psources()
+    assert gdz == g["p_glob_dz"]
+    np.testing.assert_array_equal(nz, g["ps_nz"])
+    np.testing.assert_array_equal(mp, g["ps_maxpdf"])
+
+
+@pytest.mark.parametrize("nthreads,name", [(1, "case_ps32"), (3, "case_ps32_t3")])
+def test_point_source_counts_bitexact(ps_case, nthreads, name):
+    _, o = ps_case
+    g = load_case(name)  # the 3-thread run draws other modes, so its own density field
+    ns = o.point_sources(g["dens_real"], float(g["p_sigma2_gauss"]), nthreads=nthreads)
+    ref = g["nsources"]
+    np.testing.assert_array_equal(ns.reshape(-1), ref)
+    assert ref.sum() > 1000 and ref.max() >= 2
+
+
+def test_psources_maps_bitexact(ps_case):
+    g, o = ps_case
+    maps = o.psources_maps(g["nsources"], g["dz"], nthreads=1)
+    np.testing.assert_array_equal(maps.reshape(-1), g["maps_ps"])
+    assert maps.sum() > 0
+    # the catalogue form of the same sum (FP64) agrees to rounding
+    n = o.n
+    ns = g["nsources"].reshape(n, n, 2 * (n // 2 + 1))[:, :, :n]
+    assert (ns > 0).sum() > 100
