@@ -56,6 +56,10 @@ struct gethi_ctx {
   void *fq = nullptr;       // queue of samples whose FP32 key is uncertain
   long fq_cap = 0;
   float2 *pg = nullptr, *pgn = nullptr;  // Gaussianised spectrum (gaussianise=1)
+  // point sources (do_psources=1): per-pixel sums, channel maps, tables, source count
+  float *ps_acc = nullptr, *maps_ps = nullptr, *ps_nz = nullptr, *ps_icdf = nullptr, *ps_chan = nullptr;
+  unsigned long long *ps_total = nullptr;
+  PsConst psc{};
   uint4 *tc_bmat = nullptr;                // fft_precision=tc_split tables and error flag
   float2 *tc_tw = nullptr;
   int *tc_err = nullptr;
@@ -268,6 +272,19 @@ int ensure_pg(gethi_ctx *c)
   return make_pg(c);
 }
 
+// point sources of the current (Gaussian) fields into maps_ps; cat != nullptr
+// also records the sources
+int enqueue_psources(gethi_ctx *c, cudaStream_t st, const PsCatalogue *cat)
+{
+  PsCatalogue none{};
+  CK(cudaMemsetAsync(c->ps_total, 0, sizeof(unsigned long long), st));
+  KTimer t(c, KC_PSOURCES);
+  CK(psources(c->cfg, c->psc, c->stats, reinterpret_cast<const float *>(c->main), c->vr, c->ps_acc, c->maps_ps,
+              c->ps_chan, c->ps_total, cat ? *cat : none, st));
+  c->launches += 1;
+  return GETHI_OK;
+}
+
 // All Fourier-space work of one realisation: one Z pass drawing the modes and
 // transforming delta (+ phi, + i kz phi), Y passes, X passes.
 int fields_fft(gethi_ctx *c, const float2 *src)
@@ -402,6 +419,28 @@ extern "C" int gethi_gpu_init(const gethi_params *p, int device, gethi_ctx **out
     gethi_gpu_free(c);
     return rc;
   }
+  if (s.p.do_psources) {
+    const int ni = PS_NICDF;
+    if ((rc = dalloc(&c->ps_acc, (size_t)2 * npix)) || (rc = dalloc(&c->maps_ps, (size_t)npix * s.p.n_nu)) ||
+        (rc = dalloc(&c->ps_nz, (size_t)PS_NZ)) || (rc = dalloc(&c->ps_icdf, (size_t)ni + 1)) ||
+        (rc = dalloc(&c->ps_chan, (size_t)2 * s.p.n_nu)) || (rc = dalloc(&c->ps_total, 1))) {
+      gethi_gpu_free(c);
+      return rc;
+    }
+    std::vector<float> v(s.ps_nz.begin(), s.ps_nz.end());
+    cudaMemcpy(c->ps_nz, v.data(), sizeof(float) * v.size(), cudaMemcpyHostToDevice);
+    v.assign(s.ps_icdf.begin(), s.ps_icdf.end());
+    cudaMemcpy(c->ps_icdf, v.data(), sizeof(float) * v.size(), cudaMemcpyHostToDevice);
+    v.assign(s.ps_chan.begin(), s.ps_chan.end());
+    cudaMemcpy(c->ps_chan, v.data(), sizeof(float) * v.size(), cudaMemcpyHostToDevice);
+    const double dx = s.d.l_box / n;
+    c->psc.nz = c->ps_nz;
+    c->psc.icdf = c->ps_icdf;
+    c->psc.inv_dz = (float)(1.0 / s.ps_glob_dz);
+    c->psc.z_max = (float)s.d.z_max;
+    c->psc.cell_vol = (float)(dx * dx * dx);
+    c->psc.nicdf = ni;
+  }
   if (s.p.fft_precision == 1) {
     std::vector<uint16_t> bm;
     std::vector<float2> tw;
@@ -476,7 +515,8 @@ extern "C" void gethi_gpu_free(gethi_ctx *c)
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   void *bufs[] = {c->main, c->nyq, c->bA, c->bAn, c->bB, c->bBn, c->bC, c->bCn, c->modes, c->vr, c->pg, c->pgn,
-                  c->tc_bmat, c->tc_tw, c->tc_err, c->maps, c->twN, c->twM, c->partials,
+                  c->tc_bmat, c->tc_tw, c->tc_err, c->ps_acc, c->maps_ps, c->ps_nz, c->ps_icdf, c->ps_chan,
+                  c->ps_total, c->maps, c->twN, c->twM, c->partials,
                   c->stats, c->pk_f, c->logk_f, c->tab_f, c->tab_d, c->prefac, c->edges_f, c->edges_d, c->counters};
   for (void *b : bufs)
     if (b) cudaFree(b);
@@ -550,6 +590,10 @@ extern "C" int gethi_gpu_make_fields(gethi_ctx *c, const float *modes_k)
   record(c);
   int rc = fields_fft(c, src);
   if (rc) return rc;
+  if (s.p.do_psources) {  // src/main_gh.c:55-58: on the Gaussian field, before get_HI
+    rc = enqueue_psources(c, c->stream, nullptr);
+    if (rc) return rc;
+  }
   record(c);
   c->stage = 1;
   return GETHI_OK;
@@ -707,8 +751,8 @@ extern "C" int gethi_gpu_run_batch(gethi_ctx *const *ctxs, int nctx, const int *
 {
   if (!ctxs || nctx < 1 || !job_ctx || !seeds || njobs < 0) return GETHI_E_ARG;
   for (int k = 0; k < nctx; k++)
-    if (!ctxs[k] || ctxs[k]->device != ctxs[0]->device || ctxs[k]->s.p.rng != 0) {
-      set_error("run_batch: contexts must be valid, on one device, with rng=philox");
+    if (!ctxs[k] || ctxs[k]->device != ctxs[0]->device || ctxs[k]->s.p.rng != 0 || ctxs[k]->s.p.do_psources) {
+      set_error("run_batch: contexts must be valid, on one device, with rng=philox and no point sources");
       return GETHI_E_ARG;
     }
   for (int i = 0; i < njobs; i++)
@@ -880,7 +924,82 @@ extern "C" int gethi_gpu_write_maps(const gethi_ctx *c, const float *maps)
       return GETHI_E_IO;
     }
   }
+  if (s.p.do_psources) {  // <prefix>_ps_%03d.fits (src/io_gh.c:122-128)
+    std::vector<float> ps((size_t)npix * s.p.n_nu);
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(ps.data(), c->maps_ps, sizeof(float) * ps.size(), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < s.p.n_nu; i++) {
+      char fn[600];
+      std::snprintf(fn, sizeof(fn), "%s_ps_%03d.fits", s.p.prefix_out, i + 1);
+      if (write_fits_map(fn, ps.data() + (size_t)i * npix, s.p.n_side)) {
+        set_error(std::string("cannot write ") + fn);
+        return GETHI_E_IO;
+      }
+    }
+  }
   return GETHI_OK;
+}
+
+extern "C" int gethi_gpu_psources_maps(gethi_ctx *c, float *maps_out, long *nsources)
+{
+  if (!c) return GETHI_E_ARG;
+  if (!c->s.p.do_psources) {
+    set_error("psources_maps: do_psources=0");
+    return GETHI_E_STATE;
+  }
+  if (c->stage < 1) {
+    set_error("psources_maps needs the fields of gethi_gpu_make_fields");
+    return GETHI_E_STATE;
+  }
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  const size_t bytes = sizeof(float) * 12 * (size_t)c->s.p.n_side * c->s.p.n_side * c->s.p.n_nu;
+  if (maps_out) CK(cudaMemcpy(maps_out, c->maps_ps, bytes, cudaMemcpyDeviceToHost));
+  if (nsources) {
+    unsigned long long t = 0;
+    CK(cudaMemcpy(&t, c->ps_total, sizeof(t), cudaMemcpyDeviceToHost));
+    *nsources = (long)t;
+  }
+  return GETHI_OK;
+}
+
+extern "C" int gethi_gpu_psources_catalogue(gethi_ctx *c, long cap, long *cell, float *u_l, float *dz, int *pix,
+                                            long *count)
+{
+  if (!c || cap < 0 || (cap > 0 && (!cell || !u_l || !dz || !pix))) return GETHI_E_ARG;
+  if (!c->s.p.do_psources || (c->stage != 1 && c->stage != 3)) {
+    set_error("psources_catalogue: needs do_psources=1 and the Gaussian fields (before get_HI)");
+    return GETHI_E_STATE;
+  }
+  CK(cudaSetDevice(c->device));
+  PsCatalogue cat{};
+  const size_t m = cap > 0 ? (size_t)cap : 1;
+  int rc = dalloc(&cat.count, 1);
+  if (!rc) rc = dalloc(&cat.cell, m);
+  if (!rc) rc = dalloc(&cat.u, m);
+  if (!rc) rc = dalloc(&cat.dz, m);
+  if (!rc) rc = dalloc(&cat.pix, m);
+  cat.cap = cap;
+  unsigned long long k = 0;
+  if (!rc && cudaMemsetAsync(cat.count, 0, sizeof(unsigned long long), c->stream) != cudaSuccess) rc = GETHI_E_CUDA;
+  if (!rc) rc = enqueue_psources(c, c->stream, &cat);
+  if (!rc && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = cuda_fail(cudaGetLastError(), "catalogue");
+  if (!rc && cudaMemcpy(&k, cat.count, sizeof(k), cudaMemcpyDeviceToHost) != cudaSuccess) rc = GETHI_E_CUDA;
+  const size_t got = (size_t)std::min<unsigned long long>(k, (unsigned long long)cap);
+  if (!rc && got) {
+    if (cudaMemcpy(cell, cat.cell, sizeof(long) * got, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(u_l, cat.u, sizeof(float4) * got, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(dz, cat.dz, sizeof(float) * got, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(pix, cat.pix, sizeof(int) * got, cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = GETHI_E_CUDA;
+  }
+  cudaFree(cat.count);
+  cudaFree(cat.cell);
+  cudaFree(cat.u);
+  cudaFree(cat.dz);
+  cudaFree(cat.pix);
+  if (count) *count = (long)k;
+  return rc;
 }
 
 extern "C" int gethi_gpu_download_grids(const gethi_ctx *c, float *dens, float *rvel)

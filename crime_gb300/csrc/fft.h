@@ -11,7 +11,7 @@ namespace gethi {
 
 enum KernelClass {
   KC_ZPASS = 0, KC_YPASS, KC_XPASS, KC_XPASS_VEL, KC_NYQ, KC_SIGMA, KC_FDVEL, KC_GETHI, KC_PROJECT, KC_SCALE,
-  KC_ZPASS_RAW, KC_FIXUP
+  KC_ZPASS_RAW, KC_FIXUP, KC_PSOURCES
 };
 
 enum FieldKind { FIELD_DENS = 0, FIELD_VPOT = 1, FIELD_VX = 2, FIELD_VY = 3, FIELD_VZ = 4 };
@@ -46,6 +46,28 @@ cudaError_t tc_col_pass(const DevCfg &c, const ColGeom &g, int mode, int nout, c
                         float2 *out2, cudaStream_t st);
 bool tc_tables(int n, std::vector<uint16_t> &bmat, std::vector<float2> &tw);
 size_t tc_table_bytes();
+
+// point sources (stages.cu)
+constexpr int kPsNZ = 256;                  // src/common_gh.h:35 (NZ_PSOURCES)
+constexpr uint32_t kPsKey = 0x50535243u;    // second Philox key word of the point-source draws
+struct PsConst {
+  const float *nz;    // n(z) at z = i * glob_dz, kPsNZ entries
+  const float *icdf;  // log10 L at probabilities q / nicdf, nicdf + 1 entries
+  float inv_dz, z_max, cell_vol;
+  int nicdf;
+};
+// sources captured for inspection (count == nullptr: none): cell index, (ux, uy, uz, L0), dz_rsd, pixel
+struct PsCatalogue {
+  unsigned long long *count;
+  long cap;
+  long *cell;
+  float4 *u;
+  float *dz;
+  int *pix;
+};
+cudaError_t psources(const DevCfg &c, const PsConst &p, const double *stats, const float *dens, const float *vr,
+                     float *acc, float *maps_ps, const float *chan, unsigned long long *total, const PsCatalogue &cat,
+                     cudaStream_t st);
 
 // stages.cu
 cudaError_t radial_velocity_fd(const DevCfg &c, const float *vpot, float *rvel, cudaStream_t st);

@@ -396,7 +396,6 @@ int setup_build(const gethi_params &p, Setup &s, std::string &err)
   std::memset(&s.d, 0, sizeof(s.d));
   if (p.n_grid < 4 || (p.n_grid & 1)) { err = "n_grid must be even and >= 4"; return GETHI_E_ARG; }
   if (p.n_side < 1 || p.n_side > 8192) { err = "n_side out of range"; return GETHI_E_ARG; }
-  if (p.do_psources) { err = "do_psources=1: point sources are not part of this path"; return GETHI_E_ARG; }
   if (p.fft_precision == 1 && p.n_grid != 1024) {
     err = "fft_precision=tc_split: the tensor-core column transform is built for n_grid=1024";
     return GETHI_E_ARG;
@@ -542,6 +541,8 @@ int setup_build(const gethi_params &p, Setup &s, std::string &err)
     double r = r_of_z(s, NU21 / nu - 1);
     s.prefac[inu] = M2T / (r * r * dnu);
   }
+
+  if (p.do_psources) setup_psources(s);
 
   // fraction of the shell volume [r_min, r_max] inside the box (for reporting)
   {
@@ -699,7 +700,102 @@ int write_fits_map(const char *fname, const float *map, long nside)
   return ok ? GETHI_OK : GETHI_E_IO;
 }
 
+// ---- point sources ----
+namespace {
+constexpr double kLLogMin = -5., kLLogMax = 6.;                 // src/psources.c:25-26
+constexpr double kLX = 2.11, kAlpha = -0.633, kRho = 3.2E-4;    // src/psources.c:33-35
+constexpr double kSedNorm = 0.114461;                           // src/psources.c:54
+constexpr double kFlux2Temp = 3.2548291E-2, kLum2Flux = 8.35774E7;  // src/psources.c:154-155
+
+// dn(z, L)/dlog10(L), L in 1e22 W/Hz (src/psources.c:39-52)
+double l_z_function(double L, double z)
+{
+  double rho_l = 2.5 * M_LN10 * kRho * std::pow(L / kLX, kAlpha + 1) * std::exp(-L / kLX);
+  double fz = z < 1.5 ? std::pow(1 + z, 3.1) : 17.124;
+  return fz * rho_l;
+}
+}  // namespace
+
+void setup_psources(Setup &s)
+{
+  // n(z) on NZ_PSOURCES bins of z_max / 256 and the rejection bound (src/psources.c:98-124)
+  const int NL = 256;
+  const double dlogL = (kLLogMax - kLLogMin) / NL;
+  s.ps_glob_dz = s.d.z_max / PS_NZ;
+  s.ps_nz.assign(PS_NZ, 0.0);
+  s.ps_maxpdf.assign(PS_NZ, 0.0);
+  for (int ii = 0; ii < PS_NZ; ii++) {
+    double z = ii * s.ps_glob_dz, max_dist = -1;
+    for (int jj = 0; jj < NL; jj++) {
+      double lfunc = l_z_function(std::pow(10., kLLogMin + (jj + 0.5) * dlogL), z);
+      if (lfunc >= max_dist) max_dist = lfunc;
+      s.ps_nz[ii] += dlogL * lfunc;
+    }
+    s.ps_maxpdf[ii] = s.ps_nz[ii] > 0 ? 1.1 * max_dist / s.ps_nz[ii] : 0;
+  }
+  // The reference draws log10 L by rejection with density proportional to
+  // l_z_function(L, z) on [-5, 6] (src/psources.c:126-152).  Its z factor cancels,
+  // so one inverse CDF serves every redshift: CDF by the trapezoid rule on a fine
+  // grid, inverted at PS_NICDF + 1 equally spaced probabilities.
+  const int M = 1 << 18;
+  std::vector<double> cdf(M + 1, 0.0);
+  double prev = l_z_function(std::pow(10., kLLogMin), 0.0);
+  for (int i = 1; i <= M; i++) {
+    double f = l_z_function(std::pow(10., kLLogMin + (kLLogMax - kLLogMin) * i / M), 0.0);
+    cdf[i] = cdf[i - 1] + 0.5 * (prev + f);
+    prev = f;
+  }
+  s.ps_icdf.assign(PS_NICDF + 1, 0.0);
+  int j = 0;
+  for (int q = 0; q <= PS_NICDF; q++) {
+    double target = cdf[M] * q / PS_NICDF;
+    while (j < M && cdf[j + 1] < target) j++;
+    double t = (j < M && cdf[j + 1] > cdf[j]) ? (target - cdf[j]) / (cdf[j + 1] - cdf[j]) : 0.0;
+    if (t > 1) t = 1;
+    s.ps_icdf[q] = kLLogMin + (kLLogMax - kLLogMin) * (j + t) / M;
+  }
+  s.ps_icdf[0] = kLLogMin;
+  s.ps_icdf[PS_NICDF] = kLLogMax;
+  // temp_of_l (src/psources.c:158-167) with spec_ed (src/psources.c:55-63) is
+  //   T = K L0 [(1+z)^-0.1 nu_GHz^-0.1 + 10 (1+z)^-0.75 nu_GHz^-0.75] / (r^2 (1+z) nu^2),
+  //   K = FLUX2TEMP LUM2FLUX 4 pi SED_NORM h^2 / dOmega,
+  // so per pixel S1 = sum L0 (1+z)^-1.1 / r^2 and S2 = sum 10 L0 (1+z)^-1.75 / r^2
+  // give every channel: T(nu) = a(nu) S1 + b(nu) S2.  Channel centres as in
+  // src/pixelize.c:64-71.
+  const double npix = 12.0 * s.p.n_side * s.p.n_side, dOmega = 4 * M_PI / npix;
+  const double K = kFlux2Temp * kLum2Flux * 4 * M_PI * kSedNorm * s.p.h * s.p.h / dOmega;
+  const bool regular = s.d.regular_nu != 0;
+  s.ps_chan.assign(2 * (size_t)s.p.n_nu, 0.0);
+  for (int inu = 0; inu < s.p.n_nu; inu++) {
+    double nu = regular ? s.p.nu_min + (s.p.nu_max - s.p.nu_min) * (inu + 0.5) / s.p.n_nu
+                        : (s.nu0[inu] + s.nuf[inu]) * 0.5;
+    double ng = nu * 0.001;
+    s.ps_chan[2 * inu] = K * std::pow(ng, -0.1) / (nu * nu);
+    s.ps_chan[2 * inu + 1] = K * std::pow(ng, -0.75) / (nu * nu);
+  }
+}
+
 }  // namespace gethi
+
+extern "C" int gethi_host_psources(const gethi_params *p, double *nz_arr, double *maxpdf, double *glob_dz,
+                                   double *logl_icdf)
+{
+  if (!p) return GETHI_E_ARG;
+  gethi_params q = *p;
+  q.do_psources = 1;
+  gethi::Setup s;
+  std::string err;
+  int rc = gethi::setup_build(q, s, err);
+  if (rc) {
+    gethi::set_error(err);
+    return rc;
+  }
+  if (nz_arr) std::memcpy(nz_arr, s.ps_nz.data(), sizeof(double) * gethi::PS_NZ);
+  if (maxpdf) std::memcpy(maxpdf, s.ps_maxpdf.data(), sizeof(double) * gethi::PS_NZ);
+  if (glob_dz) *glob_dz = s.ps_glob_dz;
+  if (logl_icdf) std::memcpy(logl_icdf, s.ps_icdf.data(), sizeof(double) * (gethi::PS_NICDF + 1));
+  return GETHI_OK;
+}
 
 extern "C" const char *gethi_last_error(void) { return gethi::g_err.c_str(); }
 

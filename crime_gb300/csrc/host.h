@@ -30,6 +30,11 @@ struct Setup {
   // per-channel temperature factor M2T/(r^2 dnu) (src/pixelize.c:399-414)
   std::vector<double> prefac;
   double n_scal;
+  // point sources (do_psources=1): n(z) and rejection bounds (src/psources.c:98-124),
+  // inverse CDF of log10 L, and per channel the factors a, b of
+  // T = a S1 + b S2 (S1, S2: the per-pixel sums of the sources)
+  std::vector<double> ps_nz, ps_maxpdf, ps_icdf, ps_chan;
+  double ps_glob_dz = 0;
 };
 
 // src/common.c:133-164 draw through GSL's mt19937; this is the published
@@ -43,6 +48,9 @@ struct MT19937 {
 };
 
 int setup_build(const gethi_params &p, Setup &s, std::string &err);
+constexpr int PS_NZ = 256;      // src/common_gh.h:35 (NZ_PSOURCES)
+constexpr int PS_NICDF = 4096;  // intervals of the log10 L inverse CDF
+void setup_psources(Setup &s);
 double z_of_r(const Setup &s, double r);  // src/cosmo.c:52-62
 double r_of_z(const Setup &s, double z);  // src/cosmo.c:40-50
 double pk_linear0(const Setup &s, double lgk);  // src/cosmo.c:153-170

@@ -209,6 +209,8 @@ constexpr uint32_t kKeyInvalid = 0xFFFFFFFFu;    // outside the shells
 constexpr uint32_t kKeyUncertain = 0xFFFFFFFEu;  // FP32 cannot decide: use key_exact
 // (valid keys are < n_nu * 12 nside^2 <= 2^32 - 2, checked at set-up)
 
+__device__ __forceinline__ uint32_t pixel_fast(const DevCfg &c, float X, float Y, float Z, float rho2, float iR);
+
 __device__ __forceinline__ uint32_t key_fast(const DevCfg &c, const FastConst &f, const float *ef, int log2nn, float X,
                                              float Y, float Z, float dz)
 {
@@ -247,7 +249,14 @@ __device__ __forceinline__ uint32_t key_fast(const DevCfg &c, const FastConst &f
   }
   if (bad || unc) return kKeyUncertain;
   if (inu < 0 || inu >= c.n_nu) return kKeyInvalid;
-  // ---- pixel (RING scheme)
+  const uint32_t pix = pixel_fast(c, X, Y, Z, rho2, iR);
+  return pix == kKeyUncertain ? kKeyUncertain : pix + (uint32_t)c.npix * (uint32_t)inu;
+}
+
+// RING pixel of (X, Y, Z) (cell units, |error| <= 6e-8 relative), rho2 = X^2 + Y^2,
+// iR = 1/|.|; kKeyUncertain when a floor or comparison is within its margin
+__device__ __forceinline__ uint32_t pixel_fast(const DevCfg &c, float X, float Y, float Z, float rho2, float iR)
+{
   const int nside = (int)c.nside;
   const float fn = (float)nside;
   const float cth = Z * iR;
@@ -296,7 +305,7 @@ __device__ __forceinline__ uint32_t key_fast(const DevCfg &c, const FastConst &f
     const int ip = q * ring + (int)u5;  // floor(tt ring) < 4 ring
     pix = (cth > 0) ? 2 * ring * (ring - 1) + ip : npix - 2 * ring * (ring + 1) + ip;
   }
-  return (uint32_t)pix + (uint32_t)npix * (uint32_t)inu;
+  return (uint32_t)pix;
 }
 
 // ---------------------------------------------------------------------------
@@ -587,6 +596,176 @@ cudaError_t sample_keys(const DevCfg &c, const float *dz, uint32_t *keys, int ex
 {
   long total = (long)c.n * c.n * c.n;
   sample_keys_kernel<<<grid_for(total, 128), 128, 0, st>>>(c, fast_const(c), dz, keys, exact, counters);
+  return cudaGetLastError();
+}
+
+
+// ---------------------------------------------------------------------------
+// point sources: get_point_sources (src/grid_tools.c:24-101) and
+// mk_psources_maps (src/pixelize.c:58-148) fused, one thread per cell.
+// Counter-based draws: Philox4x32-10 with key (seed, 0x50535243) and counter
+// (cell lo, cell hi, stream, block): stream 0 feeds the Poisson count, stream
+// 1 + s the position (3 uniforms) and luminosity (1 uniform) of source s.
+// Each source adds L0 (1+z)^-1.1 / r^2 and 10 L0 (1+z)^-1.75 / r^2 to its pixel's
+// two sums, from which every channel follows (ps_expand_kernel).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float u01(uint32_t w) { return ((float)(w >> 8) + 0.5f) * (1.f / 16777216.f); }
+
+// n_of_z_psources (src/psources.c:74-90)
+__device__ __forceinline__ float ps_n_of_z(const PsConst &p, float z)
+{
+  const float t = z * p.inv_dz;
+  if (!(t > -1.f) || t >= (float)kPsNZ) return -1.f;  // (int) truncation: iz in [0, 256)
+  const int iz = (int)t;
+  if (iz == kPsNZ - 1) return __ldg(&p.nz[kPsNZ - 1]);
+  const float a = __ldg(&p.nz[iz]), b = __ldg(&p.nz[iz + 1]);
+  return a + (b - a) * (t - (float)iz);
+}
+
+// table value at r (Mpc/h) by linear interpolation in r (src/cosmo.c:52-86)
+__device__ __forceinline__ float table_at_r(const DevCfg &c, const float *tab, float r)
+{
+  const float tr = fminf(fmaxf(r * c.glob_idr_f, 0.f), (float)(kNZ - 2));
+  const int ir = (int)tr;
+  const float a = __ldg(&tab[ir]), b = __ldg(&tab[ir + 1]);
+  return a + (b - a) * (tr - (float)ir);
+}
+
+// Poisson count: Knuth's multiplication method below 12, else the transformed
+// rejection PTRS of Hormann (1993, Insurance: Math. Econ. 12, 39)
+__device__ int ps_poisson(uint32_t lo, uint32_t hi, uint32_t seed, float lam)
+{
+  const uint2 key = make_uint2(seed, kPsKey);
+  if (lam < 12.f) {
+    const float emu = expf(-lam);
+    float prod = 1.f;
+    int k = 0;
+#pragma unroll 1
+    for (uint32_t j = 0; j < 64; j++) {
+      const uint4 w = philox4x32_10(make_uint4(lo, hi, 0u, j), key);
+      const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        prod *= u01(ws[q]);
+        k++;
+        if (prod <= emu) return k - 1;
+      }
+    }
+    return k;
+  }
+  const double mu = lam, smu = sqrt(mu), b = 0.931 + 2.53 * smu, a = -0.059 + 0.02483 * b;
+  const double inv_alpha = 1.1239 + 1.1328 / (b - 3.4), vr = 0.9277 - 3.6224 / (b - 2);
+  const double lmu = log(mu);
+#pragma unroll 1
+  for (uint32_t j = 0; j < 256; j++) {
+    const uint4 w = philox4x32_10(make_uint4(lo, hi, 0u, j), key);
+    const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+    for (int q = 0; q < 4; q += 2) {
+      const double U = (double)u01(ws[q]) - 0.5, V = (double)u01(ws[q + 1]);
+      const double us = 0.5 - fabs(U);
+      const double kd = floor((2 * a / us + b) * U + mu + 0.43);
+      if (us >= 0.07 && V <= vr) return (int)kd;
+      if (kd < 0 || (us < 0.013 && V > us)) continue;
+      if (log(V) + log(inv_alpha) - log(a / (us * us) + b) <= -mu + kd * lmu - lgamma(kd + 1)) return (int)kd;
+    }
+  }
+  return (int)rint(mu);
+}
+
+// RING pixel of a source at (dx ix - pos_obs) + dx u, FP64 with the reference's
+// rounding (src/pixelize.c:112-121)
+__device__ __noinline__ uint32_t ps_pixel_exact(const DevCfg &c, int ix, int iy, int iz, float ux, float uy, float uz)
+{
+  const double x = __dadd_rn(__dsub_rn(__dmul_rn(c.dx, (double)ix), c.pos_obs), __dmul_rn(c.dx, (double)ux));
+  const double y = __dadd_rn(__dsub_rn(__dmul_rn(c.dx, (double)iy), c.pos_obs), __dmul_rn(c.dx, (double)uy));
+  const double z = __dadd_rn(__dsub_rn(__dmul_rn(c.dx, (double)iz), c.pos_obs), __dmul_rn(c.dx, (double)uz));
+  const double xy2 = __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y));
+  const double r = __dsqrt_rn(__dadd_rn(xy2, __dmul_rn(z, z)));
+  const double cth = __ddiv_rn(z, r);
+  const double sth = fabs(cth) > 0.99 ? __ddiv_rn(__dsqrt_rn(xy2), r) : -5.0;
+  return (uint32_t)loc2pix_exact(c.nside, cth, sth, atan2(y, x));
+}
+
+__global__ void __launch_bounds__(256) psources_kernel(DevCfg c, PsConst p, const double *__restrict__ stats,
+                                                       const float *__restrict__ dens,
+                                                       const float *__restrict__ vr, float *__restrict__ acc,
+                                                       unsigned long long *__restrict__ total, PsCatalogue cat)
+{
+  const int n = c.n;
+  const long ncell = (long)n * n * n;
+  const float sigma2 = (float)stats[1];
+  const float half_n = 0.5f * (float)n;
+  unsigned long long count = 0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < ncell; i += (long)gridDim.x * blockDim.x) {
+    const int ix = (int)(i % n), iy = (int)((i / n) % n), iz = (int)(i / ((long)n * n));
+    // Poisson mean at the cell centre (src/grid_tools.c:67-84)
+    const float xc = c.dxf * (ix + 0.5f) - c.pos_obsf, yc = c.dxf * (iy + 0.5f) - c.pos_obsf,
+                zc = c.dxf * (iz + 0.5f) - c.pos_obsf;
+    const float rc = sqrtf(xc * xc + yc * yc + zc * zc);
+    const float ndens = ps_n_of_z(p, table_at_r(c, c.z_r2z_f, rc));
+    if (!(ndens > 0.f)) continue;
+    const float gfb = table_at_r(c, c.gd_f, rc);  // bias_psources = 1 (src/psources.c:65-68)
+    const float delta = dens[i];
+    const float lam = ndens * p.cell_vol * expf(gfb * (delta - 0.5f * gfb * sigma2));
+    const int np = ps_poisson((uint32_t)i, (uint32_t)(i >> 32), c.seed, lam);
+    if (np <= 0) continue;
+    count += (unsigned long long)np;
+    const float dz = cell_hi(c, sigma2, ix, iy, iz, delta, vr[i]).dz;  // dz_rsd of the cell
+    for (int s = 0; s < np; s++) {
+      const uint4 w = philox4x32_10(make_uint4((uint32_t)i, (uint32_t)(i >> 32), 1u + (uint32_t)s, 0u),
+                                    make_uint2(c.seed, kPsKey));
+      const float ux = u01(w.x), uy = u01(w.y), uz = u01(w.z), uL = u01(w.w);
+      const float X = ((float)ix - half_n) + ux, Y = ((float)iy - half_n) + uy, Z = ((float)iz - half_n) + uz;
+      const float rho2 = fmaf(Y, Y, X * X), R2 = fmaf(Z, Z, rho2), iR = rsqrtf(R2);
+      const float r = R2 * iR * c.dxf;
+      const float zcos = table_at_r(c, c.z_r2z_f, r);
+      if (zcos >= p.z_max) continue;  // draw_luminosity returns 0 (src/psources.c:130)
+      uint32_t pix = rho2 > 0.f ? pixel_fast(c, X, Y, Z, rho2, iR) : kKeyUncertain;
+      if (pix == kKeyUncertain) pix = ps_pixel_exact(c, ix, iy, iz, ux, uy, uz);
+      const float t = uL * (float)p.nicdf;
+      const int j = min((int)t, p.nicdf - 1);
+      const float l0 = __ldg(&p.icdf[j]), l1 = __ldg(&p.icdf[j + 1]);
+      const float L = exp10f(l0 + (l1 - l0) * (t - (float)j));
+      const float opz = 1.f + zcos + dz;
+      const float wgt = L / (r * r * opz);
+      atomicAdd(&acc[pix], wgt * exp2f(-0.1f * log2f(opz)));
+      atomicAdd(&acc[c.npix + pix], 10.f * wgt * exp2f(-0.75f * log2f(opz)));
+      if (cat.count) {
+        const unsigned long long k = atomicAdd(cat.count, 1ull);
+        if (k < (unsigned long long)cat.cap) {
+          cat.cell[k] = i;
+          cat.u[k] = make_float4(ux, uy, uz, L);
+          cat.dz[k] = dz;
+          cat.pix[k] = (int)pix;
+        }
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) count += __shfl_xor_sync(0xffffffffu, count, o);
+  if ((threadIdx.x & 31) == 0 && count) atomicAdd(total, count);
+}
+
+// maps_ps[inu][pix] = a[inu] S1[pix] + b[inu] S2[pix]
+__global__ void ps_expand_kernel(DevCfg c, const float *__restrict__ acc, const float *__restrict__ chan,
+                                 float *__restrict__ maps_ps)
+{
+  const long npix = c.npix, total = npix * c.n_nu;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    const long inu = i / npix, pix = i - inu * npix;
+    maps_ps[i] = __ldg(&chan[2 * inu]) * acc[pix] + __ldg(&chan[2 * inu + 1]) * acc[npix + pix];
+  }
+}
+
+cudaError_t psources(const DevCfg &c, const PsConst &p, const double *stats, const float *dens, const float *vr,
+                     float *acc, float *maps_ps, const float *chan, unsigned long long *total, const PsCatalogue &cat,
+                     cudaStream_t st)
+{
+  cudaError_t e = cudaMemsetAsync(acc, 0, sizeof(float) * 2 * c.npix, st);
+  if (e != cudaSuccess) return e;
+  psources_kernel<<<152 * 16, 256, 0, st>>>(c, p, stats, dens, vr, acc, total, cat);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  ps_expand_kernel<<<152 * 16, 256, 0, st>>>(c, acc, chan, maps_ps);
   return cudaGetLastError();
 }
 

@@ -94,6 +94,9 @@ def lib():
         L.gethi_gpu_fallback_count.argtypes = [vp, vp]
         L.gethi_gpu_run_batch.argtypes = [vp, C.c_int, vp, vp, C.c_int, vp, C.c_int, vp]
         L.gethi_gpu_autotune.argtypes = [vp, vp, vp]
+        L.gethi_gpu_psources_maps.argtypes = [vp, vp, vp]
+        L.gethi_gpu_psources_catalogue.argtypes = [vp, C.c_long, vp, vp, vp, vp, vp]
+        L.gethi_host_psources.argtypes = [P(Params), vp, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -143,6 +146,14 @@ def host_setup(p):
     _check(lib().gethi_host_setup(C.byref(p), C.byref(d), _ptr(tables), _ptr(logk), _ptr(pk), _ptr(offs),
                                   _ptr(pref)))
     return dict(derived=d, tables=tables, logk=logk, pk=pk, offsets=offs.reshape(10, 3), prefac=pref)
+
+
+def host_psources(p):
+    """Point-source tables of the host setup: n(z), rejection bounds, glob_dz, log10 L inverse CDF."""
+    nz, mp, icdf = np.zeros(256), np.zeros(256), np.zeros(4097)
+    gdz = np.zeros(1)
+    _check(lib().gethi_host_psources(C.byref(p), _ptr(nz), _ptr(mp), _ptr(gdz), _ptr(icdf)))
+    return dict(nz=nz, maxpdf=mp, glob_dz=float(gdz[0]), icdf=icdf)
 
 
 def host_modes_mt(p, nthreads=1):
@@ -247,7 +258,27 @@ class GetHI:
         return out
 
     KERNEL_CLASSES = ("zpass", "ypass", "xpass", "xpass_vel", "nyq", "sigma", "fd_vel", "get_hi", "project",
-                      "scale", "zpass_raw", "fixup")
+                      "scale", "zpass_raw", "fixup", "psources")
+
+    # -- point sources (do_psources=1)
+    def psources_maps(self):
+        """Point-source maps [n_nu, 12 n_side^2] (mK) and the number of sources."""
+        maps = np.zeros((self.n_nu, self.npix), np.float32)
+        ns = np.zeros(1, np.int64)
+        _check(lib().gethi_gpu_psources_maps(self._ctx, _ptr(maps), _ptr(ns)))
+        return maps, int(ns[0])
+
+    def psources_catalogue(self, cap=1 << 22):
+        """The sources of the current fields: cell index, (ux, uy, uz), L0 [1e22 W/Hz], dz_rsd, pixel."""
+        cell = np.zeros(cap, np.int64)
+        ul = np.zeros((cap, 4), np.float32)
+        dz = np.zeros(cap, np.float32)
+        pix = np.zeros(cap, np.int32)
+        cnt = np.zeros(1, np.int64)
+        _check(lib().gethi_gpu_psources_catalogue(self._ctx, cap, _ptr(cell), _ptr(ul), _ptr(dz), _ptr(pix),
+                                                  _ptr(cnt)))
+        k = min(int(cnt[0]), cap)
+        return dict(cell=cell[:k], u=ul[:k, :3], L0=ul[:k, 3], dz=dz[:k], pix=pix[:k], count=int(cnt[0]))
 
     def profile(self, on=True):
         _check(lib().gethi_gpu_profile(self._ctx, int(on)))

@@ -122,6 +122,28 @@ int gethi_gpu_set_seed(gethi_ctx *ctx, unsigned int seed);
  * byte count (>= 0) or an error code. */
 long gethi_gpu_upload_inputs(gethi_ctx *ctx);
 
+/* ---- point sources (do_psources=1) ----
+ * get_point_sources (src/grid_tools.c:24-101) and mk_psources_maps
+ * (src/pixelize.c:58-148) run inside gethi_gpu_make_fields, on the Gaussian
+ * density: per cell a Poisson number of sources with mean n(z) dx^3
+ * exp(D (delta - D sigma^2/2)), each at a uniform position in its cell with a
+ * luminosity from the reference's luminosity function (src/psources.c), its
+ * temperature added to every channel of its pixel.  Draws are counter-based
+ * (Philox4x32-10), so they follow the reference's distributions, not its GSL
+ * stream.  maps_out: [n_nu][12 n_side^2] in mK (may be NULL); nsources: the
+ * number of sources of the last realisation (may be NULL). */
+int gethi_gpu_psources_maps(gethi_ctx *ctx, float *maps_out, long *nsources);
+/* The sources of the current fields (after gethi_gpu_make_fields or
+ * gethi_gpu_run, before gethi_gpu_get_hi), drawn again with the same counters:
+ * up to cap entries of cell index ix + n (iy + n iz), (ux, uy, uz, L0) (position
+ * dx (i + u) - x_obs, luminosity in 1e22 W/Hz), the cell's dz_rsd and the RING
+ * pixel; *count = the number of sources (may exceed cap). */
+int gethi_gpu_psources_catalogue(gethi_ctx *ctx, long cap, long *cell, float *u_l, float *dz, int *pix, long *count);
+/* Host side of the point sources (src/psources.c:98-124): n(z) and rejection
+ * bounds on 256 bins of z_max/256, and the inverse CDF of log10 L that replaces
+ * the rejection loop (4097 entries); any pointer may be NULL. */
+int gethi_host_psources(const gethi_params *p, double *nz_arr, double *maxpdf, double *glob_dz, double *logl_icdf);
+
 /* ---- ensembles ----
  * The reference runs one realisation per process (src/main_gh.c:24-80); an
  * ensemble is many runs of GetHI with different seed= values.  This runs a
@@ -193,7 +215,8 @@ int gethi_project_noalloc(const gethi_params *p, const gethi_derived *d, const d
 #define GETHI_KC_SCALE 9
 #define GETHI_KC_ZPASS_RAW 10 /* Z pass of a velocity field from the stored modes */
 #define GETHI_KC_FIXUP 11     /* FP64 keys of the samples the FP32 path left uncertain */
-#define GETHI_NKCLASS 12
+#define GETHI_KC_PSOURCES 12  /* point sources: Poisson draws, positions, luminosities, maps */
+#define GETHI_NKCLASS 13
 int gethi_gpu_profile(gethi_ctx *ctx, int on);
 /* accumulated ms and launch counts per class since profiling was switched on,
  * and the total number of kernels this context has launched */

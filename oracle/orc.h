@@ -134,6 +134,8 @@ long orc_poisson_small(orc_mt *r, double mu);
 double orc_temp_of_l(double hhub, double L0, double nu_obs, double z, double r, double dOmega);
 long orc_point_sources(const orc_config *c, const orc_derived *d, const double *nz_arr, double glob_dz,
                        const float *dens, double sigma2, int nthreads, int *nsources);
+void orc_ps_lambda(const orc_config *c, const orc_derived *d, const double *nz_arr, double glob_dz,
+                   const float *dens, double sigma2, double *lam);
 void orc_psources_maps(const orc_config *c, const orc_derived *d, const double *nu0, const double *nuf,
                        const double *nz_arr, const double *maxpdf, double glob_dz, const int *nsources,
                        const float *dz, int nthreads, float *maps_ps);

@@ -82,6 +82,7 @@ def lib():
         L.orc_psources_maps_catalogue.argtypes = [P(Config), P(Derived), f64p, f64p, C.c_long, i64p, f64p, f64p,
                                                   f64p, f64p, i64p]
         L.orc_n_of_z_psources.argtypes = [f64p, C.c_double, C.c_double]
+        L.orc_ps_lambda.argtypes = [P(Config), P(Derived), f64p, C.c_double, f32p, C.c_double, f64p]
         L.orc_n_of_z_psources.restype = C.c_double
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_num_threads.restype = C.c_int
@@ -175,6 +176,14 @@ class Oracle:
         if tot < 0:
             raise ValueError("a cell's Poisson mean exceeds the restated range (<= 10)")
         return ns
+
+    def ps_lambda(self, dens_padded, sigma2):
+        """Poisson mean of every cell, compact [z][y][x]."""
+        nz, _, gdz = self.setup_psources()
+        lam = np.zeros((self.n,) * 3)
+        lib().orc_ps_lambda(C.byref(self.c), C.byref(self.d), nz, gdz,
+                            np.ascontiguousarray(dens_padded, np.float32).reshape(-1), sigma2, lam.reshape(-1))
+        return lam
 
     def psources_maps(self, nsources_padded, dz_padded, nthreads=1):
         nz, mp, gdz = self.setup_psources()

@@ -167,6 +167,27 @@ long orc_point_sources(const orc_config *c, const orc_derived *d, const double *
   return bad ? -1 : total;
 }
 
+/* Poisson means of get_point_sources (grid_tools.c:67-84), 0 where n(z) <= 0; lam:
+ * compact [z][y][x] doubles, dens padded */
+void orc_ps_lambda(const orc_config *c, const orc_derived *d, const double *nz_arr, double glob_dz,
+                   const float *dens, double sigma2, double *lam)
+{
+  int n = c->n_grid, ngx = 2 * (n / 2 + 1);
+  double dx = d->l_box / n, cell_vol = dx * dx * dx;
+  for (int iz = 0; iz < n; iz++)
+    for (int iy = 0; iy < n; iy++)
+      for (int ix = 0; ix < n; ix++) {
+        double x0 = (ix + 0.5) * dx - d->pos_obs[0], y0 = (iy + 0.5) * dx - d->pos_obs[1],
+               z0 = (iz + 0.5) * dx - d->pos_obs[2];
+        double r = sqrt(x0 * x0 + y0 * y0 + z0 * z0);
+        double ndens = orc_n_of_z_psources(nz_arr, glob_dz, orc_z_of_r(d, r));
+        double gfb = orc_dgrowth_of_r(d, r);
+        long index = ix + (long)ngx * (iy + (long)n * iz);
+        lam[ix + (long)n * (iy + (long)n * iz)] =
+            ndens > 0 ? ndens * cell_vol * exp(gfb * (dens[index] - 0.5 * gfb * sigma2)) : 0.0;
+      }
+}
+
 /* mk_psources_maps (pixelize.c:58-148).  dz: dz_rsd after get_HI, padded; maps_ps
  * [n_nu][12 n_side^2], accumulated as the reference does (float += double). */
 void orc_psources_maps(const orc_config *c, const orc_derived *d, const double *nu0, const double *nuf,

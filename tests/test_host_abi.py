@@ -134,11 +134,28 @@ def test_host_mt_modes_match_reference(gh, name):
     np.testing.assert_array_equal(modes.view(np.float32).reshape(-1), g["dens_k"])
 
 
+def test_host_psources_tables_match_reference(gh):
+    g = load_case("case_ps32")
+    t = gh.host_psources(params_for_case(gh, g))
+    assert t["glob_dz"] == g["p_glob_dz"]
+    np.testing.assert_array_equal(t["nz"], g["ps_nz"])
+    np.testing.assert_array_equal(t["maxpdf"], g["ps_maxpdf"])
+    # inverse CDF of log10 L: endpoints, monotone, and its median is the density's
+    icdf = t["icdf"]
+    assert icdf[0] == -5.0 and icdf[-1] == 6.0 and np.all(np.diff(icdf) > 0)
+    x = np.linspace(-5, 6, 400001)
+    L = 10 ** x
+    f = (L / 2.11) ** 0.367 * np.exp(-L / 2.11)
+    cdf = np.concatenate([[0], np.cumsum(0.5 * (f[1:] + f[:-1]))])
+    cdf /= cdf[-1]
+    for q in (0.1, 0.5, 0.9):
+        assert abs(np.interp(q, cdf, x) - np.interp(q * 4096, np.arange(4097), icdf)) < 2e-3
+
+
 def test_setup_rejects_bad_configs(gh):
     with pytest.raises(gh.GetHIError):
         gh.host_setup(gh.make_params(n_grid=33, pk_filename="EH", frequencies_filename=""))
-    with pytest.raises(gh.GetHIError):
-        gh.host_setup(gh.make_params(do_psources=1, pk_filename="EH", frequencies_filename=""))
+    gh.host_setup(gh.make_params(do_psources=1, pk_filename="EH", frequencies_filename=""))  # point sources: built
     with pytest.raises(gh.GetHIError) as e:  # Gaussianised draws are Philox draws
         gh.host_setup(gh.make_params(gaussianise=1, rng="mt_validation", pk_filename="EH", frequencies_filename=""))
     assert e.value.code == -1
