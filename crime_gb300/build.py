@@ -16,7 +16,7 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU = ["fft.cu", "tcfft.cu", "stages.cu", "api.cu", "noalloc.cu"]
 CXX = ["host.cpp"]
-HDRS = ["common.cuh", "fft.h", "host.h", "modes.cuh", "tc.cuh", os.path.join("..", "..", "include", "gethi_gpu.h")]
+HDRS = ["common.cuh", "fft.h", "host.h", "modes.cuh", "tc.cuh", "dfloat.cuh", os.path.join("..", "..", "include", "gethi_gpu.h")]
 
 
 def _newer(target, deps):

@@ -60,6 +60,7 @@ struct gethi_ctx {
   float *ps_acc = nullptr, *maps_ps = nullptr, *ps_nz = nullptr, *ps_icdf = nullptr, *ps_chan = nullptr;
   unsigned long long *ps_total = nullptr;
   PsConst psc{};
+  float2 *tab_df = nullptr, *edges_df = nullptr;  // double-float tables for the key refinement
   uint4 *tc_bmat = nullptr;                // fft_precision=tc_split tables and error flag
   float2 *tc_tw = nullptr;
   int *tc_err = nullptr;
@@ -160,6 +161,22 @@ void fill_cfg(gethi_ctx *c)
   g.tc_bmat = c->tc_bmat;
   g.tc_tw = c->tc_tw;
   g.tc_err = c->tc_err;
+  if (c->tab_df) {
+    auto split = [](double v) { const float h = (float)v; return make_float2(h, (float)(v - (double)h)); };
+    g.z_r2z_df = c->tab_df;
+    g.r_r2z_df = c->tab_df + NZ;
+    g.nu_edges_df = c->edges_df;
+    g.dx_df = split(g.dx);
+    g.pos_obs_df = split(g.pos_obs);
+    g.glob_idr_df = split(g.glob_idr);
+    g.inv_dnu_df = split(g.inv_dnu);
+    g.nu_min_df = split(g.nu_min);
+    for (int i = 0; i < NSUB; i++) {
+      g.xs_df[i] = split(g.xs[i]);
+      g.ys_df[i] = split(g.ys[i]);
+      g.zs_df[i] = split(g.zs[i]);
+    }
+  }
 }
 
 ColGeom geom(float2 *base, long cpp, long pstride, long cstride, long estride, long ncols)
@@ -419,6 +436,23 @@ extern "C" int gethi_gpu_init(const gethi_params *p, int device, gethi_ctx **out
     gethi_gpu_free(c);
     return rc;
   }
+  {  // double-float copies of the FP64 tables the key refinement reads
+    if ((rc = dalloc(&c->tab_df, (size_t)2 * NZ)) || (rc = dalloc(&c->edges_df, (size_t)s.p.n_nu + 1))) {
+      gethi_gpu_free(c);
+      return rc;
+    }
+    auto split = [](double v) { const float h = (float)v; return make_float2(h, (float)(v - (double)h)); };
+    std::vector<float2> t2(2 * NZ);
+    for (int i = 0; i < NZ; i++) {
+      t2[i] = split(s.z_r2z[i]);
+      t2[NZ + i] = split(s.r_r2z[i]);
+    }
+    cudaMemcpy(c->tab_df, t2.data(), sizeof(float2) * t2.size(), cudaMemcpyHostToDevice);
+    std::vector<float2> e2(s.p.n_nu + 1);
+    for (int i = 0; i < s.p.n_nu; i++) e2[i] = split(s.nu0[i]);
+    e2[s.p.n_nu] = split(s.nuf[s.p.n_nu - 1]);
+    cudaMemcpy(c->edges_df, e2.data(), sizeof(float2) * e2.size(), cudaMemcpyHostToDevice);
+  }
   if (s.p.do_psources) {
     const int ni = PS_NICDF;
     if ((rc = dalloc(&c->ps_acc, (size_t)2 * npix)) || (rc = dalloc(&c->maps_ps, (size_t)npix * s.p.n_nu)) ||
@@ -515,7 +549,7 @@ extern "C" void gethi_gpu_free(gethi_ctx *c)
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   void *bufs[] = {c->main, c->nyq, c->bA, c->bAn, c->bB, c->bBn, c->bC, c->bCn, c->modes, c->vr, c->pg, c->pgn,
-                  c->tc_bmat, c->tc_tw, c->tc_err, c->ps_acc, c->maps_ps, c->ps_nz, c->ps_icdf, c->ps_chan,
+                  c->tc_bmat, c->tc_tw, c->tc_err, c->tab_df, c->edges_df, c->ps_acc, c->maps_ps, c->ps_nz, c->ps_icdf, c->ps_chan,
                   c->ps_total, c->maps, c->twN, c->twM, c->partials,
                   c->stats, c->pk_f, c->logk_f, c->tab_f, c->tab_d, c->prefac, c->edges_f, c->edges_d, c->counters};
   for (void *b : bufs)

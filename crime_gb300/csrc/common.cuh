@@ -290,6 +290,11 @@ struct DevCfg {
   // projection tile along z / 4, and the half-width column tile of the FP32 passes
   int proj_zsteps;
   int col_variant;
+  // double-float (hi, lo) copies for the refinement of uncertain keys
+  // (z_r2z_df == nullptr: uncertain keys go straight to FP64)
+  const float2 *z_r2z_df, *r_r2z_df, *nu_edges_df;
+  float2 dx_df, pos_obs_df, glob_idr_df, inv_dnu_df, nu_min_df;
+  float2 xs_df[10], ys_df[10], zs_df[10];
 };
 
 // wave number of grid index i (src/fourier.c:264-283): Nyquist is +n/2

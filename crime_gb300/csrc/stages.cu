@@ -4,6 +4,7 @@
 #include <cstdio>
 
 #include "common.cuh"
+#include "dfloat.cuh"
 #include "fft.h"
 
 namespace gethi {
@@ -156,6 +157,116 @@ __device__ __noinline__ uint32_t key_exact(const DevCfg &c, int ix, int iy, int 
   double sth = fabs(cth) > 0.99 ? __ddiv_rn(__dsqrt_rn(xy2), r) : -5.0;
   long ipix = loc2pix_exact(c.nside, cth, sth, atan2(y, x));
   return (uint32_t)ipix + (uint32_t)c.npix * (uint32_t)inu;
+}
+
+// ---------------------------------------------------------------------------
+// Refinement of a key the FP32 path left uncertain, in double-float arithmetic
+// (about 48 bits; dfloat.cuh).  The operation sequence is key_exact's, the
+// angle comes from a double-float atan2, and every floor and comparison must
+// clear a margin of 1e-9 of its operands' scale, far above the errors of both
+// this arithmetic (< 1e-12) and the FP64 reference (< 1e-15), so a certain
+// result is the FP64 key.  unc = true hands the sample to key_exact.
+// ---------------------------------------------------------------------------
+__device__ __noinline__ uint32_t key_refine(const DevCfg &c, int ix, int iy, int iz, int is, float dzf, bool &unc)
+{
+  unc = false;
+  constexpr float kM = 1e-9f;
+  const df dx = df_of(c.dx_df), po = df_of(c.pos_obs_df);
+  const df x = df_add(df_sub(df_mul_f(dx, (float)ix + 0.5f), po), df_of(c.xs_df[is]));
+  const df y = df_add(df_sub(df_mul_f(dx, (float)iy + 0.5f), po), df_of(c.ys_df[is]));
+  const df z = df_add(df_sub(df_mul_f(dx, (float)iz + 0.5f), po), df_of(c.zs_df[is]));
+  const df xy2 = df_add(df_mul(x, x), df_mul(y, y));
+  const df r2 = df_add(xy2, df_mul(z, z));
+  if (!(r2.hi > 0.f) || !(xy2.hi > 0.f)) {
+    unc = true;
+    return 0;
+  }
+  const df r = df_sqrt(r2);
+  // z(r), src/cosmo.c:52-62 (piecewise linear: continuous, so the segment index needs no margin)
+  df red;
+  if (r.hi >= c.r_tab_max_f) {
+    red = df_of(c.z_r2z_df[kNZ - 1]);
+  } else {
+    const df tr = df_mul(r, df_of(c.glob_idr_df));
+    const int ir = min(max((int)floorf(tr.hi), 0), kNZ - 2);
+    const df z0 = df_of(c.z_r2z_df[ir]), z1 = df_of(c.z_r2z_df[ir + 1]), r0 = df_of(c.r_r2z_df[ir]);
+    red = df_add(z0, df_mul(df_mul(df_sub(z1, z0), df_sub(r, r0)), df_of(c.glob_idr_df)));
+  }
+  red = df_add(red, df_f(dzf));
+  constexpr df kNu21 = df_const(1420.40575177);
+  const df nu = df_div(kNu21, df_add(df_f(1.f), red));
+  int inu;
+  if (c.regular_nu) {  // (int) truncation, src/pixelize.c:369
+    const df t = df_mul(df_of(c.inv_dnu_df), df_sub(nu, df_of(c.nu_min_df)));
+    const float m = kM * (fabsf(t.hi) + fabsf(c.inv_dnu_df.x * nu.hi) + 1.f);
+    const int f = df_floor(t, m, unc);
+    inu = (t.hi < 0.f) ? f + 1 : f;
+  } else {  // the bin nu0 <= nu < nuf of the contiguous table (src/pixelize.c:28-56)
+    const int nn = c.n_nu;
+    int lo = -1, hi = nn + 1;  // e[lo] <= nu < e[hi] over edges 0..nn, with -1 / nn+1 as sentinels
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (df_ge(nu, df_of(c.nu_edges_df[mid]))) lo = mid;
+      else hi = mid;
+    }
+    const float m = kM * nu.hi;
+    if (lo >= 0 && fabsf(df_sub(nu, df_of(c.nu_edges_df[lo])).hi) < m) unc = true;
+    if (hi <= nn && fabsf(df_sub(nu, df_of(c.nu_edges_df[hi])).hi) < m) unc = true;
+    inu = lo < 0 ? -1 : (lo >= nn ? nn : lo);
+  }
+  if (unc) return 0;
+  if (inu < 0 || inu >= c.n_nu) return 0xFFFFFFFFu;  // outside the shells
+  // pixel (loc2pix_exact)
+  const long nside = c.nside;
+  const float dn = (float)nside;
+  const df cth = df_div(z, r);
+  const df za = df_abs(cth);
+  constexpr df kTwoThirds = df_const(2.0 / 3.0), kInvHalfPi = df_const(0.63661977236758134308);
+  if (fabsf(df_sub(za, kTwoThirds).hi) < kM) {
+    unc = true;
+    return 0;
+  }
+  df tt = df_mul(df_atan2(y, x), kInvHalfPi);
+  if (tt.hi < 0.f) tt = df_add(tt, df_f(4.f));
+  const float m = kM * (5.f * dn + 1.f);
+  long pix;
+  if (df_ge(kTwoThirds, za)) {
+    const df t1 = df_mul_f(df_add(df_f(0.5f), tt), dn);
+    const df t2 = df_mul_f(df_mul_f(cth, dn), 0.75f);
+    const long jp = df_floor(df_sub(t1, t2), m, unc), jm = df_floor(df_add(t1, t2), m, unc);
+    const long ir = nside + 1 + jp - jm;
+    const long kshift = 1 - (ir & 1);
+    long ip = (jp + jm - nside + kshift + 1) / 2;
+    ip %= 4 * nside;
+    if (ip < 0) ip += 4 * nside;
+    pix = 2 * nside * (nside - 1) + (ir - 1) * 4 * nside + ip;
+  } else {
+    const int ftt = df_floor(tt, 5.f * kM, unc);
+    const df tp = df_sub(tt, df_f((float)ftt));
+    const df sth = df_div(df_sqrt(xy2), r);
+    const df tmp = df_div(df_mul_f(sth, dn), df_sqrt(df_mul(df_add(df_f(1.f), za), df_const(1.0 / 3.0))));
+    const float mt = kM * (tmp.hi + 1.f);
+    const long jp = df_floor(df_mul(tp, tmp), mt, unc);
+    const long jm = df_floor(df_mul(df_sub(df_f(1.f), tp), tmp), mt, unc);
+    const long ir = jp + jm + 1;
+    long ip = df_floor(df_mul_f(tt, (float)ir), kM * (4.f * (float)ir + 1.f), unc);
+    ip %= 4 * ir;
+    if (ip < 0) ip += 4 * ir;
+    pix = (cth.hi > 0.f) ? 2 * ir * (ir - 1) + ip : 12 * nside * nside - 2 * ir * (ir + 1) + ip;
+  }
+  if (unc) return 0;
+  return (uint32_t)pix + (uint32_t)c.npix * (uint32_t)inu;
+}
+
+// the key of an uncertain sample: double-float refinement, FP64 when that is not decisive
+__device__ __forceinline__ uint32_t key_resolve(const DevCfg &c, int ix, int iy, int iz, int is, float dzf)
+{
+  if (c.z_r2z_df) {
+    bool unc;
+    const uint32_t k = key_refine(c, ix, iy, iz, is, dzf, unc);
+    if (!unc) return k;
+  }
+  return key_exact(c, ix, iy, iz, is, dzf);
 }
 
 // ---------------------------------------------------------------------------
@@ -424,7 +535,7 @@ __global__ void __launch_bounds__(kProjThreads) project_kernel(DevCfg c, FastCon
           q_val[slot] = msub;
           q_dz[slot] = dz;
         } else {
-          const uint32_t ke = key_exact(c, ix, iy, iz, is, dz);
+          const uint32_t ke = key_exact(c, ix, iy, iz, is, dz);  // tile queue full (rare)
           if (ke != 0xFFFFFFFFu) tile_add(hkey, hval, maps, ke, msub);
         }
       } else if (key != kKeyInvalid) {
@@ -459,7 +570,7 @@ __global__ void __launch_bounds__(kProjThreads) project_kernel(DevCfg c, FastCon
     }
     const int lc = (int)q_cell[j], k = lc / kProjThreads, t = lc % kProjThreads;
     const int ix = bx * kTile + (t & 7), iy = by * kTile + ((t >> 3) & 7), iz = bz * 4 * zsteps + (t >> 6) + 4 * k;
-    const uint32_t key = key_exact(c, ix, iy, iz, q_sub[j], q_dz[j]);
+    const uint32_t key = key_exact(c, ix, iy, iz, q_sub[j], q_dz[j]);  // global queue full (rare)
     if (key != 0xFFFFFFFFu) tile_add(hkey, hval, maps, key, q_val[j]);
   }
   __syncthreads();
@@ -482,7 +593,7 @@ __global__ void fixup_kernel(DevCfg c, const FallbackEntry *__restrict__ fq, con
     const int bx = e.tile % nt, by = (e.tile / nt) % nt, bz = e.tile / (nt * nt);
     const int lc = (int)(e.sub >> 4), is = (int)(e.sub & 15), k = lc / kProjThreads, t = lc % kProjThreads;
     const int ix = bx * kTile + (t & 7), iy = by * kTile + ((t >> 3) & 7), iz = bz * 4 * zsteps + (t >> 6) + 4 * k;
-    const uint32_t key = key_exact(c, ix, iy, iz, is, e.dz);
+    const uint32_t key = key_resolve(c, ix, iy, iz, is, e.dz);
     if (key != 0xFFFFFFFFu) atomicAdd(&maps[key], e.msub);
   }
 }
@@ -514,7 +625,7 @@ __global__ void sample_keys_kernel(DevCfg c, FastConst f, const float *__restric
       uint32_t key = kKeyUncertain;
       if (!exact) key = key_fast(c, f, c.nu_edges_f, log2nn, Xc + f.xsp[is], Yc + f.ysp[is], Zc + f.zsp[is], dz);
       if (key == kKeyUncertain) {
-        key = key_exact(c, ix, iy, iz, is, dz);
+        key = exact ? key_exact(c, ix, iy, iz, is, dz) : key_resolve(c, ix, iy, iz, is, dz);
         nfall++;
       }
       keys[i * kNSUB + is] = key;
