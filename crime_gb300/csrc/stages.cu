@@ -3,6 +3,8 @@
 // onto (HEALPix pixel, frequency shell) maps.
 #include <cstdio>
 
+#include <cmath>
+
 #include "common.cuh"
 #include "dfloat.cuh"
 #include "fft.h"
@@ -288,6 +290,11 @@ struct FastConst {
   float idr_cell;                             // glob_idr * dx
   float half_n;                               // n/2
   float nu_min, inv_dnu;                      // regular table
+  // the projection visits the sub-samples along a short path through the cell
+  // (consecutive samples then share a key more often, so a cell's runs of equal
+  // keys are longer): tour[j] is the j-th sample's index, txsp.. its offsets
+  int tour[kNSUB];
+  float txsp[kNSUB], tysp[kNSUB], tzsp[kNSUB];
 };
 
 __device__ __forceinline__ bool near_int(float u, float m) { return fabsf(u - rintf(u)) < m; }
@@ -524,9 +531,10 @@ __global__ void __launch_bounds__(kProjThreads) project_kernel(DevCfg c, FastCon
     uint32_t cur = 0xFFFFFFFFu;
     float acc = 0.f;
 #pragma unroll kProjUnroll
-    for (int is = 0; is < kNSUB; is++) {
-      const uint32_t key = key_fast(c, f, ef, log2nn, Xc + f.xsp[is], Yc + f.ysp[is], Zc + f.zsp[is], dz);
+    for (int j = 0; j < kNSUB; j++) {
+      const uint32_t key = key_fast(c, f, ef, log2nn, Xc + f.txsp[j], Yc + f.tysp[j], Zc + f.tzsp[j], dz);
       if (key == kKeyUncertain) {
+        const int is = f.tour[j];
         nfall++;
         const int slot = atomicAdd(&q_n, 1);
         if (slot < kQueueCap) {
@@ -667,6 +675,52 @@ static FastConst fast_const(const DevCfg &c)
   f.half_n = (float)(c.n / 2);
   f.nu_min = (float)c.nu_min;
   f.inv_dnu = (float)c.inv_dnu;
+  // shortest open path through the 10 offsets: nearest-neighbour tours from every
+  // start, each improved by 2-opt reversals, the shortest kept
+  auto dist = [&](int a, int b) {
+    const double dx = c.xs[a] - c.xs[b], dy = c.ys[a] - c.ys[b], dz = c.zs[a] - c.zs[b];
+    return std::sqrt(dx * dx + dy * dy + dz * dz);
+  };
+  auto length = [&](const int *o) {
+    double l = 0;
+    for (int i = 0; i + 1 < kNSUB; i++) l += dist(o[i], o[i + 1]);
+    return l;
+  };
+  double best = 1e300;
+  for (int start = 0; start < kNSUB; start++) {
+    int o[kNSUB];
+    bool used[kNSUB] = {};
+    o[0] = start;
+    used[start] = true;
+    for (int i = 1; i < kNSUB; i++) {
+      int nx = -1;
+      for (int j = 0; j < kNSUB; j++)
+        if (!used[j] && (nx < 0 || dist(o[i - 1], j) < dist(o[i - 1], nx))) nx = j;
+      o[i] = nx;
+      used[nx] = true;
+    }
+    for (bool improved = true; improved;) {
+      improved = false;
+      for (int i = 1; i + 1 < kNSUB; i++)
+        for (int j = i + 1; j < kNSUB; j++) {
+          int t[kNSUB];
+          for (int k = 0; k < kNSUB; k++) t[k] = (k >= i && k <= j) ? o[i + j - k] : o[k];
+          if (length(t) < length(o) - 1e-12) {
+            for (int k = 0; k < kNSUB; k++) o[k] = t[k];
+            improved = true;
+          }
+        }
+    }
+    if (length(o) < best) {
+      best = length(o);
+      for (int k = 0; k < kNSUB; k++) f.tour[k] = o[k];
+    }
+  }
+  for (int k = 0; k < kNSUB; k++) {
+    f.txsp[k] = f.xsp[f.tour[k]];
+    f.tysp[k] = f.ysp[f.tour[k]];
+    f.tzsp[k] = f.zsp[f.tour[k]];
+  }
   return f;
 }
 
