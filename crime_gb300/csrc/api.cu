@@ -61,6 +61,12 @@ struct gethi_ctx {
   unsigned long long *ps_total = nullptr;
   PsConst psc{};
   float2 *tab_df = nullptr, *edges_df = nullptr;  // double-float tables for the key refinement
+  // pipelined realisations (gethi_gpu_run_async): two device map buffers, a copy stream, events
+  float *maps_b[2] = {nullptr, nullptr};
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_done[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
+  bool copied_pending[2] = {false, false};
+  int cur_buf = 0;
   uint4 *tc_bmat = nullptr;                // fft_precision=tc_split tables and error flag
   float2 *tc_tw = nullptr;
   int *tc_err = nullptr;
@@ -548,8 +554,16 @@ extern "C" void gethi_gpu_free(gethi_ctx *c)
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->copy_stream) {
+    cudaStreamSynchronize(c->copy_stream);
+    cudaStreamDestroy(c->copy_stream);
+  }
+  for (int b = 0; b < 2; b++) {
+    if (c->ev_done[b]) cudaEventDestroy(c->ev_done[b]);
+    if (c->ev_copied[b]) cudaEventDestroy(c->ev_copied[b]);
+  }
   void *bufs[] = {c->main, c->nyq, c->bA, c->bAn, c->bB, c->bBn, c->bC, c->bCn, c->modes, c->vr, c->pg, c->pgn,
-                  c->tc_bmat, c->tc_tw, c->tc_err, c->tab_df, c->edges_df, c->ps_acc, c->maps_ps, c->ps_nz, c->ps_icdf, c->ps_chan,
+                  c->tc_bmat, c->tc_tw, c->tc_err, c->tab_df, c->edges_df, c->maps_b[1], c->ps_acc, c->maps_ps, c->ps_nz, c->ps_icdf, c->ps_chan,
                   c->ps_total, c->maps, c->twN, c->twM, c->partials,
                   c->stats, c->pk_f, c->logk_f, c->tab_f, c->tab_d, c->prefac, c->edges_f, c->edges_d, c->counters};
   for (void *b : bufs)
@@ -884,6 +898,59 @@ extern "C" int gethi_gpu_run_batch(gethi_ctx *const *ctxs, int nctx, const int *
   unregister();
   for (int k = 0; k < nctx; k++) ctxs[k]->stage = 3;
   return rc;
+}
+
+// Pipelined realisations: the maps of realisation i go to the host on a copy
+// stream while realisation i+1 computes into the other device buffer.
+extern "C" int gethi_gpu_run_async(gethi_ctx *c, float *maps_out)
+{
+  if (!c) return GETHI_E_ARG;
+  if (c->s.p.rng != 0) {
+    set_error("run_async: needs rng=philox");
+    return GETHI_E_ARG;
+  }
+  CK(cudaSetDevice(c->device));
+  if (!c->copy_stream) {
+    int rc = prepare(c);
+    if (rc) return rc;
+    const size_t nm = 12 * (size_t)c->s.p.n_side * c->s.p.n_side * c->s.p.n_nu;
+    c->maps_b[0] = c->maps;
+    if ((rc = dalloc(&c->maps_b[1], nm))) return rc;
+    CK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    for (int b = 0; b < 2; b++) {
+      CK(cudaEventCreateWithFlags(&c->ev_done[b], cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&c->ev_copied[b], cudaEventDisableTiming));
+    }
+  }
+  const int b = c->cur_buf;
+  const size_t bytes = sizeof(float) * 12 * (size_t)c->s.p.n_side * c->s.p.n_side * c->s.p.n_nu;
+  if (c->copied_pending[b]) CK(cudaStreamWaitEvent(c->stream, c->ev_copied[b], 0));  // buffer b is free again
+  float *const keep = c->maps;
+  c->maps = c->maps_b[b];
+  int rc = enqueue_realisation(c, c->cfg.seed, nullptr, c->stream);
+  if (!rc && c->s.p.do_psources) rc = enqueue_psources(c, c->stream, nullptr);
+  c->maps = keep;
+  if (rc) return rc;
+  CK(cudaEventRecord(c->ev_done[b], c->stream));
+  if (maps_out) {
+    CK(cudaStreamWaitEvent(c->copy_stream, c->ev_done[b], 0));
+    CK(cudaMemcpyAsync(maps_out, c->maps_b[b], bytes, cudaMemcpyDefault, c->copy_stream));
+    CK(cudaEventRecord(c->ev_copied[b], c->copy_stream));
+    c->copied_pending[b] = true;
+  }
+  c->cur_buf ^= 1;
+  c->stage = 3;
+  return GETHI_OK;
+}
+
+extern "C" int gethi_gpu_wait(gethi_ctx *c)
+{
+  if (!c) return GETHI_E_ARG;
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  if (c->copy_stream) CK(cudaStreamSynchronize(c->copy_stream));
+  c->copied_pending[0] = c->copied_pending[1] = false;
+  return check_tc(c);
 }
 
 // Launch-shape autotuner: times each candidate (projection tile depth, column

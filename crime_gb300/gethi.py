@@ -94,6 +94,8 @@ def lib():
         L.gethi_gpu_fallback_count.argtypes = [vp, vp]
         L.gethi_gpu_run_batch.argtypes = [vp, C.c_int, vp, vp, C.c_int, vp, C.c_int, vp]
         L.gethi_gpu_autotune.argtypes = [vp, vp, vp]
+        L.gethi_gpu_run_async.argtypes = [vp, vp]
+        L.gethi_gpu_wait.argtypes = [vp]
         L.gethi_gpu_psources_maps.argtypes = [vp, vp, vp]
         L.gethi_gpu_psources_catalogue.argtypes = [vp, C.c_long, vp, vp, vp, vp, vp]
         L.gethi_host_psources.argtypes = [P(Params), vp, vp, vp, vp]
@@ -227,6 +229,14 @@ class GetHI:
         if r < 0:
             _check(int(r))
         return int(r)
+
+    def run_async(self, maps_ptr=None):
+        """Enqueue a realisation and the copy of its maps to maps_ptr (an address of
+        page-locked host or device memory); returns at once (see gethi_gpu_run_async)."""
+        _check(lib().gethi_gpu_run_async(self._ctx, C.c_void_p(maps_ptr) if maps_ptr else None))
+
+    def wait(self):
+        _check(lib().gethi_gpu_wait(self._ctx))
 
     def run_into(self, maps_ptr):
         """All stages into an existing host buffer given as an address (pinned memory)."""

@@ -115,6 +115,16 @@ int gethi_gpu_make_maps(gethi_ctx *ctx, float *maps_out);
 int gethi_gpu_write_maps(const gethi_ctx *ctx, const float *maps);
 /* All stages; get_HI is fused into the projection (no separate HBM pass). */
 int gethi_gpu_run(gethi_ctx *ctx, float *maps_out);
+/* Pipelined form of gethi_gpu_run (no counterpart in the reference): enqueues
+ * one realisation and the copy of its maps to maps_out (page-locked host or
+ * device memory; NULL: no copy) and returns without waiting.  Consecutive calls
+ * alternate between two device map buffers, and the copies run on a second
+ * stream, so a realisation computes while the previous one's maps travel.
+ * maps_out must stay valid, and must not be reused, until the call after next
+ * or gethi_gpu_wait.  The point-source maps stay on the device. */
+int gethi_gpu_run_async(gethi_ctx *ctx, float *maps_out);
+/* Waits for every realisation and copy enqueued by gethi_gpu_run_async. */
+int gethi_gpu_wait(gethi_ctx *ctx);
 /* Seed of the next realisation (src/io_gh.c:246, seed=). */
 int gethi_gpu_set_seed(gethi_ctx *ctx, unsigned int seed);
 /* Copy the realisation's host inputs (P(k), distance/growth tables, shell

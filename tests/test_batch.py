@@ -55,3 +55,35 @@ def test_autotune_keeps_results(gh):  # noqa: F811
     # pixel or shell edge may move
     assert _rel(got, ref) < 1e-3
     ctx.free()
+
+
+@pytest.mark.gpu
+def test_run_async_pipeline_matches_run(gh):  # noqa: F811
+    """Pipelined realisations (two device map buffers, copies on a second stream)
+    give the maps of the same seeds run one at a time."""
+    import torch
+    ctx = gh.GetHI(params_for_case(gh, load_case("case_irr32"), velocity_mode="spectral"))
+    shape = (ctx.n_nu, ctx.npix)
+    outs = [torch.zeros(shape, dtype=torch.float32).pin_memory() for _ in range(2)]
+    dev = torch.zeros(shape, dtype=torch.float32, device="cuda")
+    seeds = [31, 32, 33, 34]
+    got = {}
+    for i, s in enumerate(seeds):
+        ctx.set_seed(s)
+        if i == 3:
+            ctx.run_async(dev.data_ptr())  # device destination
+        else:
+            if i == 2:
+                ctx.wait()  # buffer 0 is reused: collect the first result
+                got[seeds[0]] = outs[0].numpy().copy()
+            ctx.run_async(outs[i % 2].data_ptr())
+    ctx.wait()
+    got[seeds[1]] = outs[1].numpy().copy()
+    got[seeds[2]] = outs[0].numpy().copy()
+    got[seeds[3]] = dev.cpu().numpy()
+    for s in seeds:
+        ctx.set_seed(s)
+        ref = ctx.run()
+        assert np.abs(ref).max() > 0
+        assert _rel(got[s], ref) < 1e-6
+    ctx.free()
