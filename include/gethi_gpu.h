@@ -120,8 +120,10 @@ int gethi_gpu_run(gethi_ctx *ctx, float *maps_out);
  * device memory; NULL: no copy) and returns without waiting.  Consecutive calls
  * alternate between two device map buffers, and the copies run on a second
  * stream, so a realisation computes while the previous one's maps travel.
- * maps_out must stay valid, and must not be reused, until the call after next
- * or gethi_gpu_wait.  The point-source maps stay on the device. */
+ * maps_out must stay valid until gethi_gpu_wait, and the host may read it
+ * only after that; it may be passed again as the destination of the call after
+ * next (the GPU orders the two copies).  The point-source maps stay on the
+ * device. */
 int gethi_gpu_run_async(gethi_ctx *ctx, float *maps_out);
 /* Waits for every realisation and copy enqueued by gethi_gpu_run_async. */
 int gethi_gpu_wait(gethi_ctx *ctx);
