@@ -53,6 +53,27 @@ def params_for(cfg, seed_offset=0):
                           nu_max=NU21 / (1 + zmin), **COSMO, **c)
 
 
+def replica_seed(base, rank, step, stride=7919):
+    """Seed of realisation `step` on rank `rank` (replicas: every rank runs its own
+    realisations; distinct for ranks < stride)."""
+    return base + rank + stride * step
+
+
+def max_over_ranks(x, ws, device="cuda"):
+    """The slowest rank's value (replicas finish when the last one does)."""
+    if ws == 1:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_step, steps, ws, ms):
+    """Units processed by all ranks over the slowest rank's time (per second)."""
+    return units_per_step * steps * ws / (ms / 1e3)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -247,6 +268,8 @@ def bench_ensemble(args):
     import crime_gb300 as gh
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
+    if ws > 1:
+        torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
     E = ENSEMBLE
     ctxs, jobs, tuned, filled = [], [], {}, {}
     seed = E["seed"] + 1000 * rank
@@ -273,12 +296,14 @@ def bench_ensemble(args):
         for _ in range(args.steps):
             _, stats = gh.run_batch(ctxs, jobs, download=False, graph=True)
             dev_ms.append(stats["device_ms"])
-    ms = sum(dev_ms)
+    ms = max_over_ranks(sum(dev_ms), ws)
     # end to end: capture + instantiate + run + maps to the host, wall clock
+    if ws > 1:
+        torch.distributed.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         maps, st_e2e = gh.run_batch(ctxs, jobs, download=True, graph=True)
-    e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(time.perf_counter() - t0, ws)
     assert all(np.isfinite(m).all() for m in maps)
     d2h = int(sum(4 * m.size for m in maps))
     # the same batch without the graph, and one realisation at a time through gethi_gpu_run
@@ -293,10 +318,10 @@ def bench_ensemble(args):
     line = {
         "metric": "GetHI batched ensemble throughput (voxels/s): %s" % " + ".join(
             "%dx%d^3" % (cnt, n) for n, _, cnt, _ in E["members"]),
-        "value": voxels * args.steps / (ms / 1e3), "unit": "voxels/s", "n_gpus": ws, "steps": args.steps,
+        "value": whole_job_rate(voxels, args.steps, ws, ms), "unit": "voxels/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32", "data": "synthetic (Philox modes from an EH no-wiggle P(k))",
-        "realisations_per_s": len(jobs) * args.steps / (ms / 1e3),
+        "realisations_per_s": whole_job_rate(len(jobs), args.steps, ws, ms),
         "config": {"workload": "c3: " + ", ".join("%d x %d^3 (box %g Mpc/h, %d lanes)" % (cnt, n, box, ln)
                                                   for n, box, cnt, ln in E["members"]) +
                    "; seeds %d-%d; Nside %d x %d shells, z %.1f-%.1f; spectral RSD; Gaussianised P(k)" % (
@@ -306,7 +331,8 @@ def bench_ensemble(args):
                    "filled_fraction": {str(n): f for n, f in filled.items()},
                    "l2": "the batch's working set (%.1f GB of fields) exceeds L2" % (
                        sum(6 * 4 * float(n) ** 3 * ln for n, _, _, ln in E["members"]) / 1e9)},
-        "e2e": {"value": voxels * args.steps / e2e_s, "unit": "voxels/s", "h2d_bytes_per_step": 0,
+        "e2e": {"value": whole_job_rate(voxels, args.steps, ws, 1e3 * e2e_s), "unit": "voxels/s",
+                "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": d2h, "includes": "graph capture + instantiate (%.1f ms) + run + maps to "
                                                       "host" % st_e2e["capture_ms"]},
         "gpu_launches": stats["kernel_launches"] * args.steps,
@@ -319,6 +345,8 @@ def bench_ensemble(args):
         print(json.dumps(line), flush=True)
     for c in ctxs:
         c.free()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
 
 
 def bench_ours(args):
@@ -344,16 +372,9 @@ def bench_ours(args):
         if ws > 1:
             torch.distributed.barrier()
 
-    def max_over_ranks(x):
-        if ws == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
-
     # ---- device-resident throughput
     for i in range(args.warmup):
-        ctx.set_seed(cfg["seed"] + rank + 1000 * (i + 1))
+        ctx.set_seed(replica_seed(cfg["seed"], rank, i + 1, stride=1000))
         ctx.run_into(0)
     barrier()
     ctx.profile(True)
@@ -364,12 +385,12 @@ def bench_ours(args):
         start.record(stream)
         t0 = time.perf_counter()
         for i in range(args.steps):
-            ctx.set_seed(cfg["seed"] + rank + 7919 * i)
+            ctx.set_seed(replica_seed(cfg["seed"], rank, i))
             ctx.run_into(0)
         end.record(stream)
         barrier()
         wall = time.perf_counter() - t0
-    ms = max_over_ranks(start.elapsed_time(end))
+    ms = max_over_ranks(start.elapsed_time(end), ws)
     ktimes, launches1 = ctx.kernel_times()
     ctx.profile(False)
     fallbacks = ctx.fallback_count()
@@ -384,17 +405,17 @@ def bench_ours(args):
     barrier()
     t0 = time.perf_counter()
     for i in range(args.steps):
-        ctx.set_seed(cfg["seed"] + rank + 104729 * (i + 1))
+        ctx.set_seed(replica_seed(cfg["seed"], rank, i + 1, stride=104729))
         h2d = ctx.upload_inputs()
         ctx.run_async(maps_host[i % 2].data_ptr())
     ctx.wait()
-    e2e_ms = max_over_ranks(1e3 * (time.perf_counter() - t0))
+    e2e_ms = max_over_ranks(1e3 * (time.perf_counter() - t0), ws)
     barrier()
     assert all(np.isfinite(m.numpy()).all() for m in maps_host)
 
     voxels = float(n) ** 3
-    value = voxels * args.steps * ws / (ms / 1e3)
-    e2e = voxels * args.steps * ws / (e2e_ms / 1e3)
+    value = whole_job_rate(voxels, args.steps, ws, ms)
+    e2e = whole_job_rate(voxels, args.steps, ws, e2e_ms)
 
     # ---- roofline of the dominant kernel class
     peak, peak_kind = read_peaks()
