@@ -210,6 +210,7 @@ __global__ void __launch_bounds__(RW *(M / P), EPI == 2 ? 512 / (RW * (M / P)) :
     float2 acc[P];
     const int iy = (int)(row % c.n), iz = (int)(row / c.n);
     const float y = c.dxf * (iy + 0.5f) - c.pos_obsf, z = c.dxf * (iz + 0.5f) - c.pos_obsf;
+    // v . (x - x_obs) accumulated over the components, divided by |x - x_obs| once
 #pragma unroll 1
     for (int comp = 0; comp < 3; comp++) {
       row_c2r_smem<M, P, Rad>(v, sr[comp], xm[comp], t, twN, twM);
@@ -218,21 +219,28 @@ __global__ void __launch_bounds__(RW *(M / P), EPI == 2 ? 512 / (RW * (M / P)) :
 #pragma unroll
         for (int r = 0; r < RL; r++) {
           const int e = t + T * j + (M / RL) * r;
-          const float x0 = c.dxf * (2 * e + 0.5f) - c.pos_obsf, x1 = c.dxf * (2 * e + 1.5f) - c.pos_obsf;
-          const float i0 = rsqrtf(x0 * x0 + y * y + z * z), i1 = rsqrtf(x1 * x1 + y * y + z * z);
-          const float u0 = comp == 0 ? x0 * i0 : (comp == 1 ? y * i0 : z * i0);
-          const float u1 = comp == 0 ? x1 * i1 : (comp == 1 ? y * i1 : z * i1);
           const float2 x = v[j * RL + r];
-          acc[j * RL + r] = comp == 0 ? make_float2(x.x * u0, x.y * u1)
-                                      : make_float2(fmaf(x.x, u0, acc[j * RL + r].x), fmaf(x.y, u1, acc[j * RL + r].y));
+          if (comp == 0) {
+            const float x0 = c.dxf * (2 * e + 0.5f) - c.pos_obsf, x1 = c.dxf * (2 * e + 1.5f) - c.pos_obsf;
+            acc[j * RL + r] = make_float2(x.x * x0, x.y * x1);
+          } else {
+            const float w = comp == 1 ? y : z;
+            acc[j * RL + r] = make_float2(fmaf(x.x, w, acc[j * RL + r].x), fmaf(x.y, w, acc[j * RL + r].y));
+          }
         }
     }
     if (active) {
       float2 *vrow = reinterpret_cast<float2 *>(vr + row * (long)c.n);
+      const float yz = y * y + z * z;
 #pragma unroll
       for (int j = 0; j < P / RL; j++)
 #pragma unroll
-        for (int r = 0; r < RL; r++) vrow[t + T * j + (M / RL) * r] = cscale(acc[j * RL + r], scale);
+        for (int r = 0; r < RL; r++) {
+          const int e = t + T * j + (M / RL) * r;
+          const float x0 = c.dxf * (2 * e + 0.5f) - c.pos_obsf, x1 = c.dxf * (2 * e + 1.5f) - c.pos_obsf;
+          const float s0 = scale * rsqrtf(fmaf(x0, x0, yz)), s1 = scale * rsqrtf(fmaf(x1, x1, yz));
+          vrow[e] = make_float2(acc[j * RL + r].x * s0, acc[j * RL + r].y * s1);
+        }
     }
   } else {
     float2 *grow = in.main[0] + row * (long)M;
