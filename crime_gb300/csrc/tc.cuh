@@ -80,12 +80,21 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *mbar, uint32_t parity)
       : "memory");
   return ok != 0;
 }
-// bounded wait: false when the phase did not complete within `limit` polls
-__device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint32_t limit)
+__device__ __forceinline__ uint64_t global_ns()
 {
-  for (uint32_t i = 0; i < limit; i++)
-    if (mbar_try_wait(mbar, parity)) return true;
-  return false;
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// bounded wait: false when the phase did not complete within limit_ns of the
+// GPU's global timer (try_wait may suspend the thread, so the bound is on time,
+// not on the number of polls)
+__device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint64_t limit_ns)
+{
+  const uint64_t t0 = global_ns();
+  while (!mbar_try_wait(mbar, parity))
+    if (global_ns() - t0 > limit_ns) return false;
+  return true;
 }
 
 // 32 consecutive FP32 columns of this warp's 32 TMEM lanes (lane = row); taddr

@@ -19,7 +19,7 @@
 // MMAs (a kernel that allocates TMEM is resident once per SM).  Rows are ordered (sequence index, column), so a
 // warp's global loads and stores cover 8 runs of 4 adjacent columns (one 32-byte
 // sector each).  Every wait on the
-// MMA-completion barrier is bounded: on expiry the kernel records an error,
+// MMA-completion barrier is bounded (1 s of the GPU's global timer): on expiry the kernel records an error,
 // waits once more (bounded) for the MMAs in flight, frees its TMEM and returns.
 #include <cmath>
 #include <cstdio>
@@ -41,7 +41,7 @@ constexpr uint32_t kBBytes = 64 * 128;          // 64 rows (outputs) x 64 halves
 constexpr uint32_t kTwBytes = kL * 8;           // inter-stage twiddles (float2)
 constexpr size_t kSmem = 2 * kBBytes + kTwBytes + kSlots * 2 * kABytes;
 constexpr uint32_t kTmemCols = 128;             // two 128 x 64 FP32 accumulators per slot
-constexpr uint32_t kWaitPolls = 1u << 22;
+constexpr uint64_t kWaitNs = 1000000000ull;      // 1 s bound on every MMA-completion wait
 constexpr float kStage2Scale = 1.f / 32.f;      // folded into the twiddle table
 
 __device__ __forceinline__ uint32_t core_off(int r, int j) { return (r >> 3) * kSBO + j * kLBO + (r & 7) * 16; }
@@ -135,12 +135,12 @@ __global__ void __launch_bounds__(kThreads *kSlots, 1)
       }
       tc::mma_commit(bar);
     }
-    if (!tc::mbar_wait(bar, phase, kWaitPolls)) fail[slot] = 1;
+    if (!tc::mbar_wait(bar, phase, kWaitNs)) fail[slot] = 1;
     slot_sync(slot);
     const bool ok = fail[slot] == 0;
     if (!ok) {
       if (t == 0) atomicExch(err, 1);
-      tc::mbar_wait(bar, phase, kWaitPolls);  // let MMAs still in flight finish before TMEM is freed
+      tc::mbar_wait(bar, phase, kWaitNs);  // let MMAs still in flight finish before TMEM is freed
     }
     phase ^= 1;
     tc::fence_after_sync();
