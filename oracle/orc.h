@@ -143,6 +143,21 @@ void orc_psources_maps_catalogue(const orc_config *c, const orc_derived *d, cons
                                  long ns, const int64_t *cell, const double *u, const double *L0,
                                  const double *dzs, double *maps_ps, int64_t *pix);
 
+/* JoinT map combination (src/main_jt.c:98-321, src/healpix_extra.c:31-43,318-421); orc_joint.c */
+long orc_nest2ring(long nside, long ipnest);
+long orc_ring2nest(long nside, long ipring);
+void orc_ring_info(long nside, long ring, long *first, long *nph, double *z, double *sth, double *phi0);
+long orc_nalms(int lmax);
+long orc_indexlm(int l, int m, int lmax);
+void orc_lambda_m(int lmax, int m, double z, double sth, double *out);
+void orc_map2alm(long nside, int lmax, const double *map, double *alm);
+void orc_alm2map(long nside, int lmax, const double *alm, double *map);
+void orc_udgrade(const float *map_in, long nside_in, float *map_out, long nside_out);
+void orc_beam_window(int lmax, double fwhm_amin, double *beam);
+void orc_apply_beam(long nside, int n_maps, const double *fwhm_amin, float *maps);
+void orc_add_noise(long nside, int n_nu, const double *nu0, const double *nuf, double fsky, double tsys,
+                   double time_tot, int n_dish, unsigned int seed, int nthreads, float *maps);
+
 #ifdef __cplusplus
 }
 #endif

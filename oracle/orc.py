@@ -84,6 +84,19 @@ def lib():
         L.orc_n_of_z_psources.argtypes = [f64p, C.c_double, C.c_double]
         L.orc_ps_lambda.argtypes = [P(Config), P(Derived), f64p, C.c_double, f32p, C.c_double, f64p]
         L.orc_n_of_z_psources.restype = C.c_double
+        for fn in ("orc_nest2ring", "orc_ring2nest"):
+            getattr(L, fn).argtypes = [C.c_long, C.c_long]
+            getattr(L, fn).restype = C.c_long
+        L.orc_ring_info.argtypes = [C.c_long, C.c_long, P(C.c_long), P(C.c_long), P(C.c_double), P(C.c_double),
+                                    P(C.c_double)]
+        L.orc_lambda_m.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, f64p]
+        L.orc_map2alm.argtypes = [C.c_long, C.c_int, f64p, f64p]
+        L.orc_alm2map.argtypes = [C.c_long, C.c_int, f64p, f64p]
+        L.orc_udgrade.argtypes = [f32p, C.c_long, f32p, C.c_long]
+        L.orc_beam_window.argtypes = [C.c_int, C.c_double, f64p]
+        L.orc_apply_beam.argtypes = [C.c_long, C.c_int, f64p, f32p]
+        L.orc_add_noise.argtypes = [C.c_long, C.c_int, f64p, f64p, C.c_double, C.c_double, C.c_double, C.c_int,
+                                    C.c_uint, C.c_int, f32p]
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_num_threads.restype = C.c_int
         _lib = L
@@ -297,3 +310,119 @@ def set_threads(t):
 def load_pk(path):
     a = np.loadtxt(path)
     return a[:, 0], a[:, 1]
+
+
+# ---------------------------------------------------------------------------
+# JoinT (src/main_jt.c:98-372; src/healpix_extra.c:31-43, 318-421)
+# ---------------------------------------------------------------------------
+PREFAC_FWHM = 1030610.55  # src/main_jt.c:26, arcmin for nu in MHz and the dish in m
+PREFAC_TNU = 3.6e9        # src/main_jt.c:25
+
+
+def nest2ring(nside, ipnest):
+    return lib().orc_nest2ring(nside, int(ipnest))
+
+
+def ring2nest(nside, ipring):
+    return lib().orc_ring2nest(nside, int(ipring))
+
+
+def ring_info(nside, ring):
+    a, b = C.c_long(), C.c_long()
+    z, s, p = C.c_double(), C.c_double(), C.c_double()
+    lib().orc_ring_info(nside, ring, C.byref(a), C.byref(b), C.byref(z), C.byref(s), C.byref(p))
+    return a.value, b.value, z.value, s.value, p.value
+
+
+def nalms(lmax):
+    return (lmax + 1) * (lmax + 2) // 2
+
+
+def map2alm(nside, lmax, m):
+    """HEALPix a_lm (m-major triangular, complex128) of one FP64 map"""
+    out = np.zeros(2 * nalms(lmax))
+    lib().orc_map2alm(nside, lmax, np.ascontiguousarray(m, np.float64), out)
+    return out.view(np.complex128)
+
+
+def alm2map(nside, lmax, alm):
+    out = np.zeros(12 * nside * nside)
+    lib().orc_alm2map(nside, lmax, np.ascontiguousarray(np.asarray(alm, np.complex128).view(np.float64)), out)
+    return out
+
+
+def udgrade(map_in, nside_in, nside_out):
+    out = np.zeros(12 * nside_out * nside_out, np.float32)
+    lib().orc_udgrade(np.ascontiguousarray(map_in, np.float32), nside_in, out, nside_out)
+    return out
+
+
+def beam_window(lmax, fwhm_amin):
+    out = np.zeros(lmax + 1)
+    lib().orc_beam_window(lmax, fwhm_amin, out)
+    return out
+
+
+def joint_fwhm(nu0, nuf, dish):
+    """per channel FWHM in arcmin at the channel centre (src/main_jt.c:224-226)"""
+    return PREFAC_FWHM / (0.5 * (np.asarray(nu0) + np.asarray(nuf)) * dish)
+
+
+def apply_beam(maps, nside, fwhm_amin):
+    out = np.ascontiguousarray(maps, np.float32).copy()
+    lib().orc_apply_beam(nside, out.shape[0], np.ascontiguousarray(fwhm_amin, np.float64), out)
+    return out
+
+
+def add_noise(maps, nside, nu0, nuf, fsky, tsys, time_tot, n_dish, seed, nthreads=1):
+    out = np.ascontiguousarray(maps, np.float32).copy()
+    lib().orc_add_noise(nside, out.shape[0], np.ascontiguousarray(nu0, np.float64),
+                        np.ascontiguousarray(nuf, np.float64), fsky, tsys, time_tot, n_dish, seed, nthreads, out)
+    return out
+
+
+def joint(components, nside_in, nside, nu0, nuf, dish=-1.0, n_dish=1, tsys=-1.0, time_tot=1.0, seed=1,
+          mask=None, nthreads=1):
+    """The JoinT pipeline: merge_maps (src/main_jt.c:98-200, float sums in the
+    component order, then he_udgrade), apply_beam when dish > 0, add_noise when
+    tsys > 0, apply_mask.  components: [(maps [n_nu][12 nside_in^2], factor or
+    None)], the factor (polarisation leakage) applied as float * double -> float."""
+    n_nu = len(nu0)
+    acc = np.zeros((n_nu, 12 * nside_in * nside_in), np.float32)
+    for maps, fac in components:
+        m = np.asarray(maps, np.float32)
+        if fac is not None:
+            m = (m.astype(np.float64) * fac).astype(np.float32)
+        acc = acc + m
+    out = np.stack([udgrade(acc[i], nside_in, nside) for i in range(n_nu)])
+    if dish > 0:
+        out = apply_beam(out, nside, joint_fwhm(nu0, nuf, dish))
+    npix = 12 * nside * nside
+    fsky = 1.0 if mask is None else float(np.count_nonzero(mask)) / npix
+    if tsys > 0:
+        out = add_noise(out, nside, nu0, nuf, fsky, tsys, time_tot, n_dish, seed, nthreads)
+    if mask is not None:
+        out[:, np.asarray(mask) == 0] = 0
+    return out
+
+
+def joint_instrument(nside, nu0, nuf, dish, n_dish, tsys, time_tot, fsky):
+    """Rows of <prefix_out>_instrument.dat (src/main_jt.c:28-72): nu, FWHM in
+    degrees, noise rms per pointing, noise rms per pixel."""
+    rows = []
+    npix = 12 * nside * nside
+    for a, b in zip(nu0, nuf):
+        nu, dnu = 0.5 * (a + b), b - a
+        n_pix = fsky * npix
+        if dish > 0:
+            fwhm_rad = PREFAC_FWHM / (nu * dish) * np.pi / (180 * 60)
+            n_point = fsky * 4 * np.pi / (1.1330900354567985 * fwhm_rad * fwhm_rad)
+        else:
+            fwhm_rad, n_point = 0.0, fsky * npix
+        if tsys > 0:
+            s2p = n_point * tsys * tsys / (PREFAC_TNU * dnu * time_tot * n_dish)
+            s2x = n_pix * tsys * tsys / (PREFAC_TNU * dnu * time_tot * n_dish)
+        else:
+            s2p = s2x = 0.0
+        rows.append((nu, 180 * fwhm_rad / np.pi, np.sqrt(s2p), np.sqrt(s2x)))
+    return np.array(rows)
