@@ -1,5 +1,5 @@
 """Build the GB300 GetHI library in-tree: crime_gb300/lib/libgethi_gpu.so (+ the
-GetHI_gpu command-line driver and the colpass_bench column-transform benchmark).  sm_103a only; translation units compile in
+GetHI_gpu and JoinT_gpu command-line drivers and the colpass_bench column-transform benchmark).  sm_103a only; translation units compile in
 parallel.  Usage: python -m crime_gb300.build [--force]"""
 import concurrent.futures as cf
 import os
@@ -12,11 +12,13 @@ OBJ = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libgethi_gpu.so")
 EXE = os.path.join(LIBDIR, "GetHI_gpu")
+EXE_JT = os.path.join(LIBDIR, "JoinT_gpu")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU = ["fft.cu", "tcfft.cu", "stages.cu", "api.cu", "noalloc.cu"]
-CXX = ["host.cpp"]
-HDRS = ["common.cuh", "fft.h", "host.h", "modes.cuh", "tc.cuh", "dfloat.cuh", os.path.join("..", "..", "include", "gethi_gpu.h")]
+CU = ["fft.cu", "tcfft.cu", "stages.cu", "api.cu", "noalloc.cu", "joint.cu"]
+CXX = ["host.cpp", "joint_host.cpp"]
+HDRS = ["common.cuh", "fft.h", "host.h", "modes.cuh", "tc.cuh", "dfloat.cuh", "healpix.h",
+        os.path.join("..", "..", "include", "gethi_gpu.h"), os.path.join("..", "..", "include", "joint_gpu.h")]
 
 
 def _newer(target, deps):
@@ -64,6 +66,10 @@ def build(force=False, verbose=False):
     if os.path.exists(drv) and (force or _newer(EXE, [drv, LIB])):
         _run(["gcc", "-O2", "-Wall", drv, "-I" + os.path.join(os.path.dirname(PKG), "include"), "-L" + LIBDIR,
               "-lgethi_gpu", "-Wl,-rpath,$ORIGIN", "-o", EXE])
+    drv = os.path.join(CSRC, "joint_main.c")
+    if os.path.exists(drv) and (force or _newer(EXE_JT, [drv, LIB])):
+        _run(["gcc", "-O2", "-Wall", drv, "-I" + os.path.join(os.path.dirname(PKG), "include"), "-L" + LIBDIR,
+              "-lgethi_gpu", "-Wl,-rpath,$ORIGIN", "-o", EXE_JT])
     if verbose:
         print("\n".join(logs))
     return LIB

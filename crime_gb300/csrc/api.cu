@@ -733,6 +733,14 @@ extern "C" int gethi_gpu_make_maps(gethi_ctx *c, float *maps_out)
   return maps_common(c, maps_out, 0);
 }
 
+extern "C" int gethi_gpu_device_maps(const gethi_ctx *c, const float **maps, const float **maps_ps)
+{
+  if (!c || !maps) return GETHI_E_ARG;
+  *maps = c->maps;
+  if (maps_ps) *maps_ps = c->s.p.do_psources ? c->maps_ps : nullptr;
+  return GETHI_OK;
+}
+
 extern "C" int gethi_gpu_run(gethi_ctx *c, float *maps_out)
 {
   if (!c) return GETHI_E_ARG;

@@ -1,0 +1,1116 @@
+// JoinT on the GPU: merge + ud_grade, Gaussian beam through a HEALPix spherical
+// harmonic transform, white noise, mask (src/main_jt.c:98-372,
+// src/healpix_extra.c:31-130, 318-421).
+//
+// Data layout in HBM (nside N, lmax = 3N - 1, R = 2N ring pairs: the north
+// rings 1 .. 2N-1 with their south mirrors, and the equator ring alone):
+//   maps    [channel][12 N^2] float, RING order, as the reference's maps_out
+//   acc     [channel][12 N_in^2] float, the merge sum at the input resolution
+//   lam     orthonormal Legendre functions lambda_lm(theta_q) of the north
+//           rings, FP64-evaluated and stored FP32, per m two blocks (l - m even,
+//           l - m odd) of [l'][q] with l = m + 2 l' + parity: 4.8 GB at N = 512,
+//           built once per context and kept (memory traded for FP64 work,
+//           which GB300 runs at 1/64 of FP32)
+//   E, O    per m, [q][2 c] float: the ring Fourier sums of the north ring plus
+//           (E) or minus (O) those of its south mirror, for the channels c of one
+//           batch; the same buffers then hold the synthesised north and south
+//           ring sums
+//   alm     per m, [parity][l'][2 c] float
+// A transform is, per batch of channels: ring DFTs (one CTA per ring pair,
+// direct sums over the ring's pixels with shared-memory twiddles), the
+// Legendre sums as FP32 GEMMs per (m, parity) on the CUDA cores (the beam
+// factor exp(-l(l+1) sigma_c^2 / 2) and the quadrature weight 4 pi / npix
+// applied in the epilogue), the transposed GEMMs back, and the inverse ring
+// sums.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <ctime>
+#include <string>
+#include <vector>
+
+#include "../../include/joint_gpu.h"
+#include "common.cuh"
+#include "healpix.h"
+#include "host.h"
+
+using namespace gethi;
+
+namespace {
+
+constexpr double kPrefacFwhm = 1030610.55;               // src/main_jt.c:26
+constexpr double kPrefacTnu = 3.6e9;                     // src/main_jt.c:25
+constexpr double kFwhm2Sigma = 0.00012352884853326381;  // src/healpix_extra.c:388
+constexpr int kThreads = 256;
+
+struct RingPair {
+  long long first_n, first_s;  // first pixel of the north ring and of its south mirror
+  int nph;                     // pixels per ring
+  int shifted;                 // first pixel at longitude pi / nph (else 0)
+  long long tw_off;            // offset of this ring length's twiddles (2 i (i-1), nph = 4 i)
+};
+
+// ---------------------------------------------------------------------------
+// merge, ud_grade, noise, mask
+// ---------------------------------------------------------------------------
+__global__ void add_kernel(float *__restrict__ acc, const float *__restrict__ src, long long n, double factor,
+                           int scaled)
+{
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    float v = src[i];
+    if (scaled) v = (float)((double)v * factor);  // src/main_jt.c:181
+    acc[i] = __fadd_rn(acc[i], v);                // src/main_jt.c:94
+  }
+}
+
+// he_udgrade, nside_in > nside_out: FP64 sum of the NESTED children in order, times 1/ratio
+__global__ void degrade_kernel(const float *__restrict__ in, long long nside_in, float *__restrict__ out,
+                               long long nside_out, int nmaps)
+{
+  const long long npix_out = 12 * nside_out * nside_out, npix_in = 12 * nside_in * nside_in;
+  const long long ratio = npix_in / npix_out;
+  const double inv = 1.0 / (double)ratio;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < npix_out * nmaps;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long c = t / npix_out, i = t - c * npix_out;
+    const long long nest = hpx::ring2nest(nside_out, i);
+    const float *m = in + c * npix_in;
+    double tot = 0;
+    for (long long j = 0; j < ratio; j++) tot = __dadd_rn(tot, (double)m[hpx::nest2ring(nside_in, j + ratio * nest)]);
+    out[t] = (float)__dmul_rn(tot, inv);
+  }
+}
+
+// he_udgrade, nside_in < nside_out: every NESTED child takes the parent's value
+__global__ void upgrade_kernel(const float *__restrict__ in, long long nside_in, float *__restrict__ out,
+                               long long nside_out, int nmaps)
+{
+  const long long npix_out = 12 * nside_out * nside_out, npix_in = 12 * nside_in * nside_in;
+  const long long ratio = npix_out / npix_in;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < npix_out * nmaps;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long c = t / npix_out, i = t - c * npix_out;
+    const long long nest = hpx::ring2nest(nside_out, i);
+    out[t] = in[c * npix_in + hpx::nest2ring(nside_in, nest / ratio)];
+  }
+}
+
+__global__ void mask_kernel(float *__restrict__ maps, const int *__restrict__ mask, long long npix, int nmaps)
+{
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < npix * nmaps;
+       t += (long long)gridDim.x * blockDim.x)
+    if (mask[t % npix] == 0) maps[t] = 0.f;
+}
+
+// white noise with Philox4x32-10 draws, key (seed, "JOIN"), counter (pixel, channel):
+// noise = sqrt(-s2 ln(1 - u2)) cos(2 pi u1), the law of src/main_jt.c:304-311
+__global__ void noise_philox_kernel(float *__restrict__ maps, const float *__restrict__ s2, long long npix, int nmaps,
+                                    uint32_t seed)
+{
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < npix * nmaps;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long c = t / npix, i = t - c * npix;
+    const uint4 r = philox4x32_10(make_uint4((uint32_t)i, (uint32_t)(i >> 32), (uint32_t)c, 0u),
+                                  make_uint2(seed, 0x4A4F494Eu));
+    const float u1 = (float)(r.x >> 8) * (1.f / 16777216.f), u2 = (float)(r.y >> 8) * (1.f / 16777216.f);
+    const float mod = sqrtf(-s2[c] * log1pf(-u2));
+    maps[t] = __fadd_rn(maps[t], mod * cospif(2.f * u1));
+  }
+}
+
+// the reference's MT19937 noise (drawn on the host in FP64) added as it adds it:
+// float = (float)((double)float + noise)
+__global__ void noise_add_kernel(float *__restrict__ map, const double *__restrict__ noise, long long n)
+{
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    map[i] = (float)__dadd_rn((double)map[i], noise[i]);
+}
+
+// ---------------------------------------------------------------------------
+// spherical harmonic transform
+// ---------------------------------------------------------------------------
+__host__ __device__ inline long long m_offset(int m, int lmax)  // sum of (lmax - m' + 1), m' < m
+{
+  return (long long)m * (lmax + 1) - (long long)m * (m - 1) / 2;
+}
+
+// lambda_lm(theta_q), l = m .. lmax, for one m per blockIdx.y and one ring pair per
+// thread: three-term recursion in l in FP64 with a power-of-two exponent kept
+// apart (sin^m theta alone underflows FP64 for large m near the poles)
+__global__ void lambda_kernel(const double *__restrict__ ring_z, const double *__restrict__ ring_log2sin,
+                              const double *__restrict__ lmm0, int lmax, int R, float *__restrict__ lam)
+{
+  extern __shared__ double coef[];  // a_l at [l - m], b_l at [lmax + 1 + l - m]
+  const int m = blockIdx.y, nl = lmax - m + 1;
+  for (int i = threadIdx.x; i < nl; i += blockDim.x) {
+    const int l = m + i;
+    double a = 0, b = 0;
+    if (i >= 1) a = sqrt((4.0 * l * l - 1.0) / ((double)(l - m) * (l + m)));
+    if (i >= 2) b = sqrt(((double)(l - 1) * (l - 1) - (double)m * m) / (4.0 * (l - 1) * (l - 1) - 1.0));
+    coef[i] = a;
+    coef[lmax + 1 + i] = b;
+  }
+  __syncthreads();
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= R) return;
+  const int ne = (lmax - m) / 2 + 1;
+  const long long off = m_offset(m, lmax);
+  float *Le = lam + off * R + q, *Lo = lam + (off + ne) * R + q;
+  const double z = ring_z[q];
+  const double lg = lmm0[m] + (m ? m * ring_log2sin[q] : 0.0);
+  int e = (int)floor(lg);
+  double p1 = exp2(lg - e), p2 = 0.0;
+  if (m & 1) p1 = -p1;
+  double sc = exp2((double)e);  // 0 when e < -1074: such values are far below FP32 range
+  Le[0] = (float)(p1 * sc);
+  for (int i = 1; i < nl; i++) {
+    const double p = coef[i] * (z * p1 - coef[lmax + 1 + i] * p2);
+    p2 = p1;
+    p1 = p;
+    if (fabs(p1) > 0x1p300) {
+      p1 *= 0x1p-300;
+      p2 *= 0x1p-300;
+      e += 300;
+      sc = exp2((double)e);
+    }
+    const float v = (float)(p1 * sc);
+    if (i & 1) Lo[(long long)(i >> 1) * R] = v;
+    else Le[(long long)(i >> 1) * R] = v;
+  }
+}
+
+template <int CB> struct VecT;
+template <> struct VecT<2> { typedef float2 T; };
+template <> struct VecT<4> { typedef float4 T; };
+__device__ __forceinline__ float vget(const float2 &v, int i) { return i ? v.y : v.x; }
+__device__ __forceinline__ float vget(const float4 &v, int i) { return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w; }
+__device__ __forceinline__ void vset(float2 &v, int i, float x) { if (i) v.y = x; else v.x = x; }
+__device__ __forceinline__ void vset(float4 &v, int i, float x)
+{
+  if (i == 0) v.x = x; else if (i == 1) v.y = x; else if (i == 2) v.z = x; else v.w = x;
+}
+
+// Ring analysis of ring pair q for CB channels: D_k = sum_j x_j e^{-2 pi i jk/n}
+// (k <= n/2; the rest by conjugate symmetry), then for m = 0 .. lmax the
+// phase-shifted sums F_m = e^{-i m phi0} D_{m mod n} of both rings combined
+// as E = F_north + F_south and O = F_north - F_south.
+template <int CB>
+__global__ __launch_bounds__(kThreads) void ring_analysis_kernel(const float *__restrict__ maps, long long npix,
+                                                                 int nch, const RingPair *__restrict__ rings,
+                                                                 const float2 *__restrict__ tw_all, int lmax, int R,
+                                                                 int N2, float *__restrict__ E, float *__restrict__ O)
+{
+  typedef typename VecT<CB>::T VT;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int q = blockIdx.x, cb0 = blockIdx.y * CB;
+  const RingPair rp = rings[q];
+  const int n = rp.nph, half = n / 2;
+  const bool eq = (q == R - 1);
+  VT *x = reinterpret_cast<VT *>(smem_raw);
+  float2 *tw = reinterpret_cast<float2 *>(x + 2 * n);
+  float2 *D = tw + n;  // [2][half + 1][CB]
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    tw[j] = tw_all[rp.tw_off + j];
+#pragma unroll
+    for (int s = 0; s < 2; s++) {
+      VT v;
+#pragma unroll
+      for (int b = 0; b < CB; b++) {
+        const int c = cb0 + b;
+        float val = 0.f;
+        if (c < nch && (s == 0 || !eq)) val = maps[(long long)c * npix + (s ? rp.first_s : rp.first_n) + j];
+        vset(v, b, val);
+      }
+      x[s * n + j] = v;
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k <= half; k += blockDim.x) {
+    float2 an[CB], as[CB];
+#pragma unroll
+    for (int b = 0; b < CB; b++) an[b] = as[b] = make_float2(0.f, 0.f);
+    int idx = 0;
+    for (int j = 0; j < n; j++) {
+      const float2 w = tw[idx];
+      const VT xn = x[j], xs = x[n + j];
+#pragma unroll
+      for (int b = 0; b < CB; b++) {
+        an[b].x = fmaf(vget(xn, b), w.x, an[b].x);
+        an[b].y = fmaf(-vget(xn, b), w.y, an[b].y);
+        as[b].x = fmaf(vget(xs, b), w.x, as[b].x);
+        as[b].y = fmaf(-vget(xs, b), w.y, as[b].y);
+      }
+      idx += k;
+      if (idx >= n) idx -= n;
+    }
+#pragma unroll
+    for (int b = 0; b < CB; b++) {
+      D[k * CB + b] = an[b];
+      D[(half + 1 + k) * CB + b] = as[b];
+    }
+  }
+  __syncthreads();
+  for (int m = threadIdx.x; m <= lmax; m += blockDim.x) {
+    int k = m % n;
+    const bool cj = k > half;
+    if (cj) k = n - k;
+    float2 ph = make_float2(1.f, 0.f);
+    if (rp.shifted) {
+      float s, c;
+      sincospif((float)(m % (2 * n)) / (float)n, &s, &c);
+      ph = make_float2(c, -s);
+    }
+#pragma unroll
+    for (int b = 0; b < CB; b++) {
+      const int c = cb0 + b;
+      if (c >= nch) continue;
+      float2 dn = D[k * CB + b], ds = D[(half + 1 + k) * CB + b];
+      if (cj) {
+        dn.y = -dn.y;
+        ds.y = -ds.y;
+      }
+      const float2 e = make_float2(dn.x + ds.x, dn.y + ds.y), o = make_float2(dn.x - ds.x, dn.y - ds.y);
+      const long long base = ((long long)m * R + q) * N2 + 2 * c;
+      *reinterpret_cast<float2 *>(E + base) = make_float2(e.x * ph.x - e.y * ph.y, e.x * ph.y + e.y * ph.x);
+      *reinterpret_cast<float2 *>(O + base) = make_float2(o.x * ph.x - o.y * ph.y, o.x * ph.y + o.y * ph.x);
+    }
+  }
+}
+
+// Ring synthesis: for each ring of pair q, fold c_m G_m e^{i m phi0} (c_0 = 1,
+// c_m = 2) into the frequencies k = m mod n, pair k with n - k (real output),
+// and sum map_j = sum_k Re(Q_k e^{2 pi i jk/n}).
+template <int CB>
+__global__ __launch_bounds__(kThreads) void ring_synthesis_kernel(const float *__restrict__ Gn,
+                                                                  const float *__restrict__ Gs,
+                                                                  const RingPair *__restrict__ rings,
+                                                                  const float2 *__restrict__ tw_all, int lmax, int R,
+                                                                  int N2, int nch, float *__restrict__ maps,
+                                                                  long long npix)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int q = blockIdx.x, cb0 = blockIdx.y * CB;
+  const RingPair rp = rings[q];
+  const int n = rp.nph, half = n / 2;
+  const bool eq = (q == R - 1);
+  float2 *tw = reinterpret_cast<float2 *>(smem_raw);
+  float2 *Q = tw + n;  // [2][half + 1][CB]
+  for (int j = threadIdx.x; j < n; j += blockDim.x) tw[j] = tw_all[rp.tw_off + j];
+  for (int t = threadIdx.x; t < 2 * (half + 1); t += blockDim.x) {
+    const int s = t / (half + 1), k = t - s * (half + 1);
+    const float *G = s ? Gs : Gn;
+    float2 acc[CB];
+#pragma unroll
+    for (int b = 0; b < CB; b++) acc[b] = make_float2(0.f, 0.f);
+    if (s == 0 || !eq) {
+      for (int pass = 0; pass < 2; pass++) {
+        if (pass == 1 && (k == 0 || k == half)) break;
+        const float sg = pass ? -1.f : 1.f;  // pass 1: conjugate of the n - k terms
+        for (int m = pass ? n - k : k; m <= lmax; m += n) {
+          float2 ph = make_float2(1.f, 0.f);
+          if (rp.shifted) {
+            float sn, cs;
+            sincospif((float)(m % (2 * n)) / (float)n, &sn, &cs);
+            ph = make_float2(cs, sn);
+          }
+          const float cm = m ? 2.f : 1.f;
+#pragma unroll
+          for (int b = 0; b < CB; b++) {
+            if (cb0 + b >= nch) continue;
+            const float2 g = *reinterpret_cast<const float2 *>(G + ((long long)m * R + q) * N2 + 2 * (cb0 + b));
+            acc[b].x += cm * (g.x * ph.x - g.y * ph.y);
+            acc[b].y += sg * cm * (g.x * ph.y + g.y * ph.x);
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int b = 0; b < CB; b++) Q[t * CB + b] = acc[b];
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    float vn[CB], vs[CB];
+#pragma unroll
+    for (int b = 0; b < CB; b++) vn[b] = vs[b] = 0.f;
+    int idx = 0;
+    for (int k = 0; k <= half; k++) {
+      const float2 w = tw[idx];
+#pragma unroll
+      for (int b = 0; b < CB; b++) {
+        const float2 a = Q[k * CB + b], c = Q[(half + 1 + k) * CB + b];
+        vn[b] = fmaf(a.x, w.x, fmaf(-a.y, w.y, vn[b]));
+        vs[b] = fmaf(c.x, w.x, fmaf(-c.y, w.y, vs[b]));
+      }
+      idx += j;
+      if (idx >= n) idx -= n;
+    }
+#pragma unroll
+    for (int b = 0; b < CB; b++) {
+      const int c = cb0 + b;
+      if (c >= nch) continue;
+      maps[(long long)c * npix + rp.first_n + j] = vn[b];
+      if (!eq) maps[(long long)c * npix + rp.first_s + j] = vs[b];
+    }
+  }
+}
+
+constexpr int BM = 64, BN = 64, BK = 16;
+
+// Legendre analysis, one 64 x 64 tile of one (m, parity) per CTA:
+// alm[l'][col] = scale(l, col) sum_q lam[l'][q] EO[q][col]
+__global__ __launch_bounds__(kThreads) void legendre_analysis_kernel(const float *__restrict__ lam,
+                                                                     const float *__restrict__ E,
+                                                                     const float *__restrict__ O,
+                                                                     float *__restrict__ alm,
+                                                                     const int4 *__restrict__ tasks, int R, int lmax,
+                                                                     int N2, float w, const float *__restrict__ sig2)
+{
+  __shared__ __align__(16) float As[BK][BM + 4];
+  __shared__ __align__(16) float Bs[BK][BN];
+  const int4 t = tasks[blockIdx.x];
+  const int m = t.x, p = t.y, row0 = t.z * BM, col0 = t.w * BN;
+  const int ne = (lmax - m) / 2 + 1, no = (lmax - m + 1) / 2, M = p ? no : ne;
+  const long long off = m_offset(m, lmax) + (p ? ne : 0);
+  const float *A = lam + off * R;
+  const float *B = (p ? O : E) + (long long)m * R * N2;
+  float *C = alm + off * N2;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  float acc[4][4] = {};
+  for (int k0 = 0; k0 < R; k0 += BK) {
+#pragma unroll
+    for (int i = 0; i < 4; i++) {  // A: 64 rows x 16 q, 4 per thread
+      const int e = tid + i * kThreads, r = e >> 4, k = e & 15;
+      As[k][r] = (row0 + r < M && k0 + k < R) ? A[(long long)(row0 + r) * R + k0 + k] : 0.f;
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++) {  // B: 16 q x 64 columns
+      const int e = tid + i * kThreads, k = e >> 6, c = e & 63;
+      Bs[k][c] = (k0 + k < R && col0 + c < N2) ? B[(long long)(k0 + k) * N2 + col0 + c] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < BK; k++) {
+      const float4 a = *reinterpret_cast<const float4 *>(&As[k][ty * 4]);
+      const float4 b = *reinterpret_cast<const float4 *>(&Bs[k][tx * 4]);
+      const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const int r = row0 + ty * 4 + i;
+    if (r >= M) continue;
+    const float l = (float)(m + 2 * r + p);
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int col = col0 + tx * 4 + j;
+      if (col >= N2) continue;
+      float s = w;
+      if (sig2) s *= expf(-0.5f * l * (l + 1.f) * sig2[col >> 1]);
+      C[(long long)r * N2 + col] = acc[i][j] * s;
+    }
+  }
+}
+
+// Legendre synthesis, one 64 x 64 tile (ring pairs x columns) of one m per CTA:
+// G_e[q][col] = sum_l' lam_e[l'][q] alm_e[l'][col] and the same for l - m odd;
+// north ring sums G_e + G_o, south G_e - G_o (lambda_lm(-z) = (-1)^{l+m} lambda_lm(z))
+__global__ __launch_bounds__(kThreads) void legendre_synthesis_kernel(const float *__restrict__ lam,
+                                                                      const float *__restrict__ alm,
+                                                                      float *__restrict__ Gn, float *__restrict__ Gs,
+                                                                      const int4 *__restrict__ tasks, int R, int lmax,
+                                                                      int N2)
+{
+  __shared__ __align__(16) float As[BK][BM];
+  __shared__ __align__(16) float Bs[BK][BN];
+  const int4 t = tasks[blockIdx.x];
+  const int m = t.x, row0 = t.z * BM, col0 = t.w * BN;
+  const int ne = (lmax - m) / 2 + 1, no = (lmax - m + 1) / 2;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  float ae[4][4] = {}, ao[4][4] = {};
+#pragma unroll 1
+  for (int p = 0; p < 2; p++) {
+    const int K = p ? no : ne;
+    const long long off = m_offset(m, lmax) + (p ? ne : 0);
+    const float *A = lam + off * R;  // [l'][q]
+    const float *B = alm + off * N2;  // [l'][col]
+    for (int k0 = 0; k0 < K; k0 += BK) {
+#pragma unroll
+      for (int i = 0; i < 4; i++) {  // A^T: 16 l' x 64 q
+        const int e = tid + i * kThreads, k = e >> 6, r = e & 63;
+        As[k][r] = (k0 + k < K && row0 + r < R) ? A[(long long)(k0 + k) * R + row0 + r] : 0.f;
+      }
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        const int e = tid + i * kThreads, k = e >> 6, c = e & 63;
+        Bs[k][c] = (k0 + k < K && col0 + c < N2) ? B[(long long)(k0 + k) * N2 + col0 + c] : 0.f;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < BK; k++) {
+        const float4 a = *reinterpret_cast<const float4 *>(&As[k][ty * 4]);
+        const float4 b = *reinterpret_cast<const float4 *>(&Bs[k][tx * 4]);
+        const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+        if (p == 0) {
+#pragma unroll
+          for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) ae[i][j] = fmaf(av[i], bv[j], ae[i][j]);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) ao[i][j] = fmaf(av[i], bv[j], ao[i][j]);
+        }
+      }
+      __syncthreads();
+    }
+  }
+  float *gn = Gn + (long long)m * R * N2, *gs = Gs + (long long)m * R * N2;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const int r = row0 + ty * 4 + i;
+    if (r >= R) continue;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int col = col0 + tx * 4 + j;
+      if (col >= N2) continue;
+      gn[(long long)r * N2 + col] = ae[i][j] + ao[i][j];
+      gs[(long long)r * N2 + col] = ae[i][j] - ao[i][j];
+    }
+  }
+}
+
+// internal a_lm [m][parity][l'][2c] <-> HEALPix order [c][l + m lmax - m(m-1)/2] (complex)
+__global__ void alm_to_healpix_kernel(const float *__restrict__ alm, float2 *__restrict__ out, int lmax, int N2,
+                                      int nch, long long nalm)
+{
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nalm * nch;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long c = t / nalm, i = t - c * nalm;
+    // i = m_offset(m) + (l - m): find m
+    const float b2 = 2.f * lmax + 3.f;
+    int m = max(0, min(lmax, (int)((b2 - sqrtf(fmaxf(b2 * b2 - 8.f * (float)i, 0.f))) * 0.5f)));
+    while (m > 0 && m_offset(m, lmax) > i) m--;
+    while (m < lmax && m_offset(m + 1, lmax) <= i) m++;
+    const int l = m + (int)(i - m_offset(m, lmax)), ne = (lmax - m) / 2 + 1, p = (l - m) & 1;
+    const long long row = m_offset(m, lmax) + (p ? ne : 0) + ((l - m) >> 1);
+    out[t] = *reinterpret_cast<const float2 *>(alm + row * N2 + 2 * c);
+  }
+}
+
+__global__ void alm_from_healpix_kernel(const float2 *__restrict__ in, float *__restrict__ alm, int lmax, int N2,
+                                        int nch, long long nalm)
+{
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nalm * nch;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long c = t / nalm, i = t - c * nalm;
+    const float b2 = 2.f * lmax + 3.f;
+    int m = max(0, min(lmax, (int)((b2 - sqrtf(fmaxf(b2 * b2 - 8.f * (float)i, 0.f))) * 0.5f)));
+    while (m > 0 && m_offset(m, lmax) > i) m--;
+    while (m < lmax && m_offset(m + 1, lmax) <= i) m++;
+    const int l = m + (int)(i - m_offset(m, lmax)), ne = (lmax - m) / 2 + 1, p = (l - m) & 1;
+    const long long row = m_offset(m, lmax) + (p ? ne : 0) + ((l - m) >> 1);
+    *reinterpret_cast<float2 *>(alm + row * N2 + 2 * c) = in[t];
+  }
+}
+
+int grid_for(long long n)
+{
+  long long b = (n + kThreads - 1) / kThreads;
+  return (int)std::max(1LL, std::min(b, 152LL * 16));
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+struct joint_ctx {
+  joint_params p{};
+  std::vector<double> nu0, nuf;
+  std::vector<int> mask;  // empty: no mask
+  double fsky = 1.0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  long long npix = 0;
+  int lmax = 0, R = 0;
+  float *maps = nullptr;   // [n_nu][npix]
+  float *acc = nullptr;    // merge sum at nside_in
+  long long nside_in = 0, acc_cap = 0;
+  float *stage_buf = nullptr;  // host components staged on the device
+  long long stage_cap = 0;
+  int *dmask = nullptr;
+  float *s2 = nullptr;     // per channel noise variance (Philox path)
+  int stage = 0;           // 0 nothing added, 1 adding components, 2 merged (maps valid)
+  bool have_acc = false;   // acc holds the sum of the components added since the last merge
+  // spherical harmonic transform
+  RingPair *rings = nullptr;
+  float2 *tw = nullptr;
+  float *lam = nullptr;
+  int chunk = 0, N2 = 0;
+  float *E = nullptr, *O = nullptr, *alm = nullptr, *sig2 = nullptr, *tmp_maps = nullptr;
+  float2 *alm_hp = nullptr;
+  int4 *tasks_a = nullptr, *tasks_s = nullptr;
+  int ntasks_a = 0, ntasks_s = 0;
+  double *noise_h = nullptr, *noise_d = nullptr;  // mt_validation staging (pinned host, device)
+  cudaEvent_t ev[5] = {};
+  float times[4] = {};
+};
+
+namespace {
+
+int jfail(cudaError_t e, const char *what)
+{
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return GETHI_E_CUDA;
+}
+#define JCK(call)                                       \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return jfail(e_, #call);     \
+  } while (0)
+
+template <class T>
+int jalloc(T **p, size_t count)
+{
+  cudaError_t e = cudaMalloc((void **)p, std::max<size_t>(count, 1) * sizeof(T));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    set_error(std::string("cudaMalloc of ") + std::to_string(count * sizeof(T)) + " bytes: " + cudaGetErrorString(e));
+    return GETHI_E_NOMEM;
+  }
+  return GETHI_OK;
+}
+
+size_t analysis_smem(int n, int cb) { return (size_t)2 * n * cb * 4 + (size_t)n * 8 + (size_t)2 * (n / 2 + 1) * cb * 8; }
+size_t synthesis_smem(int n, int cb) { return (size_t)n * 8 + (size_t)2 * (n / 2 + 1) * cb * 8; }
+int ring_cb(long long nside) { return nside <= 512 ? 4 : 2; }
+
+// ring pairs, twiddles and the Legendre table of the context's nside (first transform)
+int ensure_sht(joint_ctx *c)
+{
+  if (c->lam) return GETHI_OK;
+  const long long N = c->p.nside;
+  if (N > 1024) {
+    set_error("spherical harmonic transforms support nside <= 1024");
+    return GETHI_E_ARG;
+  }
+  const int R = (int)(2 * N), lmax = (int)(3 * N - 1);
+  c->R = R;
+  c->lmax = lmax;
+  std::vector<RingPair> rp(R);
+  std::vector<double> z(R), lsin(R), lmm0(lmax + 1);
+  const long long npix = 12 * N * N, ncap = 2 * N * (N - 1);
+  for (int q = 0; q < R; q++) {
+    const long long i = q + 1;  // north ring number (q = R - 1: the equator)
+    double cz, sz;
+    RingPair r;
+    if (i < N) {
+      const double a = (double)i * i / (3.0 * N * N);
+      cz = 1.0 - a;
+      sz = std::sqrt(a * (2.0 - a));
+      r.nph = (int)(4 * i);
+      r.shifted = 1;
+      r.first_n = 2 * i * (i - 1);
+    } else {
+      cz = (double)(2 * N - i) * (2.0 / (3.0 * N));
+      sz = std::sqrt((1.0 - cz) * (1.0 + cz));
+      r.nph = (int)(4 * N);
+      r.shifted = ((i - N) & 1) ? 0 : 1;
+      r.first_n = ncap + (i - N) * 4 * N;
+    }
+    r.first_s = npix - r.nph - r.first_n;
+    const long long i4 = r.nph / 4;
+    r.tw_off = 2 * i4 * (i4 - 1);
+    rp[q] = r;
+    z[q] = cz;
+    lsin[q] = std::log2(sz);
+  }
+  double acc = 0;
+  for (int m = 0; m <= lmax; m++) {
+    if (m > 0) acc += 0.5 * std::log2((2.0 * m - 1.0) / (2.0 * m));
+    lmm0[m] = 0.5 * std::log2((2.0 * m + 1.0) / (4.0 * M_PI)) + acc;
+  }
+  // twiddles e^{2 pi i j/n} of every ring length n = 4 i, i = 1 .. N, at 2 i (i - 1)
+  std::vector<float2> tw(2 * N * (N + 1));
+  for (long long i = 1; i <= N; i++) {
+    const long long n = 4 * i, o = 2 * i * (i - 1);
+    for (long long j = 0; j < n; j++) {
+      const double a = 2.0 * M_PI * (double)j / (double)n;
+      tw[o + j] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+  }
+  int rc;
+  const size_t lam_elems = (size_t)m_offset(lmax + 1, lmax) * R;
+  if ((rc = jalloc(&c->rings, R)) || (rc = jalloc(&c->tw, tw.size())) || (rc = jalloc(&c->lam, lam_elems)))
+    return rc;
+  double *dz = nullptr, *dl = nullptr, *dm = nullptr;
+  if ((rc = jalloc(&dz, R)) || (rc = jalloc(&dl, R)) || (rc = jalloc(&dm, lmax + 1))) {
+    cudaFree(dz);
+    cudaFree(dl);
+    return rc;
+  }
+  JCK(cudaMemcpyAsync(c->rings, rp.data(), sizeof(RingPair) * R, cudaMemcpyHostToDevice, c->stream));
+  JCK(cudaMemcpyAsync(c->tw, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice, c->stream));
+  JCK(cudaMemcpyAsync(dz, z.data(), sizeof(double) * R, cudaMemcpyHostToDevice, c->stream));
+  JCK(cudaMemcpyAsync(dl, lsin.data(), sizeof(double) * R, cudaMemcpyHostToDevice, c->stream));
+  JCK(cudaMemcpyAsync(dm, lmm0.data(), sizeof(double) * (lmax + 1), cudaMemcpyHostToDevice, c->stream));
+  const size_t smem = sizeof(double) * 2 * (lmax + 1);
+  JCK(cudaFuncSetAttribute(lambda_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  lambda_kernel<<<dim3((R + 127) / 128, lmax + 1), 128, smem, c->stream>>>(dz, dl, dm, lmax, R, c->lam);
+  JCK(cudaGetLastError());
+  JCK(cudaStreamSynchronize(c->stream));
+  cudaFree(dz);
+  cudaFree(dl);
+  cudaFree(dm);
+  // channel batches and the GEMM tile lists
+  c->chunk = c->p.sht_chunk > 0 ? c->p.sht_chunk : 64;
+  c->N2 = 2 * c->chunk;
+  const int tcol = (c->N2 + BN - 1) / BN;
+  std::vector<int4> ta, ts;
+  for (int m = 0; m <= lmax; m++) {
+    const int ne = (lmax - m) / 2 + 1, no = (lmax - m + 1) / 2;
+    for (int p = 0; p < 2; p++) {
+      const int M = p ? no : ne;
+      for (int tr = 0; tr < (M + BM - 1) / BM; tr++)
+        for (int tc = 0; tc < tcol; tc++) ta.push_back(make_int4(m, p, tr, tc));
+    }
+    for (int tr = 0; tr < (R + BM - 1) / BM; tr++)
+      for (int tc = 0; tc < tcol; tc++) ts.push_back(make_int4(m, 0, tr, tc));
+  }
+  c->ntasks_a = (int)ta.size();
+  c->ntasks_s = (int)ts.size();
+  const size_t eo = (size_t)(lmax + 1) * R * c->N2;
+  if ((rc = jalloc(&c->tasks_a, ta.size())) || (rc = jalloc(&c->tasks_s, ts.size())) || (rc = jalloc(&c->E, eo)) ||
+      (rc = jalloc(&c->O, eo)) || (rc = jalloc(&c->alm, (size_t)m_offset(lmax + 1, lmax) * c->N2)) ||
+      (rc = jalloc(&c->sig2, c->chunk)))
+    return rc;
+  JCK(cudaMemcpyAsync(c->tasks_a, ta.data(), sizeof(int4) * ta.size(), cudaMemcpyHostToDevice, c->stream));
+  JCK(cudaMemcpyAsync(c->tasks_s, ts.data(), sizeof(int4) * ts.size(), cudaMemcpyHostToDevice, c->stream));
+  const int cb = ring_cb(N);
+  const int n = (int)(4 * N);
+  if (cb == 4) {
+    JCK(cudaFuncSetAttribute(ring_analysis_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)analysis_smem(n, 4)));
+    JCK(cudaFuncSetAttribute(ring_synthesis_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)synthesis_smem(n, 4)));
+  } else {
+    JCK(cudaFuncSetAttribute(ring_analysis_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)analysis_smem(n, 2)));
+    JCK(cudaFuncSetAttribute(ring_synthesis_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)synthesis_smem(n, 2)));
+  }
+  JCK(cudaStreamSynchronize(c->stream));
+  return GETHI_OK;
+}
+
+// map2alm of nch (<= chunk) device maps into c->alm (beam factors when sig2 != null)
+int sht_analysis(joint_ctx *c, const float *dmaps, int nch, const float *sig2)
+{
+  const int R = c->R, lmax = c->lmax, cb = ring_cb(c->p.nside), n = 4 * c->p.nside;
+  const dim3 g(R, (nch + cb - 1) / cb);
+  if (cb == 4)
+    ring_analysis_kernel<4><<<g, kThreads, analysis_smem(n, 4), c->stream>>>(dmaps, c->npix, nch, c->rings, c->tw,
+                                                                             lmax, R, c->N2, c->E, c->O);
+  else
+    ring_analysis_kernel<2><<<g, kThreads, analysis_smem(n, 2), c->stream>>>(dmaps, c->npix, nch, c->rings, c->tw,
+                                                                             lmax, R, c->N2, c->E, c->O);
+  JCK(cudaGetLastError());
+  const float w = (float)(4.0 * M_PI / (double)c->npix);
+  legendre_analysis_kernel<<<c->ntasks_a, kThreads, 0, c->stream>>>(c->lam, c->E, c->O, c->alm, c->tasks_a, R, lmax,
+                                                                    c->N2, w, sig2);
+  JCK(cudaGetLastError());
+  return GETHI_OK;
+}
+
+// alm2map of c->alm into nch device maps
+int sht_synthesis(joint_ctx *c, float *dmaps, int nch)
+{
+  const int R = c->R, lmax = c->lmax, cb = ring_cb(c->p.nside), n = 4 * c->p.nside;
+  legendre_synthesis_kernel<<<c->ntasks_s, kThreads, 0, c->stream>>>(c->lam, c->alm, c->E, c->O, c->tasks_s, R,
+                                                                     lmax, c->N2);
+  JCK(cudaGetLastError());
+  const dim3 g(R, (nch + cb - 1) / cb);
+  if (cb == 4)
+    ring_synthesis_kernel<4><<<g, kThreads, synthesis_smem(n, 4), c->stream>>>(c->E, c->O, c->rings, c->tw, lmax, R,
+                                                                               c->N2, nch, dmaps, c->npix);
+  else
+    ring_synthesis_kernel<2><<<g, kThreads, synthesis_smem(n, 2), c->stream>>>(c->E, c->O, c->rings, c->tw, lmax, R,
+                                                                               c->N2, nch, dmaps, c->npix);
+  JCK(cudaGetLastError());
+  return GETHI_OK;
+}
+
+void record(joint_ctx *c, int i) { cudaEventRecord(c->ev[i], c->stream); }
+
+}  // namespace
+
+extern "C" int joint_gpu_init(const joint_params *p, int device, joint_ctx **out)
+{
+  if (!p || !out) return GETHI_E_ARG;
+  *out = nullptr;
+  if (p->nside < 1 || p->nside > 8192 || (p->nside & (p->nside - 1))) {
+    set_error("nside must be a power of two between 1 and 8192");
+    return GETHI_E_ARG;
+  }
+  if (p->n_nu < 1 || !p->nu0 || !p->nuf) {
+    set_error("JoinT needs a frequency table (n_nu >= 1)");
+    return GETHI_E_ARG;
+  }
+  if (p->rng != JOINT_RNG_PHILOX && p->rng != JOINT_RNG_MT_VALIDATION) {
+    set_error("rng must be philox or mt_validation");
+    return GETHI_E_ARG;
+  }
+  if (p->tsys > 0 && (p->time_tot <= 0 || p->n_dish <= 0)) {
+    set_error("noise needs time_total > 0 and n_dishes > 0");
+    return GETHI_E_ARG;
+  }
+  JCK(cudaSetDevice(device));
+  joint_ctx *c = new joint_ctx;
+  c->p = *p;
+  c->device = device;
+  c->nu0.assign(p->nu0, p->nu0 + p->n_nu);
+  c->nuf.assign(p->nuf, p->nuf + p->n_nu);
+  c->p.nu0 = c->nu0.data();
+  c->p.nuf = c->nuf.data();
+  c->npix = 12LL * p->nside * p->nside;
+  if (p->mask) {
+    c->mask.assign(p->mask, p->mask + c->npix);
+    long long on = 0;
+    for (int v : c->mask) on += v != 0;
+    c->fsky = (double)on / (double)c->npix;  // src/io_jt.c:76
+  }
+  c->p.mask = c->mask.empty() ? nullptr : c->mask.data();
+  int rc;
+  if ((rc = jalloc(&c->maps, (size_t)c->npix * p->n_nu)) || (rc = jalloc(&c->s2, p->n_nu)) ||
+      (!c->mask.empty() && (rc = jalloc(&c->dmask, c->npix)))) {
+    joint_gpu_free(c);
+    return rc;
+  }
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    joint_gpu_free(c);
+    return jfail(e, "cudaStreamCreate");
+  }
+  c->own_stream = true;
+  for (auto &ev : c->ev) cudaEventCreate(&ev);
+  if (!c->mask.empty())
+    cudaMemcpyAsync(c->dmask, c->mask.data(), sizeof(int) * c->npix, cudaMemcpyHostToDevice, c->stream);
+  std::vector<float> s2(p->n_nu);
+  for (int i = 0; i < p->n_nu; i++) {
+    const double dnu = c->nuf[i] - c->nu0[i];
+    s2[i] = (float)(c->fsky * c->npix * p->tsys * p->tsys / (kPrefacTnu * dnu * p->time_tot * p->n_dish));
+  }
+  cudaMemcpyAsync(c->s2, s2.data(), sizeof(float) * p->n_nu, cudaMemcpyHostToDevice, c->stream);
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    joint_gpu_free(c);
+    return jfail(e, "joint_gpu_init");
+  }
+  *out = c;
+  return GETHI_OK;
+}
+
+extern "C" void joint_gpu_free(joint_ctx *c)
+{
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (void *ptr : {(void *)c->maps, (void *)c->acc, (void *)c->stage_buf, (void *)c->dmask, (void *)c->s2,
+                    (void *)c->rings, (void *)c->tw, (void *)c->lam, (void *)c->E, (void *)c->O, (void *)c->alm,
+                    (void *)c->sig2, (void *)c->tmp_maps, (void *)c->alm_hp, (void *)c->tasks_a, (void *)c->tasks_s,
+                    (void *)c->noise_d})
+    cudaFree(ptr);
+  if (c->noise_h) cudaFreeHost(c->noise_h);
+  for (auto &ev : c->ev)
+    if (ev) cudaEventDestroy(ev);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+extern "C" int joint_gpu_set_stream(joint_ctx *c, void *stream)
+{
+  if (!c) return GETHI_E_ARG;
+  JCK(cudaStreamSynchronize(c->stream));
+  if (c->own_stream) cudaStreamDestroy(c->stream);
+  c->stream = (cudaStream_t)stream;
+  c->own_stream = false;
+  return GETHI_OK;
+}
+
+extern "C" double joint_gpu_fsky(const joint_ctx *c) { return c ? c->fsky : -1.0; }
+
+static int add_common(joint_ctx *c, const float *dsrc, long nside_in, double factor)
+{
+  const long long npix_in = 12LL * nside_in * nside_in, n = npix_in * c->p.n_nu;
+  if (c->stage == 1 && nside_in != c->nside_in) {
+    set_error("read nside is not the same as provided : " + std::to_string(c->nside_in) +
+              " != " + std::to_string(nside_in));  // src/main_jt.c:74-81
+    return GETHI_E_ARG;
+  }
+  if (c->stage != 1) {  // the first component of a new combination
+    if (n > c->acc_cap) {
+      cudaFree(c->acc);
+      c->acc = nullptr;
+      int rc = jalloc(&c->acc, n);
+      if (rc) return rc;
+      c->acc_cap = n;
+    }
+    JCK(cudaMemsetAsync(c->acc, 0, sizeof(float) * n, c->stream));
+    c->nside_in = nside_in;
+    c->stage = 1;
+    c->have_acc = true;
+  }
+  add_kernel<<<grid_for(n), kThreads, 0, c->stream>>>(c->acc, dsrc, n, factor, factor != 1.0);
+  JCK(cudaGetLastError());
+  return GETHI_OK;
+}
+
+static bool valid_nside(long ns) { return ns >= 1 && ns <= 8192 && !(ns & (ns - 1)); }
+
+extern "C" int joint_gpu_add_maps(joint_ctx *c, const float *maps, long nside_in, double factor)
+{
+  if (!c || !maps || !valid_nside(nside_in)) return GETHI_E_ARG;
+  JCK(cudaSetDevice(c->device));
+  const long long n = 12LL * nside_in * nside_in * c->p.n_nu;
+  if (n > c->stage_cap) {
+    JCK(cudaStreamSynchronize(c->stream));
+    cudaFree(c->stage_buf);
+    c->stage_buf = nullptr;
+    int rc = jalloc(&c->stage_buf, n);
+    if (rc) return rc;
+    c->stage_cap = n;
+  }
+  JCK(cudaMemcpyAsync(c->stage_buf, maps, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
+  int rc = add_common(c, c->stage_buf, nside_in, factor);
+  if (rc) return rc;
+  JCK(cudaStreamSynchronize(c->stream));  // the caller may reuse `maps`
+  return GETHI_OK;
+}
+
+extern "C" int joint_gpu_add_maps_device(joint_ctx *c, const float *dmaps, long nside_in, double factor)
+{
+  if (!c || !dmaps || !valid_nside(nside_in)) return GETHI_E_ARG;
+  JCK(cudaSetDevice(c->device));
+  return add_common(c, dmaps, nside_in, factor);
+}
+
+extern "C" int joint_gpu_merge(joint_ctx *c)
+{
+  if (!c) return GETHI_E_ARG;
+  JCK(cudaSetDevice(c->device));
+  const long long N = c->p.nside, n = c->npix * c->p.n_nu;
+  if (!c->have_acc) {  // no component: the reference leaves the calloc'ed maps at zero
+    JCK(cudaMemsetAsync(c->maps, 0, sizeof(float) * n, c->stream));
+  } else {  // (again) from the sum, so a repeated run starts from the merged components
+    if (c->nside_in == N)
+      JCK(cudaMemcpyAsync(c->maps, c->acc, sizeof(float) * n, cudaMemcpyDeviceToDevice, c->stream));
+    else if (c->nside_in > N)
+      degrade_kernel<<<grid_for(n), kThreads, 0, c->stream>>>(c->acc, c->nside_in, c->maps, N, c->p.n_nu);
+    else
+      upgrade_kernel<<<grid_for(n), kThreads, 0, c->stream>>>(c->acc, c->nside_in, c->maps, N, c->p.n_nu);
+    JCK(cudaGetLastError());
+  }
+  c->stage = 2;
+  return GETHI_OK;
+}
+
+static int need_maps(joint_ctx *c)
+{
+  if (c->stage != 2) {
+    set_error("the maps are not merged yet (joint_gpu_merge)");
+    return GETHI_E_STATE;
+  }
+  return GETHI_OK;
+}
+
+extern "C" int joint_gpu_apply_beam(joint_ctx *c)
+{
+  if (!c) return GETHI_E_ARG;
+  int rc = need_maps(c);
+  if (rc) return rc;
+  JCK(cudaSetDevice(c->device));
+  if (c->p.dish_diameter <= 0) {
+    set_error("apply_beam needs dish_diameter > 0");
+    return GETHI_E_ARG;
+  }
+  if ((rc = ensure_sht(c))) return rc;
+  for (int c0 = 0; c0 < c->p.n_nu; c0 += c->chunk) {
+    const int nch = std::min(c->chunk, c->p.n_nu - c0);
+    std::vector<float> sg(c->chunk, 0.f);
+    for (int i = 0; i < nch; i++) {  // src/main_jt.c:224-226, src/healpix_extra.c:390-400
+      const double nu = 0.5 * (c->nu0[c0 + i] + c->nuf[c0 + i]);
+      const double fwhm = kPrefacFwhm / (nu * c->p.dish_diameter);
+      const double sigma = kFwhm2Sigma * fwhm;
+      sg[i] = (float)(sigma * sigma);
+    }
+    JCK(cudaMemcpyAsync(c->sig2, sg.data(), sizeof(float) * c->chunk, cudaMemcpyHostToDevice, c->stream));
+    float *m = c->maps + (long long)c0 * c->npix;
+    if ((rc = sht_analysis(c, m, nch, c->sig2))) return rc;
+    if ((rc = sht_synthesis(c, m, nch))) return rc;
+  }
+  return GETHI_OK;
+}
+
+extern "C" int joint_gpu_add_noise(joint_ctx *c)
+{
+  if (!c) return GETHI_E_ARG;
+  int rc = need_maps(c);
+  if (rc) return rc;
+  JCK(cudaSetDevice(c->device));
+  if (c->p.tsys <= 0) {
+    set_error("add_noise needs t_system > 0");
+    return GETHI_E_ARG;
+  }
+  const long long npix = c->npix;
+  if (c->p.rng == JOINT_RNG_PHILOX) {
+    noise_philox_kernel<<<grid_for(npix * c->p.n_nu), kThreads, 0, c->stream>>>(c->maps, c->s2, npix, c->p.n_nu,
+                                                                                 c->p.seed);
+    JCK(cudaGetLastError());
+    return GETHI_OK;
+  }
+  // mt_validation: the draws of src/main_jt.c:284-313, per emulated OpenMP thread t an
+  // MT19937 seeded seed + t over t's static block of channels
+  if (!c->noise_h) {
+    JCK(cudaMallocHost((void **)&c->noise_h, sizeof(double) * npix));
+    if ((rc = jalloc(&c->noise_d, npix))) return rc;
+  }
+  const int T = std::max(1, c->p.omp_threads_for_noise), n_nu = c->p.n_nu;
+  for (int t = 0; t < T; t++) {
+    int q = n_nu / T, r = n_nu % T, i0;
+    if (t < r) {
+      q++;
+      i0 = q * t;
+    } else
+      i0 = q * t + r;
+    MT19937 rng(c->p.seed + (unsigned)t);
+    for (int inu = i0; inu < i0 + q; inu++) {
+      const double dnu = c->nuf[inu] - c->nu0[inu];
+      const double s2 = c->fsky * npix * c->p.tsys * c->p.tsys / (kPrefacTnu * dnu * c->p.time_tot * c->p.n_dish);
+      JCK(cudaStreamSynchronize(c->stream));  // the staging buffer of the previous channel is free
+      for (long long i = 0; i < npix; i++) {
+        const double phase = 2 * M_PI * rng.uniform();
+        const double u = rng.uniform();
+        c->noise_h[i] = std::sqrt(-s2 * std::log(1 - u)) * std::cos(phase);
+      }
+      JCK(cudaMemcpyAsync(c->noise_d, c->noise_h, sizeof(double) * npix, cudaMemcpyHostToDevice, c->stream));
+      noise_add_kernel<<<grid_for(npix), kThreads, 0, c->stream>>>(c->maps + (long long)inu * npix, c->noise_d, npix);
+      JCK(cudaGetLastError());
+    }
+  }
+  JCK(cudaStreamSynchronize(c->stream));
+  return GETHI_OK;
+}
+
+extern "C" int joint_gpu_apply_mask(joint_ctx *c)
+{
+  if (!c) return GETHI_E_ARG;
+  int rc = need_maps(c);
+  if (rc) return rc;
+  JCK(cudaSetDevice(c->device));
+  if (!c->dmask) return GETHI_OK;  // "none"/"default": every pixel kept
+  mask_kernel<<<grid_for(c->npix * c->p.n_nu), kThreads, 0, c->stream>>>(c->maps, c->dmask, c->npix, c->p.n_nu);
+  JCK(cudaGetLastError());
+  return GETHI_OK;
+}
+
+extern "C" int joint_gpu_get_maps(joint_ctx *c, float *maps_out)
+{
+  if (!c || !maps_out) return GETHI_E_ARG;
+  int rc = need_maps(c);
+  if (rc) return rc;
+  JCK(cudaSetDevice(c->device));
+  JCK(cudaMemcpyAsync(maps_out, c->maps, sizeof(float) * c->npix * c->p.n_nu, cudaMemcpyDeviceToHost, c->stream));
+  JCK(cudaStreamSynchronize(c->stream));
+  return GETHI_OK;
+}
+
+extern "C" int joint_gpu_device_maps(const joint_ctx *c, const float **dmaps)
+{
+  if (!c || !dmaps) return GETHI_E_ARG;
+  *dmaps = c->maps;
+  return GETHI_OK;
+}
+
+extern "C" int joint_gpu_run(joint_ctx *c, float *maps_out)
+{
+  if (!c) return GETHI_E_ARG;
+  JCK(cudaSetDevice(c->device));
+  int rc;
+  record(c, 0);
+  if ((rc = joint_gpu_merge(c))) return rc;
+  record(c, 1);
+  if (c->p.dish_diameter > 0 && (rc = joint_gpu_apply_beam(c))) return rc;
+  record(c, 2);
+  if (c->p.tsys > 0 && (rc = joint_gpu_add_noise(c))) return rc;
+  record(c, 3);
+  if ((rc = joint_gpu_apply_mask(c))) return rc;
+  record(c, 4);
+  if (maps_out) {
+    if ((rc = joint_gpu_get_maps(c, maps_out))) return rc;
+  } else {
+    JCK(cudaStreamSynchronize(c->stream));
+  }
+  for (int i = 0; i < 4; i++) cudaEventElapsedTime(&c->times[i], c->ev[i], c->ev[i + 1]);
+  return GETHI_OK;
+}
+
+extern "C" int joint_gpu_stage_times(const joint_ctx *c, float *ms4)
+{
+  if (!c || !ms4) return GETHI_E_ARG;
+  for (int i = 0; i < 4; i++) ms4[i] = c->times[i];
+  return GETHI_OK;
+}
+
+static int sht_api(joint_ctx *c, const float *in, int n_maps, float *out, bool analysis)
+{
+  if (!c || !in || !out || n_maps < 1) return GETHI_E_ARG;
+  JCK(cudaSetDevice(c->device));
+  int rc = ensure_sht(c);
+  if (rc) return rc;
+  const long long nalm = m_offset(c->lmax + 1, c->lmax);
+  if (!c->tmp_maps) {
+    if ((rc = jalloc(&c->tmp_maps, (size_t)c->chunk * c->npix)) || (rc = jalloc(&c->alm_hp, (size_t)c->chunk * nalm)))
+      return rc;
+  }
+  for (int c0 = 0; c0 < n_maps; c0 += c->chunk) {
+    const int nch = std::min(c->chunk, n_maps - c0);
+    if (analysis) {
+      JCK(cudaMemcpyAsync(c->tmp_maps, in + (long long)c0 * c->npix, sizeof(float) * nch * c->npix,
+                          cudaMemcpyHostToDevice, c->stream));
+      if ((rc = sht_analysis(c, c->tmp_maps, nch, nullptr))) return rc;
+      alm_to_healpix_kernel<<<grid_for(nalm * nch), kThreads, 0, c->stream>>>(c->alm, c->alm_hp, c->lmax, c->N2, nch,
+                                                                              nalm);
+      JCK(cudaGetLastError());
+      JCK(cudaMemcpyAsync(out + 2 * (long long)c0 * nalm, c->alm_hp, sizeof(float2) * nch * nalm,
+                          cudaMemcpyDeviceToHost, c->stream));
+    } else {
+      JCK(cudaMemcpyAsync(c->alm_hp, in + 2 * (long long)c0 * nalm, sizeof(float2) * nch * nalm,
+                          cudaMemcpyHostToDevice, c->stream));
+      alm_from_healpix_kernel<<<grid_for(nalm * nch), kThreads, 0, c->stream>>>(c->alm_hp, c->alm, c->lmax, c->N2,
+                                                                                nch, nalm);
+      JCK(cudaGetLastError());
+      if ((rc = sht_synthesis(c, c->tmp_maps, nch))) return rc;
+      JCK(cudaMemcpyAsync(out + (long long)c0 * c->npix, c->tmp_maps, sizeof(float) * nch * c->npix,
+                          cudaMemcpyDeviceToHost, c->stream));
+    }
+    JCK(cudaStreamSynchronize(c->stream));
+  }
+  return GETHI_OK;
+}
+
+extern "C" int joint_gpu_map2alm(joint_ctx *c, const float *maps, int n_maps, float *alms)
+{
+  return sht_api(c, maps, n_maps, alms, true);
+}
+
+extern "C" int joint_gpu_alm2map(joint_ctx *c, const float *alms, int n_maps, float *maps)
+{
+  return sht_api(c, alms, n_maps, maps, false);
+}

@@ -111,6 +111,12 @@ int gethi_gpu_get_hi(gethi_ctx *ctx);
 /* mk_T_maps (src/pixelize.c:303-417): maps[n_nu][12 n_side^2] in mK.
  * maps_out may be NULL (maps stay on the device). */
 int gethi_gpu_make_maps(gethi_ctx *ctx, float *maps_out);
+/* Device pointers of the maps the last make_maps / run left on the context's
+ * device ([n_nu][12 n_side^2] float32; maps_ps NULL without point sources),
+ * valid until the next realisation or free.  No counterpart in the reference,
+ * whose JoinT reads the maps back from FITS files (src/main_jt.c:98-200); this
+ * hands them to joint_gpu_add_maps_device without a host round trip. */
+int gethi_gpu_device_maps(const gethi_ctx *ctx, const float **maps, const float **maps_ps);
 /* write_maps (src/io_gh.c:109-131): <prefix>_%03d.fits, RING, column T [mK]. */
 int gethi_gpu_write_maps(const gethi_ctx *ctx, const float *maps);
 /* All stages; get_HI is fused into the projection (no separate HBM pass). */

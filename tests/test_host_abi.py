@@ -20,15 +20,18 @@ def gh():
 
 
 def header_symbols():
-    src = open(os.path.join(REPO, "include", "gethi_gpu.h")).read()
-    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(gethi_\w+)\s*\(", src)))
+    syms = set()
+    for h in sorted(os.listdir(os.path.join(REPO, "include"))):
+        src = open(os.path.join(REPO, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        syms |= set(re.findall(r"\b((?:gethi|joint)_\w+)\s*\(", src))
+    return sorted(syms)
 
 
 def test_library_exports_every_declared_symbol(gh):
     lib = ctypes.CDLL(gh.gethi.LIB_PATH)
     syms = header_symbols()
-    assert len(syms) >= 19
+    assert len(syms) >= 40 and "joint_gpu_apply_beam" in syms
     for s in syms:
         assert hasattr(lib, s), s
 
