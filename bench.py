@@ -349,6 +349,135 @@ def bench_ensemble(args):
         torch.distributed.destroy_process_group()
 
 
+JOINT = dict(n_side=512, n_nu=150, zmin=0.3, zmax=2.0, dish_diameter=30.0, n_dish=64, tsys=25000.0,
+             time_tot=10000.0, seed=6001, b_cut_deg=10.0)
+
+
+def joint_workload():
+    E = JOINT
+    edges = np.linspace(NU21 / (1 + E["zmax"]), NU21 / (1 + E["zmin"]), E["n_nu"] + 1)
+    nside = E["n_side"]
+    npix = 12 * nside * nside
+    # galactic-plane cut |b| < b_cut (the RING pixel heights: z = cos(theta) per ring)
+    z = np.empty(npix)
+    ncap = 2 * nside * (nside - 1)
+    for i in range(1, 4 * nside):
+        north = i if i <= 2 * nside else 4 * nside - i
+        if north < nside:
+            zz, nph, first = 1 - north * north / (3.0 * nside * nside), 4 * north, 2 * north * (north - 1)
+        else:
+            zz, nph, first = (2 * nside - north) * 2.0 / (3 * nside), 4 * nside, ncap + (north - nside) * 4 * nside
+        if north != i:
+            zz, first = -zz, npix - nph - first
+        z[first:first + nph] = zz
+    mask = (np.abs(z) >= np.sin(np.radians(E["b_cut_deg"]))).astype(np.int32)
+    return edges[:-1], edges[1:], mask
+
+
+def bench_joint(args):
+    """The JoinT combination of a c2-sized set of maps (Nside 512 x 150 channels):
+    two components (HI and a foreground) summed, beam of a 30 m dish through the
+    spherical harmonic transform (lmax 1535), Philox noise, |b| < 10 deg mask.
+    value = map pixels (channels x 12 Nside^2) per second with the components
+    resident in HBM; e2e = the same through the C ABI with the components copied in
+    from pinned host memory and the maps copied back every step."""
+    import torch
+
+    from crime_gb300 import joint as jt
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    E = JOINT
+    nu0, nuf, mask = joint_workload()
+    nside, n_nu = E["n_side"], E["n_nu"]
+    npix = 12 * nside * nside
+    g = torch.Generator(device="cuda").manual_seed(E["seed"] + rank)
+    comp = [torch.randn((n_nu, npix), device="cuda", generator=g) * s for s in (0.1, 1000.0)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    j = jt.JoinT(nside, nu0, nuf, seed=E["seed"] + rank, dish_diameter=E["dish_diameter"], n_dish=E["n_dish"],
+                 tsys=E["tsys"], time_tot=E["time_tot"], mask=mask, device=local)
+
+    def step():
+        for c in comp:
+            j.add_maps_device(c.data_ptr(), nside)
+        j.run(copy_out=False)
+
+    step()  # builds the Legendre table (once per context)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    stages = np.zeros(4)
+    with ClockSampler(local) as clk:
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        start.record()
+        for _ in range(args.steps):
+            step()
+            st = j.stage_times()
+            stages += [st["merge"], st["beam"], st["noise"], st["mask"]]
+        end.record()
+        torch.cuda.synchronize()
+    ms = max_over_ranks(start.elapsed_time(end), ws)
+    units = float(npix) * n_nu
+    # end to end: pinned host components in, maps out
+    host = [c.cpu().pin_memory() for c in comp]
+    out = torch.empty((n_nu, npix), dtype=torch.float32, pin_memory=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for h in host:
+            jt.lib().joint_gpu_add_maps(j._ctx, h.data_ptr(), nside, 1.0)
+        jt._check(jt.lib().joint_gpu_run(j._ctx, out.data_ptr()))
+    e2e_ms = max_over_ranks(1e3 * (time.perf_counter() - t0), ws)
+    assert np.isfinite(out.numpy()).all()
+    chunks = -(-n_nu // 64)
+    line = {
+        "metric": "JoinT map combination throughput (map pixels/s): Nside %d x %d channels, beam + noise + mask" % (
+            nside, n_nu),
+        "value": whole_job_rate(units, args.steps, ws, ms), "unit": "pixels/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic (Gaussian component maps, seeded)",
+        "config": {"workload": "joint: Nside %d, %d channels over z %.1f-%.1f, 2 components, %g m dish "
+                               "(lmax %d), Philox noise (t_sys %g mK, %g h, %d dishes), |b| < %g deg mask" % (
+                                   nside, n_nu, E["zmin"], E["zmax"], E["dish_diameter"], 3 * nside - 1, E["tsys"],
+                                   E["time_tot"], E["n_dish"], E["b_cut_deg"]),
+                   "fsky": j.fsky, "legendre_table_gb": round(4.0 * (3 * nside) * (3 * nside + 1) / 2 * 2 * nside / 1e9, 2),
+                   "setup_s_incl_legendre_table": round(setup_s, 3),
+                   "l2": "inputs larger than L2 (maps %.1f GB, Legendre table above)" % (4 * units / 1e9)},
+        "stage_ms": dict(zip(("merge", "beam", "noise", "mask"), np.round(stages / args.steps, 3).tolist())),
+        "e2e": {"value": whole_job_rate(units, args.steps, ws, e2e_ms), "unit": "pixels/s",
+                "h2d_bytes_per_step": int(4 * units * len(comp)), "d2h_bytes_per_step": int(4 * units)},
+        "gpu_launches": args.steps * (len(comp) + 4 * chunks + 2),
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_joint()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    j.close()
+
+
+def cpu_baseline_joint(nside=64, n_nu=16):
+    """The oracle's JoinT (FP64 transforms, one host thread) on a bounded sample:
+    Nside 64, 16 channels, the same beam, noise and mask law."""
+    from oracle import orc
+    E = JOINT
+    edges = np.linspace(NU21 / (1 + E["zmax"]), NU21 / (1 + E["zmin"]), n_nu + 1)
+    rng = np.random.default_rng(1)
+    npix = 12 * nside * nside
+    comps = [(rng.standard_normal((n_nu, npix)).astype(np.float32), None) for _ in range(2)]
+    mask = (rng.random(npix) > 0.17).astype(np.int32)
+    t0 = time.perf_counter()
+    orc.joint(comps, nside, nside, edges[:-1], edges[1:], dish=E["dish_diameter"] / 8, n_dish=E["n_dish"],
+              tsys=E["tsys"], time_tot=E["time_tot"], seed=1, mask=mask)
+    dt = time.perf_counter() - t0
+    return {"value": npix * n_nu / dt, "unit": "pixels/s", "cores": 1, "kind": "port",
+            "sample": "oracle JoinT (merge, FP64 map2alm/alm2map beam, MT noise, mask) at Nside %d x %d channels, "
+                      "%.1f s" % (nside, n_nu, dt)}
+
+
 def bench_ours(args):
     import torch
 
@@ -555,7 +684,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS) + ["c3"])
+    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS) + ["c3", "joint"])
     ap.add_argument("--cpu-sample", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fft-compare", action="store_true",
@@ -565,6 +694,8 @@ def main():
         bench_reference(args)
     elif args.config == "c3":
         bench_ensemble(args)
+    elif args.config == "joint":
+        bench_joint(args)
     else:
         bench_ours(args)
 

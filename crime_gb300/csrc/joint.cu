@@ -16,8 +16,10 @@
 //           batch; the same buffers then hold the synthesised north and south
 //           ring sums
 //   alm     per m, [parity][l'][2 c] float
-// A transform is, per batch of channels: ring DFTs (one CTA per ring pair,
-// direct sums over the ring's pixels with shared-memory twiddles), the
+// A transform is, per batch of channels: ring DFTs (one CTA per ring pair: the
+// 2 nside + 1 equatorial rings, 4 nside pixels each, by a shared-memory radix-2
+// FFT of north + i south; the polar rings, 4 i pixels, by direct sums with
+// shared-memory twiddles), the
 // Legendre sums as FP32 GEMMs per (m, parity) on the CUDA cores (the beam
 // factor exp(-l(l+1) sigma_c^2 / 2) and the quadrature weight 4 pi / npix
 // applied in the epilogue), the transposed GEMMs back, and the inverse ring
@@ -47,7 +49,10 @@ struct RingPair {
   long long first_n, first_s;  // first pixel of the north ring and of its south mirror
   int nph;                     // pixels per ring
   int shifted;                 // first pixel at longitude pi / nph (else 0)
-  long long tw_off;            // offset of this ring length's twiddles (2 i (i-1), nph = 4 i)
+  long long tw_off;            // offset of the ring's twiddles e^{2 pi i t/nph} in the power-of-two table
+  int bm;                      // polar rings: Bluestein FFT size, the power of two >= 2 nph - 1
+  int pad_;
+  long long b_off;             // polar rings: offset of the chirp spectrum in the Bluestein table
 };
 
 // ---------------------------------------------------------------------------
@@ -179,92 +184,134 @@ __global__ void lambda_kernel(const double *__restrict__ ring_z, const double *_
   }
 }
 
-template <int CB> struct VecT;
-template <> struct VecT<2> { typedef float2 T; };
-template <> struct VecT<4> { typedef float4 T; };
-__device__ __forceinline__ float vget(const float2 &v, int i) { return i ? v.y : v.x; }
-__device__ __forceinline__ float vget(const float4 &v, int i) { return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w; }
-__device__ __forceinline__ void vset(float2 &v, int i, float x) { if (i) v.y = x; else v.x = x; }
-__device__ __forceinline__ void vset(float4 &v, int i, float x)
+// Q_k of ring s (0 north, 1 south) of pair q for CB channels (see fold_ring_sums)
+template <int CB>
+__device__ __forceinline__ void fold_one(const float *__restrict__ G, const RingPair &rp, int q, int k, int lmax, int R,
+                                         int N2, int nch, int cb0, float2 *acc)
 {
-  if (i == 0) v.x = x; else if (i == 1) v.y = x; else if (i == 2) v.z = x; else v.w = x;
+  const int n = rp.nph, half = n / 2;
+#pragma unroll
+  for (int b = 0; b < CB; b++) acc[b] = make_float2(0.f, 0.f);
+  for (int pass = 0; pass < 2; pass++) {
+    if (pass == 1 && (k == 0 || k == half)) break;
+    const float sg = pass ? -1.f : 1.f;
+    for (int m = pass ? n - k : k; m <= lmax; m += n) {
+      float2 ph = make_float2(1.f, 0.f);
+      if (rp.shifted) {
+        float sn, cs;
+        sincospif((float)(m % (2 * n)) / (float)n, &sn, &cs);
+        ph = make_float2(cs, sn);
+      }
+      const float cm = m ? 2.f : 1.f;
+#pragma unroll
+      for (int b = 0; b < CB; b++) {
+        if (cb0 + b >= nch) continue;
+        const float2 g = *reinterpret_cast<const float2 *>(G + ((long long)m * R + q) * N2 + 2 * (cb0 + b));
+        acc[b].x += cm * (g.x * ph.x - g.y * ph.y);
+        acc[b].y += sg * cm * (g.x * ph.y + g.y * ph.x);
+      }
+    }
+  }
 }
 
-// Ring analysis of ring pair q for CB channels: D_k = sum_j x_j e^{-2 pi i jk/n}
-// (k <= n/2; the rest by conjugate symmetry), then for m = 0 .. lmax the
-// phase-shifted sums F_m = e^{-i m phi0} D_{m mod n} of both rings combined
-// as E = F_north + F_south and O = F_north - F_south.
+// Q[s][k][b], k = 0 .. n/2, of ring s (0 north, 1 south) of pair q: the sums
+// c_m G_m e^{i m phi0} over m = k mod n, plus the conjugates of those over
+// m = n - k mod n (0 < k < n/2), so that map_j = sum_k Re(Q_k e^{2 pi i jk/n})
 template <int CB>
-__global__ __launch_bounds__(kThreads) void ring_analysis_kernel(const float *__restrict__ maps, long long npix,
-                                                                 int nch, const RingPair *__restrict__ rings,
-                                                                 const float2 *__restrict__ tw_all, int lmax, int R,
-                                                                 int N2, float *__restrict__ E, float *__restrict__ O)
+__device__ void fold_ring_sums(const float *__restrict__ Gn, const float *__restrict__ Gs, const RingPair &rp, int q,
+                               bool eq, int lmax, int R, int N2, int nch, int cb0, float2 *Q)
 {
-  typedef typename VecT<CB>::T VT;
+  const int half = rp.nph / 2;
+  for (int t = threadIdx.x; t < 2 * (half + 1); t += blockDim.x) {
+    const int s = t / (half + 1), k = t - s * (half + 1);
+    float2 acc[CB];
+    if (s == 0 || !eq) {
+      fold_one<CB>(s ? Gs : Gn, rp, q, k, lmax, R, N2, nch, cb0, acc);
+    } else {
+#pragma unroll
+      for (int b = 0; b < CB; b++) acc[b] = make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int b = 0; b < CB; b++) Q[t * CB + b] = acc[b];
+  }
+}
+
+// In-place radix-2 decimation-in-time FFT of CB sequences of length n = 2^logn
+// stored one after the other in z in bit-reversed order; sign -1 for
+// e^{-2 pi i jk/n}, +1 for e^{+2 pi i jk/n}; tw[t] = e^{2 pi i t/n}.
+template <int CB>
+__device__ void smem_fft(float2 *z, const float2 *tw, int n, int logn, float sign)
+{
+  for (int st = 0; st < logn; st++) {
+    const int h = 1 << st, step = n >> (st + 1);
+    for (int t = threadIdx.x; t < CB * (n >> 1); t += blockDim.x) {
+      const int b = t >> (logn - 1), u = t & ((n >> 1) - 1);
+      const int jj = u & (h - 1), i0 = ((u >> st) << (st + 1)) + jj;
+      float2 w = tw[jj * step];
+      w.y *= sign;
+      float2 *zb = z + b * n;
+      const float2 a = zb[i0], c = zb[i0 + h];
+      const float2 v = make_float2(c.x * w.x - c.y * w.y, c.x * w.y + c.y * w.x);
+      zb[i0] = make_float2(a.x + v.x, a.y + v.y);
+      zb[i0 + h] = make_float2(a.x - v.x, a.y - v.y);
+    }
+    __syncthreads();
+  }
+}
+
+// Ring analysis of the equatorial ring pairs (q >= nside - 1: n = 4 nside, a power
+// of two) by one complex FFT per channel of z_j = north_j + i south_j:
+// D_north,k = (Z_k + conj Z_{n-k}) / 2, D_south,k = (Z_k - conj Z_{n-k}) / 2i;
+// then for m = 0 .. lmax the phase-shifted sums F_m = e^{-i m phi0} D_{m mod n}
+// (D_{n-k} = conj D_k) of both rings combined as E = F_north + F_south and
+// O = F_north - F_south.
+template <int CB>
+__global__ __launch_bounds__(kThreads) void ring_analysis_fft_kernel(const float *__restrict__ maps, long long npix,
+                                                                     int nch, const RingPair *__restrict__ rings,
+                                                                     const float2 *__restrict__ tw_all, int lmax,
+                                                                     int R, int N2, int q0, float *__restrict__ E,
+                                                                     float *__restrict__ O)
+{
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int q = blockIdx.x, cb0 = blockIdx.y * CB;
+  const int q = q0 + blockIdx.x, cb0 = blockIdx.y * CB;
   const RingPair rp = rings[q];
-  const int n = rp.nph, half = n / 2;
+  const int n = rp.nph, half = n / 2, logn = __ffs(n) - 1;
   const bool eq = (q == R - 1);
-  VT *x = reinterpret_cast<VT *>(smem_raw);
-  float2 *tw = reinterpret_cast<float2 *>(x + 2 * n);
-  float2 *D = tw + n;  // [2][half + 1][CB]
+  float2 *z = reinterpret_cast<float2 *>(smem_raw);  // [CB][n]
+  float2 *tw = z + CB * n;
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
     tw[j] = tw_all[rp.tw_off + j];
-#pragma unroll
-    for (int s = 0; s < 2; s++) {
-      VT v;
-#pragma unroll
-      for (int b = 0; b < CB; b++) {
-        const int c = cb0 + b;
-        float val = 0.f;
-        if (c < nch && (s == 0 || !eq)) val = maps[(long long)c * npix + (s ? rp.first_s : rp.first_n) + j];
-        vset(v, b, val);
-      }
-      x[s * n + j] = v;
-    }
-  }
-  __syncthreads();
-  for (int k = threadIdx.x; k <= half; k += blockDim.x) {
-    float2 an[CB], as[CB];
-#pragma unroll
-    for (int b = 0; b < CB; b++) an[b] = as[b] = make_float2(0.f, 0.f);
-    int idx = 0;
-    for (int j = 0; j < n; j++) {
-      const float2 w = tw[idx];
-      const VT xn = x[j], xs = x[n + j];
-#pragma unroll
-      for (int b = 0; b < CB; b++) {
-        an[b].x = fmaf(vget(xn, b), w.x, an[b].x);
-        an[b].y = fmaf(-vget(xn, b), w.y, an[b].y);
-        as[b].x = fmaf(vget(xs, b), w.x, as[b].x);
-        as[b].y = fmaf(-vget(xs, b), w.y, as[b].y);
-      }
-      idx += k;
-      if (idx >= n) idx -= n;
-    }
+    const int jr = (int)(__brev((unsigned)j) >> (32 - logn));
 #pragma unroll
     for (int b = 0; b < CB; b++) {
-      D[k * CB + b] = an[b];
-      D[(half + 1 + k) * CB + b] = as[b];
+      const int c = cb0 + b;
+      float xn = 0.f, xs = 0.f;
+      if (c < nch) {
+        xn = maps[(long long)c * npix + rp.first_n + j];
+        if (!eq) xs = maps[(long long)c * npix + rp.first_s + j];
+      }
+      z[b * n + jr] = make_float2(xn, xs);
     }
   }
   __syncthreads();
+  smem_fft<CB>(z, tw, n, logn, -1.f);
   for (int m = threadIdx.x; m <= lmax; m += blockDim.x) {
     int k = m % n;
     const bool cj = k > half;
     if (cj) k = n - k;
     float2 ph = make_float2(1.f, 0.f);
     if (rp.shifted) {
-      float s, c;
-      sincospif((float)(m % (2 * n)) / (float)n, &s, &c);
-      ph = make_float2(c, -s);
+      float sn, cs;
+      sincospif((float)(m % (2 * n)) / (float)n, &sn, &cs);
+      ph = make_float2(cs, -sn);
     }
 #pragma unroll
     for (int b = 0; b < CB; b++) {
       const int c = cb0 + b;
       if (c >= nch) continue;
-      float2 dn = D[k * CB + b], ds = D[(half + 1 + k) * CB + b];
+      const float2 zk = z[b * n + k], zm = z[b * n + ((n - k) & (n - 1))];
+      float2 dn = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+      float2 ds = eq ? make_float2(0.f, 0.f) : make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
       if (cj) {
         dn.y = -dn.y;
         ds.y = -ds.y;
@@ -277,137 +324,339 @@ __global__ __launch_bounds__(kThreads) void ring_analysis_kernel(const float *__
   }
 }
 
-// Ring synthesis: for each ring of pair q, fold c_m G_m e^{i m phi0} (c_0 = 1,
-// c_m = 2) into the frequencies k = m mod n, pair k with n - k (real output),
-// and sum map_j = sum_k Re(Q_k e^{2 pi i jk/n}).
+// Ring synthesis of the equatorial ring pairs: the Hermitian spectra H of both
+// rings (H_k = Q_k / 2, H_{n-k} = conj Q_k / 2, H_0 = Re Q_0, H_{n/2} = Re Q_{n/2})
+// in one complex inverse FFT of H_north + i H_south, whose real and imaginary
+// parts are the two rings' pixels.
 template <int CB>
-__global__ __launch_bounds__(kThreads) void ring_synthesis_kernel(const float *__restrict__ Gn,
-                                                                  const float *__restrict__ Gs,
-                                                                  const RingPair *__restrict__ rings,
-                                                                  const float2 *__restrict__ tw_all, int lmax, int R,
-                                                                  int N2, int nch, float *__restrict__ maps,
-                                                                  long long npix)
+__global__ __launch_bounds__(kThreads) void ring_synthesis_fft_kernel(const float *__restrict__ Gn,
+                                                                      const float *__restrict__ Gs,
+                                                                      const RingPair *__restrict__ rings,
+                                                                      const float2 *__restrict__ tw_all, int lmax,
+                                                                      int R, int N2, int nch, int q0,
+                                                                      float *__restrict__ maps, long long npix)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int q = blockIdx.x, cb0 = blockIdx.y * CB;
+  const int q = q0 + blockIdx.x, cb0 = blockIdx.y * CB;
   const RingPair rp = rings[q];
-  const int n = rp.nph, half = n / 2;
+  const int n = rp.nph, half = n / 2, logn = __ffs(n) - 1;
   const bool eq = (q == R - 1);
   float2 *tw = reinterpret_cast<float2 *>(smem_raw);
-  float2 *Q = tw + n;  // [2][half + 1][CB]
+  float2 *Q = tw + n;                   // [2][half + 1][CB]
+  float2 *z = Q + 2 * (half + 1) * CB;  // [CB][n]
   for (int j = threadIdx.x; j < n; j += blockDim.x) tw[j] = tw_all[rp.tw_off + j];
-  for (int t = threadIdx.x; t < 2 * (half + 1); t += blockDim.x) {
-    const int s = t / (half + 1), k = t - s * (half + 1);
-    const float *G = s ? Gs : Gn;
-    float2 acc[CB];
+  fold_ring_sums<CB>(Gn, Gs, rp, q, eq, lmax, R, N2, nch, cb0, Q);
+  __syncthreads();
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const int kk = k <= half ? k : n - k, kr = (int)(__brev((unsigned)k) >> (32 - logn));
 #pragma unroll
-    for (int b = 0; b < CB; b++) acc[b] = make_float2(0.f, 0.f);
-    if (s == 0 || !eq) {
-      for (int pass = 0; pass < 2; pass++) {
-        if (pass == 1 && (k == 0 || k == half)) break;
-        const float sg = pass ? -1.f : 1.f;  // pass 1: conjugate of the n - k terms
-        for (int m = pass ? n - k : k; m <= lmax; m += n) {
-          float2 ph = make_float2(1.f, 0.f);
-          if (rp.shifted) {
-            float sn, cs;
-            sincospif((float)(m % (2 * n)) / (float)n, &sn, &cs);
-            ph = make_float2(cs, sn);
-          }
-          const float cm = m ? 2.f : 1.f;
-#pragma unroll
-          for (int b = 0; b < CB; b++) {
-            if (cb0 + b >= nch) continue;
-            const float2 g = *reinterpret_cast<const float2 *>(G + ((long long)m * R + q) * N2 + 2 * (cb0 + b));
-            acc[b].x += cm * (g.x * ph.x - g.y * ph.y);
-            acc[b].y += sg * cm * (g.x * ph.y + g.y * ph.x);
-          }
-        }
+    for (int b = 0; b < CB; b++) {
+      float2 hn = Q[kk * CB + b], hs = eq ? make_float2(0.f, 0.f) : Q[(half + 1 + kk) * CB + b];
+      if (k == 0 || k == half) {
+        hn.y = 0.f;
+        hs.y = 0.f;
+      } else {
+        hn = make_float2(0.5f * hn.x, 0.5f * (k < half ? hn.y : -hn.y));
+        hs = make_float2(0.5f * hs.x, 0.5f * (k < half ? hs.y : -hs.y));
       }
+      z[b * n + kr] = make_float2(hn.x - hs.y, hn.y + hs.x);
     }
-#pragma unroll
-    for (int b = 0; b < CB; b++) Q[t * CB + b] = acc[b];
   }
   __syncthreads();
+  smem_fft<CB>(z, tw, n, logn, 1.f);
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
-    float vn[CB], vs[CB];
-#pragma unroll
-    for (int b = 0; b < CB; b++) vn[b] = vs[b] = 0.f;
-    int idx = 0;
-    for (int k = 0; k <= half; k++) {
-      const float2 w = tw[idx];
-#pragma unroll
-      for (int b = 0; b < CB; b++) {
-        const float2 a = Q[k * CB + b], c = Q[(half + 1 + k) * CB + b];
-        vn[b] = fmaf(a.x, w.x, fmaf(-a.y, w.y, vn[b]));
-        vs[b] = fmaf(c.x, w.x, fmaf(-c.y, w.y, vs[b]));
-      }
-      idx += j;
-      if (idx >= n) idx -= n;
-    }
 #pragma unroll
     for (int b = 0; b < CB; b++) {
       const int c = cb0 + b;
       if (c >= nch) continue;
-      maps[(long long)c * npix + rp.first_n + j] = vn[b];
-      if (!eq) maps[(long long)c * npix + rp.first_s + j] = vs[b];
+      const float2 v = z[b * n + j];
+      maps[(long long)c * npix + rp.first_n + j] = v.x;
+      if (!eq) maps[(long long)c * npix + rp.first_s + j] = v.y;
     }
   }
 }
 
-constexpr int BM = 64, BN = 64, BK = 16;
 
-// Legendre analysis, one 64 x 64 tile of one (m, parity) per CTA:
-// alm[l'][col] = scale(l, col) sum_q lam[l'][q] EO[q][col]
-__global__ __launch_bounds__(kThreads) void legendre_analysis_kernel(const float *__restrict__ lam,
-                                                                     const float *__restrict__ E,
-                                                                     const float *__restrict__ O,
-                                                                     float *__restrict__ alm,
-                                                                     const int4 *__restrict__ tasks, int R, int lmax,
-                                                                     int N2, float w, const float *__restrict__ sig2)
+// In-place radix-2 decimation-in-frequency FFT (natural order in, bit-reversed
+// out) of CB sequences of length n = 2^logn; tw[t] = e^{2 pi i t/n}.
+template <int CB>
+__device__ void smem_fft_dif(float2 *z, const float2 *tw, int n, int logn, float sign)
 {
-  __shared__ __align__(16) float As[BK][BM + 4];
-  __shared__ __align__(16) float Bs[BK][BN];
+  for (int st = logn - 1; st >= 0; st--) {
+    const int h = 1 << st, step = n >> (st + 1);
+    for (int t = threadIdx.x; t < CB * (n >> 1); t += blockDim.x) {
+      const int b = t >> (logn - 1), u = t & ((n >> 1) - 1);
+      const int jj = u & (h - 1), i0 = ((u >> st) << (st + 1)) + jj;
+      float2 w = tw[jj * step];
+      w.y *= sign;
+      float2 *zb = z + b * n;
+      const float2 a = zb[i0], c = zb[i0 + h];
+      const float2 d = make_float2(a.x - c.x, a.y - c.y);
+      zb[i0] = make_float2(a.x + c.x, a.y + c.y);
+      zb[i0 + h] = make_float2(d.x * w.x - d.y * w.y, d.x * w.y + d.y * w.x);
+    }
+    __syncthreads();
+  }
+}
+
+// e^{-i pi j^2 / n}, the Bluestein chirp, with j^2 reduced exactly modulo 2n
+__device__ __forceinline__ float2 chirp(int j, int n)
+{
+  float sn, cs;
+  sincospif((float)((long long)j * j % (2 * n)) / (float)n, &sn, &cs);
+  return make_float2(cs, -sn);
+}
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+
+// Bluestein DFT of the CB sequences a[b][j], j < n (zero beyond, length M):
+// Z_k = c_k (a c) (*) conj(c), the convolution by a DIF FFT, the product with
+// the precomputed spectrum of conj(c) (bit-reversed order) and a DIT inverse
+// FFT; on return a[b][k] = Z_k for k < n.
+template <int CB>
+__device__ void bluestein(float2 *a, const float2 *Bt, const float2 *tw, int n, int M, int logM)
+{
+  for (int t = threadIdx.x; t < CB * n; t += blockDim.x) {
+    const int b = t / n, j = t - b * n;
+    a[b * M + j] = cmul(a[b * M + j], chirp(j, n));
+  }
+  __syncthreads();
+  smem_fft_dif<CB>(a, tw, M, logM, -1.f);
+  for (int t = threadIdx.x; t < CB * M; t += blockDim.x) a[t] = cmul(a[t], Bt[t & (M - 1)]);
+  __syncthreads();
+  smem_fft<CB>(a, tw, M, logM, 1.f);
+  const float inv = 1.f / (float)M;
+  for (int t = threadIdx.x; t < CB * n; t += blockDim.x) {
+    const int b = t / n, k = t - b * n;
+    const float2 v = cmul(a[b * M + k], chirp(k, n));
+    a[b * M + k] = make_float2(v.x * inv, v.y * inv);
+  }
+  __syncthreads();
+}
+
+// Ring analysis of the polar ring pairs (q < nside - 1, n = 4 (q + 1) pixels)
+// by a Bluestein DFT of z_j = north_j + i south_j; then E and O as in
+// ring_analysis_fft_kernel.
+template <int CB>
+__global__ __launch_bounds__(kThreads) void ring_analysis_bluestein_kernel(
+    const float *__restrict__ maps, long long npix, int nch, const RingPair *__restrict__ rings,
+    const float2 *__restrict__ tw2, const float2 *__restrict__ btab, int lmax, int R, int N2, float *__restrict__ E,
+    float *__restrict__ O)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int q = blockIdx.x, cb0 = blockIdx.y * CB;
+  const RingPair rp = rings[q];
+  const int n = rp.nph, half = n / 2, M = rp.bm, logM = __ffs(M) - 1;
+  float2 *a = reinterpret_cast<float2 *>(smem_raw);  // [CB][M]
+  float2 *Bt = a + CB * M, *tw = Bt + M;
+  for (int t = threadIdx.x; t < M; t += blockDim.x) {
+    tw[t] = tw2[M + t];
+    Bt[t] = btab[rp.b_off + t];
+  }
+  for (int t = threadIdx.x; t < CB * M; t += blockDim.x) {
+    const int b = t / M, j = t - b * M, c = cb0 + b;
+    float2 v = make_float2(0.f, 0.f);
+    if (j < n && c < nch)
+      v = make_float2(maps[(long long)c * npix + rp.first_n + j], maps[(long long)c * npix + rp.first_s + j]);
+    a[t] = v;
+  }
+  __syncthreads();
+  bluestein<CB>(a, Bt, tw, n, M, logM);
+  for (int m = threadIdx.x; m <= lmax; m += blockDim.x) {
+    int k = m % n;
+    const bool cj = k > half;
+    if (cj) k = n - k;
+    float sn, cs;
+    sincospif((float)(m % (2 * n)) / (float)n, &sn, &cs);  // polar rings: phi0 = pi / n
+    const float2 ph = make_float2(cs, -sn);
+#pragma unroll
+    for (int b = 0; b < CB; b++) {
+      const int c = cb0 + b;
+      if (c >= nch) continue;
+      const float2 zk = a[b * M + k], zm = a[b * M + (k ? n - k : 0)];
+      float2 dn = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+      float2 ds = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
+      if (cj) {
+        dn.y = -dn.y;
+        ds.y = -ds.y;
+      }
+      const float2 e = make_float2(dn.x + ds.x, dn.y + ds.y), o = make_float2(dn.x - ds.x, dn.y - ds.y);
+      const long long base = ((long long)m * R + q) * N2 + 2 * c;
+      *reinterpret_cast<float2 *>(E + base) = cmul(e, ph);
+      *reinterpret_cast<float2 *>(O + base) = cmul(o, ph);
+    }
+  }
+}
+
+// Ring synthesis of the polar ring pairs: the Hermitian-packed spectra
+// H_north + i H_south (as in ring_synthesis_fft_kernel) inverse-transformed as
+// conj(DFT(conj(.))) with the Bluestein DFT.
+template <int CB>
+__global__ __launch_bounds__(kThreads) void ring_synthesis_bluestein_kernel(
+    const float *__restrict__ Gn, const float *__restrict__ Gs, const RingPair *__restrict__ rings,
+    const float2 *__restrict__ tw2, const float2 *__restrict__ btab, int lmax, int R, int N2, int nch,
+    float *__restrict__ maps, long long npix)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int q = blockIdx.x, cb0 = blockIdx.y * CB;
+  const RingPair rp = rings[q];
+  const int n = rp.nph, half = n / 2, M = rp.bm, logM = __ffs(M) - 1;
+  float2 *a = reinterpret_cast<float2 *>(smem_raw);  // [CB][M]
+  float2 *Bt = a + CB * M, *tw = Bt + M;
+  for (int t = threadIdx.x; t < M; t += blockDim.x) {
+    tw[t] = tw2[M + t];
+    Bt[t] = btab[rp.b_off + t];
+  }
+  for (int t = threadIdx.x; t < CB * M; t += blockDim.x) a[t] = make_float2(0.f, 0.f);
+  __syncthreads();
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const int kk = k <= half ? k : n - k;
+    float2 qn[CB], qs[CB];
+    fold_one<CB>(Gn, rp, q, kk, lmax, R, N2, nch, cb0, qn);
+    fold_one<CB>(Gs, rp, q, kk, lmax, R, N2, nch, cb0, qs);
+#pragma unroll
+    for (int b = 0; b < CB; b++) {
+      float2 hn = qn[b], hs = qs[b];
+      if (k == 0 || k == half) {
+        hn.y = 0.f;
+        hs.y = 0.f;
+      } else {
+        hn = make_float2(0.5f * hn.x, 0.5f * (k < half ? hn.y : -hn.y));
+        hs = make_float2(0.5f * hs.x, 0.5f * (k < half ? hs.y : -hs.y));
+      }
+      a[b * M + k] = make_float2(hn.x - hs.y, -(hn.y + hs.x));  // conj(H_north + i H_south)
+    }
+  }
+  __syncthreads();
+  bluestein<CB>(a, Bt, tw, n, M, logM);
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+#pragma unroll
+    for (int b = 0; b < CB; b++) {
+      const int c = cb0 + b;
+      if (c >= nch) continue;
+      const float2 v = a[b * M + j];  // conj of the pixel pair (north + i south)
+      maps[(long long)c * npix + rp.first_n + j] = v.x;
+      maps[(long long)c * npix + rp.first_s + j] = -v.y;
+    }
+  }
+}
+
+constexpr int BM = 64, BN = 128, BK = 16;
+
+// Tiles of the Legendre GEMMs, staged through registers into two shared-memory
+// buffers (one barrier per k step): A as As[k][row] (rows padded by 4 floats),
+// B as Bs[k][col].  A thread owns rows ty*4 .. ty*4+3 and the column groups
+// tx*4 .. tx*4+3 and 64 + tx*4 .. 64 + tx*4+3.
+struct GemmSmem {
+  float As[2][BK][BM + 4];
+  float Bs[2][BK][BN];
+};
+
+// 4 consecutive floats of a row (zero-filled beyond `len`)
+__device__ __forceinline__ float4 load4(const float *__restrict__ row, int i, int len, bool vec)
+{
+  if (vec && i + 3 < len) return *reinterpret_cast<const float4 *>(row + i);
+  float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (i < len) v.x = row[i];
+  if (i + 1 < len) v.y = row[i + 1];
+  if (i + 2 < len) v.z = row[i + 2];
+  if (i + 3 < len) v.w = row[i + 3];
+  return v;
+}
+
+__device__ __forceinline__ void mma_tile(const GemmSmem &sm, int buf, int tx, int ty, float (&acc)[4][8])
+{
+#pragma unroll
+  for (int k = 0; k < BK; k++) {
+    const float4 a = *reinterpret_cast<const float4 *>(&sm.As[buf][k][ty * 4]);
+    const float4 b0 = *reinterpret_cast<const float4 *>(&sm.Bs[buf][k][tx * 4]);
+    const float4 b1 = *reinterpret_cast<const float4 *>(&sm.Bs[buf][k][64 + tx * 4]);
+    const float av[4] = {a.x, a.y, a.z, a.w}, bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int j = 0; j < 8; j++) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+  }
+}
+
+// acc += A[row0.., 0..K) B[0..K), col0..) with A row-major [rows][K] (TRANS_A
+// false, lda = K) or stored transposed as [K][lda] (TRANS_A true), B [K][N2]
+template <bool TRANS_A>
+__device__ __forceinline__ void gemm_tile(GemmSmem &sm, const float *__restrict__ A, int lda, int rows,
+                                          const float *__restrict__ B, int N2, int K, int row0, int col0,
+                                          float (&acc)[4][8])
+{
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const bool vec = (lda % 4 == 0) && (N2 % 4 == 0);
+  const int nk = (K + BK - 1) / BK;
+  float4 ra, rb0, rb1;
+  auto load = [&](int k0) {
+    if (!TRANS_A) {  // 64 rows x 16 k: row tid/4, k (tid%4)*4
+      const int r = row0 + (tid >> 2), k = (tid & 3) * 4;
+      ra = r < rows ? load4(A + (long long)r * lda + k0, k, K - k0, vec) : make_float4(0.f, 0.f, 0.f, 0.f);
+    } else {         // 16 k x 64 rows: k tid/16, rows (tid%16)*4
+      const int k = tid >> 4, r = (tid & 15) * 4;
+      ra = k0 + k < K ? load4(A + (long long)(k0 + k) * lda + row0, r, rows - row0, vec)
+                      : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    const int kb = tid >> 5, c = (tid & 31) * 4;  // B: k rows kb and kb + 8, columns c .. c+3
+    rb0 = k0 + kb < K ? load4(B + (long long)(k0 + kb) * N2 + col0, c, N2 - col0, vec) : make_float4(0.f, 0.f, 0.f, 0.f);
+    rb1 = k0 + kb + 8 < K ? load4(B + (long long)(k0 + kb + 8) * N2 + col0, c, N2 - col0, vec)
+                          : make_float4(0.f, 0.f, 0.f, 0.f);
+  };
+  auto store = [&](int buf) {
+    if (!TRANS_A) {
+      const int r = tid >> 2, k = (tid & 3) * 4;
+      sm.As[buf][k][r] = ra.x;
+      sm.As[buf][k + 1][r] = ra.y;
+      sm.As[buf][k + 2][r] = ra.z;
+      sm.As[buf][k + 3][r] = ra.w;
+    } else {
+      *reinterpret_cast<float4 *>(&sm.As[buf][tid >> 4][(tid & 15) * 4]) = ra;
+    }
+    const int kb = tid >> 5, c = (tid & 31) * 4;
+    *reinterpret_cast<float4 *>(&sm.Bs[buf][kb][c]) = rb0;
+    *reinterpret_cast<float4 *>(&sm.Bs[buf][kb + 8][c]) = rb1;
+  };
+  if (nk == 0) return;
+  load(0);
+  store(0);
+  __syncthreads();
+  for (int kt = 0; kt < nk; kt++) {
+    const int buf = kt & 1;
+    if (kt + 1 < nk) load((kt + 1) * BK);
+    mma_tile(sm, buf, tx, ty, acc);
+    if (kt + 1 < nk) store(buf ^ 1);
+    __syncthreads();
+  }
+}
+
+// Legendre analysis, one 64 x 128 tile of one (m, parity) per CTA:
+// alm[l'][col] = scale(l, col) sum_q lam[l'][q] EO[q][col]
+__global__ __launch_bounds__(kThreads, 2) void legendre_analysis_kernel(const float *__restrict__ lam,
+                                                                        const float *__restrict__ E,
+                                                                        const float *__restrict__ O,
+                                                                        float *__restrict__ alm,
+                                                                        const int4 *__restrict__ tasks, int R,
+                                                                        int lmax, int N2, float w,
+                                                                        const float *__restrict__ sig2)
+{
+  __shared__ __align__(16) GemmSmem sm;
   const int4 t = tasks[blockIdx.x];
   const int m = t.x, p = t.y, row0 = t.z * BM, col0 = t.w * BN;
   const int ne = (lmax - m) / 2 + 1, no = (lmax - m + 1) / 2, M = p ? no : ne;
   const long long off = m_offset(m, lmax) + (p ? ne : 0);
-  const float *A = lam + off * R;
-  const float *B = (p ? O : E) + (long long)m * R * N2;
+  float acc[4][8] = {};
+  gemm_tile<false>(sm, lam + off * R, R, M, (p ? O : E) + (long long)m * R * N2, N2, R, row0, col0, acc);
   float *C = alm + off * N2;
-  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  float acc[4][4] = {};
-  for (int k0 = 0; k0 < R; k0 += BK) {
-#pragma unroll
-    for (int i = 0; i < 4; i++) {  // A: 64 rows x 16 q, 4 per thread
-      const int e = tid + i * kThreads, r = e >> 4, k = e & 15;
-      As[k][r] = (row0 + r < M && k0 + k < R) ? A[(long long)(row0 + r) * R + k0 + k] : 0.f;
-    }
-#pragma unroll
-    for (int i = 0; i < 4; i++) {  // B: 16 q x 64 columns
-      const int e = tid + i * kThreads, k = e >> 6, c = e & 63;
-      Bs[k][c] = (k0 + k < R && col0 + c < N2) ? B[(long long)(k0 + k) * N2 + col0 + c] : 0.f;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < BK; k++) {
-      const float4 a = *reinterpret_cast<const float4 *>(&As[k][ty * 4]);
-      const float4 b = *reinterpret_cast<const float4 *>(&Bs[k][tx * 4]);
-      const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
-#pragma unroll
-      for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int j = 0; j < 4; j++) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
-    }
-    __syncthreads();
-  }
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
 #pragma unroll
   for (int i = 0; i < 4; i++) {
     const int r = row0 + ty * 4 + i;
     if (r >= M) continue;
     const float l = (float)(m + 2 * r + p);
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-      const int col = col0 + tx * 4 + j;
+    for (int j = 0; j < 8; j++) {
+      const int col = col0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + j - 4);
       if (col >= N2) continue;
       float s = w;
       if (sig2) s *= expf(-0.5f * l * (l + 1.f) * sig2[col >> 1]);
@@ -416,68 +665,33 @@ __global__ __launch_bounds__(kThreads) void legendre_analysis_kernel(const float
   }
 }
 
-// Legendre synthesis, one 64 x 64 tile (ring pairs x columns) of one m per CTA:
+// Legendre synthesis, one 64 x 128 tile (ring pairs x columns) of one m per CTA:
 // G_e[q][col] = sum_l' lam_e[l'][q] alm_e[l'][col] and the same for l - m odd;
 // north ring sums G_e + G_o, south G_e - G_o (lambda_lm(-z) = (-1)^{l+m} lambda_lm(z))
-__global__ __launch_bounds__(kThreads) void legendre_synthesis_kernel(const float *__restrict__ lam,
-                                                                      const float *__restrict__ alm,
-                                                                      float *__restrict__ Gn, float *__restrict__ Gs,
-                                                                      const int4 *__restrict__ tasks, int R, int lmax,
-                                                                      int N2)
+__global__ __launch_bounds__(kThreads, 2) void legendre_synthesis_kernel(const float *__restrict__ lam,
+                                                                         const float *__restrict__ alm,
+                                                                         float *__restrict__ Gn,
+                                                                         float *__restrict__ Gs,
+                                                                         const int4 *__restrict__ tasks, int R,
+                                                                         int lmax, int N2)
 {
-  __shared__ __align__(16) float As[BK][BM];
-  __shared__ __align__(16) float Bs[BK][BN];
+  __shared__ __align__(16) GemmSmem sm;
   const int4 t = tasks[blockIdx.x];
   const int m = t.x, row0 = t.z * BM, col0 = t.w * BN;
   const int ne = (lmax - m) / 2 + 1, no = (lmax - m + 1) / 2;
-  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  float ae[4][4] = {}, ao[4][4] = {};
-#pragma unroll 1
-  for (int p = 0; p < 2; p++) {
-    const int K = p ? no : ne;
-    const long long off = m_offset(m, lmax) + (p ? ne : 0);
-    const float *A = lam + off * R;  // [l'][q]
-    const float *B = alm + off * N2;  // [l'][col]
-    for (int k0 = 0; k0 < K; k0 += BK) {
-#pragma unroll
-      for (int i = 0; i < 4; i++) {  // A^T: 16 l' x 64 q
-        const int e = tid + i * kThreads, k = e >> 6, r = e & 63;
-        As[k][r] = (k0 + k < K && row0 + r < R) ? A[(long long)(k0 + k) * R + row0 + r] : 0.f;
-      }
-#pragma unroll
-      for (int i = 0; i < 4; i++) {
-        const int e = tid + i * kThreads, k = e >> 6, c = e & 63;
-        Bs[k][c] = (k0 + k < K && col0 + c < N2) ? B[(long long)(k0 + k) * N2 + col0 + c] : 0.f;
-      }
-      __syncthreads();
-#pragma unroll
-      for (int k = 0; k < BK; k++) {
-        const float4 a = *reinterpret_cast<const float4 *>(&As[k][ty * 4]);
-        const float4 b = *reinterpret_cast<const float4 *>(&Bs[k][tx * 4]);
-        const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
-        if (p == 0) {
-#pragma unroll
-          for (int i = 0; i < 4; i++)
-#pragma unroll
-            for (int j = 0; j < 4; j++) ae[i][j] = fmaf(av[i], bv[j], ae[i][j]);
-        } else {
-#pragma unroll
-          for (int i = 0; i < 4; i++)
-#pragma unroll
-            for (int j = 0; j < 4; j++) ao[i][j] = fmaf(av[i], bv[j], ao[i][j]);
-        }
-      }
-      __syncthreads();
-    }
-  }
+  const long long off = m_offset(m, lmax);
+  float ae[4][8] = {}, ao[4][8] = {};
+  gemm_tile<true>(sm, lam + off * R, R, R, alm + off * N2, N2, ne, row0, col0, ae);
+  gemm_tile<true>(sm, lam + (off + ne) * R, R, R, alm + (off + ne) * N2, N2, no, row0, col0, ao);
   float *gn = Gn + (long long)m * R * N2, *gs = Gs + (long long)m * R * N2;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
 #pragma unroll
   for (int i = 0; i < 4; i++) {
     const int r = row0 + ty * 4 + i;
     if (r >= R) continue;
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-      const int col = col0 + tx * 4 + j;
+    for (int j = 0; j < 8; j++) {
+      const int col = col0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + j - 4);
       if (col >= N2) continue;
       gn[(long long)r * N2 + col] = ae[i][j] + ao[i][j];
       gs[(long long)r * N2 + col] = ae[i][j] - ao[i][j];
@@ -551,9 +765,10 @@ struct joint_ctx {
   bool have_acc = false;   // acc holds the sum of the components added since the last merge
   // spherical harmonic transform
   RingPair *rings = nullptr;
-  float2 *tw = nullptr;
+  float2 *tw2 = nullptr;   // e^{2 pi i t/M} at [M + t] for every power of two M
+  float2 *btab = nullptr;  // polar rings: spectra of the conjugate Bluestein chirps (bit-reversed)
   float *lam = nullptr;
-  int chunk = 0, N2 = 0;
+  int chunk = 0, N2 = 0, bmax = 0;
   float *E = nullptr, *O = nullptr, *alm = nullptr, *sig2 = nullptr, *tmp_maps = nullptr;
   float2 *alm_hp = nullptr;
   int4 *tasks_a = nullptr, *tasks_s = nullptr;
@@ -588,9 +803,50 @@ int jalloc(T **p, size_t count)
   return GETHI_OK;
 }
 
-size_t analysis_smem(int n, int cb) { return (size_t)2 * n * cb * 4 + (size_t)n * 8 + (size_t)2 * (n / 2 + 1) * cb * 8; }
-size_t synthesis_smem(int n, int cb) { return (size_t)n * 8 + (size_t)2 * (n / 2 + 1) * cb * 8; }
-int ring_cb(long long nside) { return nside <= 512 ? 4 : 2; }
+size_t analysis_fft_smem(int n, int cb) { return (size_t)cb * n * 8 + (size_t)n * 8; }
+size_t synthesis_fft_smem(int n, int cb) { return (size_t)n * 8 + (size_t)2 * (n / 2 + 1) * cb * 8 + (size_t)cb * n * 8; }
+size_t bluestein_smem(int M, int cb) { return ((size_t)cb * M + 2 * (size_t)M) * 8; }
+int ring_cb(long long nside) { return nside <= 512 ? 4 : 2; }        // channels per CTA, equatorial FFTs
+int bluestein_cb(long long nside) { return nside <= 512 ? 4 : 1; }   // channels per CTA, polar Bluestein
+int bluestein_size(int n)  // the power of two >= 2n - 1
+{
+  int M = 1;
+  while (M < 2 * n - 1) M <<= 1;
+  return M;
+}
+
+// forward DFT (e^{-2 pi i jk/M}) of a power-of-two length in FP64 on the host
+void host_fft(std::vector<double> &re, std::vector<double> &im)
+{
+  const size_t n = re.size();
+  for (size_t i = 1, j = 0; i < n; i++) {
+    size_t bit = n >> 1;
+    for (; j & bit; bit >>= 1) j ^= bit;
+    j ^= bit;
+    if (i < j) {
+      std::swap(re[i], re[j]);
+      std::swap(im[i], im[j]);
+    }
+  }
+  std::vector<double> wr(n / 2), wi(n / 2);
+  for (size_t k = 0; k < n / 2; k++) {
+    wr[k] = std::cos(2 * M_PI * (double)k / (double)n);
+    wi[k] = -std::sin(2 * M_PI * (double)k / (double)n);
+  }
+  for (size_t len = 2; len <= n; len <<= 1) {
+    const size_t st = n / len;
+    for (size_t i = 0; i < n; i += len)
+      for (size_t k = 0; k < len / 2; k++) {
+        const double cr = wr[k * st], ci = wi[k * st];
+        const size_t a = i + k, b = a + len / 2;
+        const double vr = re[b] * cr - im[b] * ci, vi = re[b] * ci + im[b] * cr;
+        re[b] = re[a] - vr;
+        im[b] = im[a] - vi;
+        re[a] += vr;
+        im[a] += vi;
+      }
+  }
+}
 
 // ring pairs, twiddles and the Legendre table of the context's nside (first transform)
 int ensure_sht(joint_ctx *c)
@@ -626,8 +882,10 @@ int ensure_sht(joint_ctx *c)
       r.first_n = ncap + (i - N) * 4 * N;
     }
     r.first_s = npix - r.nph - r.first_n;
-    const long long i4 = r.nph / 4;
-    r.tw_off = 2 * i4 * (i4 - 1);
+    r.tw_off = r.nph;  // equatorial rings: tw2[nph + t]
+    r.bm = i < N ? bluestein_size(r.nph) : 0;
+    r.pad_ = 0;
+    r.b_off = 0;
     rp[q] = r;
     z[q] = cz;
     lsin[q] = std::log2(sz);
@@ -637,18 +895,42 @@ int ensure_sht(joint_ctx *c)
     if (m > 0) acc += 0.5 * std::log2((2.0 * m - 1.0) / (2.0 * m));
     lmm0[m] = 0.5 * std::log2((2.0 * m + 1.0) / (4.0 * M_PI)) + acc;
   }
-  // twiddles e^{2 pi i j/n} of every ring length n = 4 i, i = 1 .. N, at 2 i (i - 1)
-  std::vector<float2> tw(2 * N * (N + 1));
-  for (long long i = 1; i <= N; i++) {
-    const long long n = 4 * i, o = 2 * i * (i - 1);
-    for (long long j = 0; j < n; j++) {
-      const double a = 2.0 * M_PI * (double)j / (double)n;
-      tw[o + j] = make_float2((float)std::cos(a), (float)std::sin(a));
+  // power-of-two twiddles, and per polar ring the spectrum of its conjugate chirp
+  // b_t = e^{i pi t^2 / n} (t = -(n-1) .. n-1, wrapped modulo M) for Bluestein's DFT
+  int Mmax = (int)(4 * N);
+  for (int q = 0; q < N - 1; q++) Mmax = std::max(Mmax, rp[q].bm);
+  std::vector<float2> tw2(2 * (size_t)Mmax);
+  for (int M = 1; M <= Mmax; M <<= 1)
+    for (int t = 0; t < M; t++) {
+      const double a = 2.0 * M_PI * (double)t / (double)M;
+      tw2[M + t] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+  std::vector<float2> btab;
+  for (int q = 0; q < N - 1; q++) {
+    const int n = rp[q].nph, M = rp[q].bm, logM = __builtin_ctz((unsigned)M);
+    std::vector<double> re(M, 0.0), im(M, 0.0);
+    for (int t = 0; t < n; t++) {
+      const double a = M_PI * (double)(((long long)t * t) % (2 * n)) / (double)n;
+      re[t] = std::cos(a);
+      im[t] = std::sin(a);
+      if (t) {
+        re[M - t] = re[t];
+        im[M - t] = im[t];
+      }
+    }
+    host_fft(re, im);
+    rp[q].b_off = (long long)btab.size();
+    btab.resize(btab.size() + M);
+    for (int t = 0; t < M; t++) {
+      unsigned r = 0;
+      for (int bit = 0; bit < logM; bit++) r |= ((t >> bit) & 1u) << (logM - 1 - bit);
+      btab[rp[q].b_off + r] = make_float2((float)re[t], (float)im[t]);
     }
   }
   int rc;
   const size_t lam_elems = (size_t)m_offset(lmax + 1, lmax) * R;
-  if ((rc = jalloc(&c->rings, R)) || (rc = jalloc(&c->tw, tw.size())) || (rc = jalloc(&c->lam, lam_elems)))
+  if ((rc = jalloc(&c->rings, R)) || (rc = jalloc(&c->tw2, tw2.size())) || (rc = jalloc(&c->btab, btab.size())) ||
+      (rc = jalloc(&c->lam, lam_elems)))
     return rc;
   double *dz = nullptr, *dl = nullptr, *dm = nullptr;
   if ((rc = jalloc(&dz, R)) || (rc = jalloc(&dl, R)) || (rc = jalloc(&dm, lmax + 1))) {
@@ -657,7 +939,9 @@ int ensure_sht(joint_ctx *c)
     return rc;
   }
   JCK(cudaMemcpyAsync(c->rings, rp.data(), sizeof(RingPair) * R, cudaMemcpyHostToDevice, c->stream));
-  JCK(cudaMemcpyAsync(c->tw, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice, c->stream));
+  JCK(cudaMemcpyAsync(c->tw2, tw2.data(), sizeof(float2) * tw2.size(), cudaMemcpyHostToDevice, c->stream));
+  if (!btab.empty())
+    JCK(cudaMemcpyAsync(c->btab, btab.data(), sizeof(float2) * btab.size(), cudaMemcpyHostToDevice, c->stream));
   JCK(cudaMemcpyAsync(dz, z.data(), sizeof(double) * R, cudaMemcpyHostToDevice, c->stream));
   JCK(cudaMemcpyAsync(dl, lsin.data(), sizeof(double) * R, cudaMemcpyHostToDevice, c->stream));
   JCK(cudaMemcpyAsync(dm, lmm0.data(), sizeof(double) * (lmax + 1), cudaMemcpyHostToDevice, c->stream));
@@ -693,38 +977,76 @@ int ensure_sht(joint_ctx *c)
     return rc;
   JCK(cudaMemcpyAsync(c->tasks_a, ta.data(), sizeof(int4) * ta.size(), cudaMemcpyHostToDevice, c->stream));
   JCK(cudaMemcpyAsync(c->tasks_s, ts.data(), sizeof(int4) * ts.size(), cudaMemcpyHostToDevice, c->stream));
-  const int cb = ring_cb(N);
-  const int n = (int)(4 * N);
-  if (cb == 4) {
-    JCK(cudaFuncSetAttribute(ring_analysis_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)analysis_smem(n, 4)));
-    JCK(cudaFuncSetAttribute(ring_synthesis_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)synthesis_smem(n, 4)));
+  const int mb = Mmax, ne = (int)(4 * N);  // largest Bluestein size, equatorial ring length
+  if (ring_cb(N) == 4) {
+    JCK(cudaFuncSetAttribute(ring_analysis_fft_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)analysis_fft_smem(ne, 4)));
+    JCK(cudaFuncSetAttribute(ring_synthesis_fft_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)synthesis_fft_smem(ne, 4)));
   } else {
-    JCK(cudaFuncSetAttribute(ring_analysis_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)analysis_smem(n, 2)));
-    JCK(cudaFuncSetAttribute(ring_synthesis_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)synthesis_smem(n, 2)));
+    JCK(cudaFuncSetAttribute(ring_analysis_fft_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)analysis_fft_smem(ne, 2)));
+    JCK(cudaFuncSetAttribute(ring_synthesis_fft_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)synthesis_fft_smem(ne, 2)));
   }
+  if (bluestein_cb(N) == 4) {
+    JCK(cudaFuncSetAttribute(ring_analysis_bluestein_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)bluestein_smem(mb, 4)));
+    JCK(cudaFuncSetAttribute(ring_synthesis_bluestein_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)bluestein_smem(mb, 4)));
+  } else {
+    JCK(cudaFuncSetAttribute(ring_analysis_bluestein_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)bluestein_smem(mb, 1)));
+    JCK(cudaFuncSetAttribute(ring_synthesis_bluestein_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)bluestein_smem(mb, 1)));
+  }
+  c->bmax = mb;
   JCK(cudaStreamSynchronize(c->stream));
   return GETHI_OK;
 }
 
 // map2alm of nch (<= chunk) device maps into c->alm (beam factors when sig2 != null)
+template <int CB>
+void launch_ring_analysis(joint_ctx *c, const float *dmaps, int nch)
+{
+  const int N = c->p.nside, nb = (nch + CB - 1) / CB;
+  ring_analysis_fft_kernel<CB><<<dim3(N + 1, nb), kThreads, analysis_fft_smem(4 * N, CB), c->stream>>>(
+      dmaps, c->npix, nch, c->rings, c->tw2, c->lmax, c->R, c->N2, N - 1, c->E, c->O);
+}
+template <int CB>
+void launch_polar_analysis(joint_ctx *c, const float *dmaps, int nch)
+{
+  const int N = c->p.nside, nb = (nch + CB - 1) / CB;
+  if (N > 1)  // polar ring pairs q < N - 1
+    ring_analysis_bluestein_kernel<CB><<<dim3(N - 1, nb), kThreads, bluestein_smem(c->bmax, CB), c->stream>>>(
+        dmaps, c->npix, nch, c->rings, c->tw2, c->btab, c->lmax, c->R, c->N2, c->E, c->O);
+}
+template <int CB>
+void launch_ring_synthesis(joint_ctx *c, float *dmaps, int nch)
+{
+  const int N = c->p.nside, nb = (nch + CB - 1) / CB;
+  ring_synthesis_fft_kernel<CB><<<dim3(N + 1, nb), kThreads, synthesis_fft_smem(4 * N, CB), c->stream>>>(
+      c->E, c->O, c->rings, c->tw2, c->lmax, c->R, c->N2, nch, N - 1, dmaps, c->npix);
+}
+template <int CB>
+void launch_polar_synthesis(joint_ctx *c, float *dmaps, int nch)
+{
+  const int N = c->p.nside, nb = (nch + CB - 1) / CB;
+  if (N > 1)
+    ring_synthesis_bluestein_kernel<CB><<<dim3(N - 1, nb), kThreads, bluestein_smem(c->bmax, CB), c->stream>>>(
+        c->E, c->O, c->rings, c->tw2, c->btab, c->lmax, c->R, c->N2, nch, dmaps, c->npix);
+}
+
 int sht_analysis(joint_ctx *c, const float *dmaps, int nch, const float *sig2)
 {
-  const int R = c->R, lmax = c->lmax, cb = ring_cb(c->p.nside), n = 4 * c->p.nside;
-  const dim3 g(R, (nch + cb - 1) / cb);
-  if (cb == 4)
-    ring_analysis_kernel<4><<<g, kThreads, analysis_smem(n, 4), c->stream>>>(dmaps, c->npix, nch, c->rings, c->tw,
-                                                                             lmax, R, c->N2, c->E, c->O);
-  else
-    ring_analysis_kernel<2><<<g, kThreads, analysis_smem(n, 2), c->stream>>>(dmaps, c->npix, nch, c->rings, c->tw,
-                                                                             lmax, R, c->N2, c->E, c->O);
+  if (ring_cb(c->p.nside) == 4) launch_ring_analysis<4>(c, dmaps, nch);
+  else launch_ring_analysis<2>(c, dmaps, nch);
+  if (bluestein_cb(c->p.nside) == 4) launch_polar_analysis<4>(c, dmaps, nch);
+  else launch_polar_analysis<1>(c, dmaps, nch);
   JCK(cudaGetLastError());
   const float w = (float)(4.0 * M_PI / (double)c->npix);
-  legendre_analysis_kernel<<<c->ntasks_a, kThreads, 0, c->stream>>>(c->lam, c->E, c->O, c->alm, c->tasks_a, R, lmax,
-                                                                    c->N2, w, sig2);
+  legendre_analysis_kernel<<<c->ntasks_a, kThreads, 0, c->stream>>>(c->lam, c->E, c->O, c->alm, c->tasks_a, c->R,
+                                                                    c->lmax, c->N2, w, sig2);
   JCK(cudaGetLastError());
   return GETHI_OK;
 }
@@ -732,17 +1054,13 @@ int sht_analysis(joint_ctx *c, const float *dmaps, int nch, const float *sig2)
 // alm2map of c->alm into nch device maps
 int sht_synthesis(joint_ctx *c, float *dmaps, int nch)
 {
-  const int R = c->R, lmax = c->lmax, cb = ring_cb(c->p.nside), n = 4 * c->p.nside;
-  legendre_synthesis_kernel<<<c->ntasks_s, kThreads, 0, c->stream>>>(c->lam, c->alm, c->E, c->O, c->tasks_s, R,
-                                                                     lmax, c->N2);
+  legendre_synthesis_kernel<<<c->ntasks_s, kThreads, 0, c->stream>>>(c->lam, c->alm, c->E, c->O, c->tasks_s, c->R,
+                                                                     c->lmax, c->N2);
   JCK(cudaGetLastError());
-  const dim3 g(R, (nch + cb - 1) / cb);
-  if (cb == 4)
-    ring_synthesis_kernel<4><<<g, kThreads, synthesis_smem(n, 4), c->stream>>>(c->E, c->O, c->rings, c->tw, lmax, R,
-                                                                               c->N2, nch, dmaps, c->npix);
-  else
-    ring_synthesis_kernel<2><<<g, kThreads, synthesis_smem(n, 2), c->stream>>>(c->E, c->O, c->rings, c->tw, lmax, R,
-                                                                               c->N2, nch, dmaps, c->npix);
+  if (ring_cb(c->p.nside) == 4) launch_ring_synthesis<4>(c, dmaps, nch);
+  else launch_ring_synthesis<2>(c, dmaps, nch);
+  if (bluestein_cb(c->p.nside) == 4) launch_polar_synthesis<4>(c, dmaps, nch);
+  else launch_polar_synthesis<1>(c, dmaps, nch);
   JCK(cudaGetLastError());
   return GETHI_OK;
 }
@@ -823,7 +1141,7 @@ extern "C" void joint_gpu_free(joint_ctx *c)
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (void *ptr : {(void *)c->maps, (void *)c->acc, (void *)c->stage_buf, (void *)c->dmask, (void *)c->s2,
-                    (void *)c->rings, (void *)c->tw, (void *)c->lam, (void *)c->E, (void *)c->O, (void *)c->alm,
+                    (void *)c->rings, (void *)c->tw2, (void *)c->btab, (void *)c->lam, (void *)c->E, (void *)c->O, (void *)c->alm,
                     (void *)c->sig2, (void *)c->tmp_maps, (void *)c->alm_hp, (void *)c->tasks_a, (void *)c->tasks_s,
                     (void *)c->noise_d})
     cudaFree(ptr);
