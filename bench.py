@@ -353,8 +353,7 @@ JOINT = dict(n_side=512, n_nu=150, zmin=0.3, zmax=2.0, dish_diameter=30.0, n_dis
              time_tot=10000.0, seed=6001, b_cut_deg=10.0)
 
 
-def joint_workload():
-    E = JOINT
+def joint_workload(E=JOINT):
     edges = np.linspace(NU21 / (1 + E["zmax"]), NU21 / (1 + E["zmin"]), E["n_nu"] + 1)
     nside = E["n_side"]
     npix = 12 * nside * nside
@@ -386,8 +385,12 @@ def bench_joint(args):
     from crime_gb300 import joint as jt
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
-    E = JOINT
-    nu0, nuf, mask = joint_workload()
+    E = dict(JOINT)
+    if args.joint_nside:
+        E["n_side"] = args.joint_nside
+    if args.joint_nnu:
+        E["n_nu"] = args.joint_nnu
+    nu0, nuf, mask = joint_workload(E)
     nside, n_nu = E["n_side"], E["n_nu"]
     npix = 12 * nside * nside
     g = torch.Generator(device="cuda").manual_seed(E["seed"] + rank)
@@ -433,6 +436,28 @@ def bench_joint(args):
     e2e_ms = max_over_ranks(1e3 * (time.perf_counter() - t0), ws)
     assert np.isfinite(out.numpy()).all()
     chunks = -(-n_nu // 64)
+    # per-kernel-class device time of the beam over one more profiled step
+    j.profile(True)
+    step()
+    kt = j.kernel_times()
+    j.profile(False)
+    lmax, R, N2 = 3 * nside - 1, 2 * nside, 2 * min(64, n_nu)
+    nalm = (lmax + 1) * (lmax + 2) // 2
+    gemm_bytes = 4.0 * (nalm * R + 2 * (lmax + 1) * R * N2 + nalm * N2)  # Legendre table + E/O + a_lm per batch
+    gemm_flops = 2.0 * nalm * R * N2
+    dom = max(("legendre_analysis", "legendre_synthesis"), key=lambda k: kt[k][0])
+    per_launch = kt[dom][0] / kt[dom][1]
+    peak_hbm, peak_kind = read_peaks()
+    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12  # TFLOP/s: SMs x FP32 lanes x 2 x max clock (nominal)
+    tflops = gemm_flops / (per_launch / 1e3) / 1e12
+    roof = {"bound": "fp32", "kernel": dom, "achieved": round(tflops, 2), "peak": round(fp32_peak, 1),
+            "unit": "TFLOP/s", "frac": round(tflops / fp32_peak, 3),
+            "peak_source": "nominal FP32 CUDA-core rate (152 SMs x 128 lanes x 2 x 2.07 GHz); no measured figure",
+            "flops_per_launch": gemm_flops, "avg_launch_ms": round(per_launch, 3),
+            "hbm": {"algorithmic_bytes_per_launch": gemm_bytes,
+                    "achieved_gbs": round(gemm_bytes / (per_launch / 1e3) / 1e9, 1), "peak_gbs": peak_hbm,
+                    "frac": round(gemm_bytes / (per_launch / 1e3) / 1e9 / peak_hbm, 3), "peak_source": peak_kind},
+            "traffic": None}
     line = {
         "metric": "JoinT map combination throughput (map pixels/s): Nside %d x %d channels, beam + noise + mask" % (
             nside, n_nu),
@@ -447,6 +472,8 @@ def bench_joint(args):
                    "setup_s_incl_legendre_table": round(setup_s, 3),
                    "l2": "inputs larger than L2 (maps %.1f GB, Legendre table above)" % (4 * units / 1e9)},
         "stage_ms": dict(zip(("merge", "beam", "noise", "mask"), np.round(stages / args.steps, 3).tolist())),
+        "beam_kernels_ms": {k: round(v[0], 3) for k, v in kt.items()},
+        "roofline": roof,
         "e2e": {"value": whole_job_rate(units, args.steps, ws, e2e_ms), "unit": "pixels/s",
                 "h2d_bytes_per_step": int(4 * units * len(comp)), "d2h_bytes_per_step": int(4 * units)},
         "gpu_launches": args.steps * (len(comp) + 4 * chunks + 2),
@@ -687,6 +714,8 @@ def main():
     ap.add_argument("--config", default="c2", choices=sorted(CONFIGS) + ["c3", "joint"])
     ap.add_argument("--cpu-sample", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--joint-nside", type=int, default=0, help="joint: Nside (default 512; smaller for profiling)")
+    ap.add_argument("--joint-nnu", type=int, default=0, help="joint: channels (default 150)")
     ap.add_argument("--no-fft-compare", action="store_true",
                     help="skip the tensor-core split-precision FFT comparison (1024^3 workloads)")
     args = ap.parse_args()

@@ -776,6 +776,13 @@ struct joint_ctx {
   double *noise_h = nullptr, *noise_d = nullptr;  // mt_validation staging (pinned host, device)
   cudaEvent_t ev[5] = {};
   float times[4] = {};
+  // optional per-kernel-class device times of the beam (joint_gpu_profile):
+  // ring analysis, Legendre analysis, Legendre synthesis, ring synthesis
+  int prof = 0;
+  std::vector<cudaEvent_t> kev;
+  std::vector<int> kcls;
+  double ktime[4] = {};
+  long kcount[4] = {};
 };
 
 namespace {
@@ -1037,16 +1044,52 @@ void launch_polar_synthesis(joint_ctx *c, float *dmaps, int nch)
         c->E, c->O, c->rings, c->tw2, c->btab, c->lmax, c->R, c->N2, nch, dmaps, c->npix);
 }
 
+// events around one kernel class when profiling (joint_gpu_profile)
+struct KSpan {
+  joint_ctx *c;
+  int cls;
+  KSpan(joint_ctx *c_, int cls_) : c(c_), cls(cls_) { mark(); }
+  ~KSpan() { mark(); }
+  void mark()
+  {
+    if (!c->prof) return;
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, c->stream);
+    c->kev.push_back(e);
+    c->kcls.push_back(cls);
+  }
+};
+
+void collect_kernel_times(joint_ctx *c)  // after a synchronize
+{
+  for (size_t i = 0; i + 1 < c->kev.size(); i += 2) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->kev[i], c->kev[i + 1]);
+    c->ktime[c->kcls[i]] += ms;
+    c->kcount[c->kcls[i]]++;
+  }
+  for (cudaEvent_t e : c->kev) cudaEventDestroy(e);
+  c->kev.clear();
+  c->kcls.clear();
+}
+
 int sht_analysis(joint_ctx *c, const float *dmaps, int nch, const float *sig2)
 {
-  if (ring_cb(c->p.nside) == 4) launch_ring_analysis<4>(c, dmaps, nch);
-  else launch_ring_analysis<2>(c, dmaps, nch);
-  if (bluestein_cb(c->p.nside) == 4) launch_polar_analysis<4>(c, dmaps, nch);
-  else launch_polar_analysis<1>(c, dmaps, nch);
+  {
+    KSpan k(c, 0);
+    if (ring_cb(c->p.nside) == 4) launch_ring_analysis<4>(c, dmaps, nch);
+    else launch_ring_analysis<2>(c, dmaps, nch);
+    if (bluestein_cb(c->p.nside) == 4) launch_polar_analysis<4>(c, dmaps, nch);
+    else launch_polar_analysis<1>(c, dmaps, nch);
+  }
   JCK(cudaGetLastError());
   const float w = (float)(4.0 * M_PI / (double)c->npix);
-  legendre_analysis_kernel<<<c->ntasks_a, kThreads, 0, c->stream>>>(c->lam, c->E, c->O, c->alm, c->tasks_a, c->R,
-                                                                    c->lmax, c->N2, w, sig2);
+  {
+    KSpan k(c, 1);
+    legendre_analysis_kernel<<<c->ntasks_a, kThreads, 0, c->stream>>>(c->lam, c->E, c->O, c->alm, c->tasks_a, c->R,
+                                                                      c->lmax, c->N2, w, sig2);
+  }
   JCK(cudaGetLastError());
   return GETHI_OK;
 }
@@ -1054,13 +1097,19 @@ int sht_analysis(joint_ctx *c, const float *dmaps, int nch, const float *sig2)
 // alm2map of c->alm into nch device maps
 int sht_synthesis(joint_ctx *c, float *dmaps, int nch)
 {
-  legendre_synthesis_kernel<<<c->ntasks_s, kThreads, 0, c->stream>>>(c->lam, c->alm, c->E, c->O, c->tasks_s, c->R,
-                                                                     c->lmax, c->N2);
+  {
+    KSpan k(c, 2);
+    legendre_synthesis_kernel<<<c->ntasks_s, kThreads, 0, c->stream>>>(c->lam, c->alm, c->E, c->O, c->tasks_s,
+                                                                       c->R, c->lmax, c->N2);
+  }
   JCK(cudaGetLastError());
-  if (ring_cb(c->p.nside) == 4) launch_ring_synthesis<4>(c, dmaps, nch);
-  else launch_ring_synthesis<2>(c, dmaps, nch);
-  if (bluestein_cb(c->p.nside) == 4) launch_polar_synthesis<4>(c, dmaps, nch);
-  else launch_polar_synthesis<1>(c, dmaps, nch);
+  {
+    KSpan k(c, 3);
+    if (ring_cb(c->p.nside) == 4) launch_ring_synthesis<4>(c, dmaps, nch);
+    else launch_ring_synthesis<2>(c, dmaps, nch);
+    if (bluestein_cb(c->p.nside) == 4) launch_polar_synthesis<4>(c, dmaps, nch);
+    else launch_polar_synthesis<1>(c, dmaps, nch);
+  }
   JCK(cudaGetLastError());
   return GETHI_OK;
 }
@@ -1146,6 +1195,7 @@ extern "C" void joint_gpu_free(joint_ctx *c)
                     (void *)c->noise_d})
     cudaFree(ptr);
   if (c->noise_h) cudaFreeHost(c->noise_h);
+  for (cudaEvent_t e : c->kev) cudaEventDestroy(e);
   for (auto &ev : c->ev)
     if (ev) cudaEventDestroy(ev);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -1376,6 +1426,32 @@ extern "C" int joint_gpu_run(joint_ctx *c, float *maps_out)
     JCK(cudaStreamSynchronize(c->stream));
   }
   for (int i = 0; i < 4; i++) cudaEventElapsedTime(&c->times[i], c->ev[i], c->ev[i + 1]);
+  collect_kernel_times(c);
+  return GETHI_OK;
+}
+
+extern "C" int joint_gpu_profile(joint_ctx *c, int on)
+{
+  if (!c) return GETHI_E_ARG;
+  JCK(cudaStreamSynchronize(c->stream));
+  collect_kernel_times(c);
+  c->prof = on ? 1 : 0;
+  for (int i = 0; i < 4; i++) {
+    c->ktime[i] = 0;
+    c->kcount[i] = 0;
+  }
+  return GETHI_OK;
+}
+
+extern "C" int joint_gpu_kernel_times(joint_ctx *c, double *ms4, long *launches4)
+{
+  if (!c || !ms4) return GETHI_E_ARG;
+  JCK(cudaStreamSynchronize(c->stream));
+  collect_kernel_times(c);
+  for (int i = 0; i < 4; i++) {
+    ms4[i] = c->ktime[i];
+    if (launches4) launches4[i] = c->kcount[i];
+  }
   return GETHI_OK;
 }
 

@@ -57,6 +57,8 @@ def lib():
         L.joint_gpu_map2alm.argtypes = [vp, vp, C.c_int, vp]
         L.joint_gpu_alm2map.argtypes = [vp, vp, C.c_int, vp]
         L.joint_gpu_stage_times.argtypes = [vp, vp]
+        L.joint_gpu_profile.argtypes = [vp, C.c_int]
+        L.joint_gpu_kernel_times.argtypes = [vp, vp, vp]
         L.joint_host_read_map.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_long), vp]
         L.joint_host_read_nutable.argtypes = [C.c_char_p, C.POINTER(C.c_int), vp, vp]
         L.joint_host_write_maps.argtypes = [C.c_char_p, C.c_long, C.c_int, vp]
@@ -174,6 +176,17 @@ class JoinT:
         t = np.zeros(4, np.float32)
         _check(lib().joint_gpu_stage_times(self._ctx, t.ctypes.data))
         return dict(zip(("merge", "beam", "noise", "mask"), t.tolist()))
+
+    BEAM_KERNELS = ("ring_analysis", "legendre_analysis", "legendre_synthesis", "ring_synthesis")
+
+    def profile(self, on=True):
+        _check(lib().joint_gpu_profile(self._ctx, 1 if on else 0))
+
+    def kernel_times(self):
+        """{class: (device ms, launches)} of the beam while profiling"""
+        ms, n = np.zeros(4), np.zeros(4, np.int64)
+        _check(lib().joint_gpu_kernel_times(self._ctx, ms.ctypes.data, n.ctypes.data))
+        return {k: (float(a), int(b)) for k, a, b in zip(self.BEAM_KERNELS, ms, n)}
 
     # he_map2alm / he_alm2map (src/healpix_extra.c:44-130)
     def map2alm(self, maps):

@@ -92,6 +92,12 @@ int joint_gpu_alm2map(joint_ctx *c, const float *alms, int n_maps, float *maps);
 
 /* device time of the last joint_gpu_run per stage (ms): merge, beam, noise, mask */
 int joint_gpu_stage_times(const joint_ctx *c, float *ms4);
+/* Per-kernel-class device times of the beam, accumulated while profiling is on
+ * (events around each class; off by default): ring analysis (FFT + Bluestein),
+ * Legendre analysis GEMM, Legendre synthesis GEMM, ring synthesis.  Turning
+ * profiling on or off resets the sums.  No counterpart in the reference. */
+int joint_gpu_profile(joint_ctx *c, int on);
+int joint_gpu_kernel_times(joint_ctx *c, double *ms4, long *launches4);
 
 /* ---- host helpers (no GPU) ---- */
 
