@@ -214,87 +214,89 @@ __device__ __forceinline__ void fold_one(const float *__restrict__ G, const Ring
   }
 }
 
-// Q[s][k][b], k = 0 .. n/2, of ring s (0 north, 1 south) of pair q: the sums
-// c_m G_m e^{i m phi0} over m = k mod n, plus the conjugates of those over
-// m = n - k mod n (0 < k < n/2), so that map_j = sum_k Re(Q_k e^{2 pi i jk/n})
-template <int CB>
-__device__ void fold_ring_sums(const float *__restrict__ Gn, const float *__restrict__ Gs, const RingPair &rp, int q,
-                               bool eq, int lmax, int R, int N2, int nch, int cb0, float2 *Q)
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ int bit_reverse(int v, int bits) { return (int)(__brev((unsigned)v) >> (32 - bits)); }
+
+// One radix-2 stage (butterflies i0, i0 + h) over CB sequences of length n = 2^logn
+// stored one after the other in z, decimation in time (DIT) or in frequency.  The
+// twiddle e^{sign 2 pi i jj/(2h)} comes from the power-of-two table, tw2[2h + jj]
+// (contiguous in jj, read-only path); four butterflies per thread are in flight.
+template <int CB, bool DIT>
+__device__ __forceinline__ void fft_stage(float2 *z, const float2 *__restrict__ tw2, int n, int logn, int st,
+                                          float sign)
 {
-  const int half = rp.nph / 2;
-  for (int t = threadIdx.x; t < 2 * (half + 1); t += blockDim.x) {
-    const int s = t / (half + 1), k = t - s * (half + 1);
-    float2 acc[CB];
-    if (s == 0 || !eq) {
-      fold_one<CB>(s ? Gs : Gn, rp, q, k, lmax, R, N2, nch, cb0, acc);
-    } else {
+  const int h = 1 << st, total = CB * (n >> 1), nt = blockDim.x;
+  const float2 *twp = tw2 + 2 * h;
+  int t = threadIdx.x;
+  for (; t + 3 * nt < total; t += 4 * nt) {
+    int i0[4];
+    float2 a[4], c[4], w[4];
 #pragma unroll
-      for (int b = 0; b < CB; b++) acc[b] = make_float2(0.f, 0.f);
+    for (int r = 0; r < 4; r++) {
+      const int tt = t + r * nt, b = tt >> (logn - 1), u = tt & ((n >> 1) - 1), jj = u & (h - 1);
+      i0[r] = b * n + ((u >> st) << (st + 1)) + jj;
+      w[r] = __ldg(twp + jj);
+      a[r] = z[i0[r]];
+      c[r] = z[i0[r] + h];
     }
 #pragma unroll
-    for (int b = 0; b < CB; b++) Q[t * CB + b] = acc[b];
+    for (int r = 0; r < 4; r++) {
+      const float2 ww = make_float2(w[r].x, sign * w[r].y);
+      if (DIT) {
+        const float2 v = cmul(c[r], ww);
+        z[i0[r]] = make_float2(a[r].x + v.x, a[r].y + v.y);
+        z[i0[r] + h] = make_float2(a[r].x - v.x, a[r].y - v.y);
+      } else {
+        z[i0[r]] = make_float2(a[r].x + c[r].x, a[r].y + c[r].y);
+        z[i0[r] + h] = cmul(make_float2(a[r].x - c[r].x, a[r].y - c[r].y), ww);
+      }
+    }
+  }
+  for (; t < total; t += nt) {
+    const int b = t >> (logn - 1), u = t & ((n >> 1) - 1), jj = u & (h - 1);
+    const int i0 = b * n + ((u >> st) << (st + 1)) + jj;
+    const float2 w = __ldg(twp + jj), ww = make_float2(w.x, sign * w.y);
+    const float2 a = z[i0], c = z[i0 + h];
+    if (DIT) {
+      const float2 v = cmul(c, ww);
+      z[i0] = make_float2(a.x + v.x, a.y + v.y);
+      z[i0 + h] = make_float2(a.x - v.x, a.y - v.y);
+    } else {
+      z[i0] = make_float2(a.x + c.x, a.y + c.y);
+      z[i0 + h] = cmul(make_float2(a.x - c.x, a.y - c.y), ww);
+    }
   }
 }
 
-// In-place radix-2 decimation-in-time FFT of CB sequences of length n = 2^logn
-// stored one after the other in z in bit-reversed order; sign -1 for
-// e^{-2 pi i jk/n}, +1 for e^{+2 pi i jk/n}; tw[t] = e^{2 pi i t/n}.
+// radix-2 FFT, bit-reversed order in, natural order out (sign -1: e^{-2 pi i jk/n})
 template <int CB>
-__device__ void smem_fft(float2 *z, const float2 *tw, int n, int logn, float sign)
+__device__ void fft_dit(float2 *z, const float2 *__restrict__ tw2, int n, int logn, float sign)
 {
   for (int st = 0; st < logn; st++) {
-    const int h = 1 << st, step = n >> (st + 1);
-    for (int t = threadIdx.x; t < CB * (n >> 1); t += blockDim.x) {
-      const int b = t >> (logn - 1), u = t & ((n >> 1) - 1);
-      const int jj = u & (h - 1), i0 = ((u >> st) << (st + 1)) + jj;
-      float2 w = tw[jj * step];
-      w.y *= sign;
-      float2 *zb = z + b * n;
-      const float2 a = zb[i0], c = zb[i0 + h];
-      const float2 v = make_float2(c.x * w.x - c.y * w.y, c.x * w.y + c.y * w.x);
-      zb[i0] = make_float2(a.x + v.x, a.y + v.y);
-      zb[i0 + h] = make_float2(a.x - v.x, a.y - v.y);
-    }
+    fft_stage<CB, true>(z, tw2, n, logn, st, sign);
+    __syncthreads();
+  }
+}
+// radix-2 FFT, natural order in, bit-reversed order out
+template <int CB>
+__device__ void fft_dif(float2 *z, const float2 *__restrict__ tw2, int n, int logn, float sign)
+{
+  for (int st = logn - 1; st >= 0; st--) {
+    fft_stage<CB, false>(z, tw2, n, logn, st, sign);
     __syncthreads();
   }
 }
 
-// Ring analysis of the equatorial ring pairs (q >= nside - 1: n = 4 nside, a power
-// of two) by one complex FFT per channel of z_j = north_j + i south_j:
-// D_north,k = (Z_k + conj Z_{n-k}) / 2, D_south,k = (Z_k - conj Z_{n-k}) / 2i;
-// then for m = 0 .. lmax the phase-shifted sums F_m = e^{-i m phi0} D_{m mod n}
-// (D_{n-k} = conj D_k) of both rings combined as E = F_north + F_south and
-// O = F_north - F_south.
+// E and O of pair q for m = 0 .. lmax from the DFT Z of z_j = north_j + i south_j
+// (held in a[b * stride + k], k < n): D_north,k = (Z_k + conj Z_{n-k}) / 2,
+// D_south,k = (Z_k - conj Z_{n-k}) / 2i, F_m = e^{-i m phi0} D_{m mod n} with
+// D_{n-k} = conj D_k, E = F_north + F_south, O = F_north - F_south.
 template <int CB>
-__global__ __launch_bounds__(kThreads) void ring_analysis_fft_kernel(const float *__restrict__ maps, long long npix,
-                                                                     int nch, const RingPair *__restrict__ rings,
-                                                                     const float2 *__restrict__ tw_all, int lmax,
-                                                                     int R, int N2, int q0, float *__restrict__ E,
-                                                                     float *__restrict__ O)
+__device__ __forceinline__ void write_eo(const float2 *a, int stride, const RingPair &rp, int q, bool eq, int lmax,
+                                         int R, int N2, int nch, int cb0, float *__restrict__ E,
+                                         float *__restrict__ O)
 {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int q = q0 + blockIdx.x, cb0 = blockIdx.y * CB;
-  const RingPair rp = rings[q];
-  const int n = rp.nph, half = n / 2, logn = __ffs(n) - 1;
-  const bool eq = (q == R - 1);
-  float2 *z = reinterpret_cast<float2 *>(smem_raw);  // [CB][n]
-  float2 *tw = z + CB * n;
-  for (int j = threadIdx.x; j < n; j += blockDim.x) {
-    tw[j] = tw_all[rp.tw_off + j];
-    const int jr = (int)(__brev((unsigned)j) >> (32 - logn));
-#pragma unroll
-    for (int b = 0; b < CB; b++) {
-      const int c = cb0 + b;
-      float xn = 0.f, xs = 0.f;
-      if (c < nch) {
-        xn = maps[(long long)c * npix + rp.first_n + j];
-        if (!eq) xs = maps[(long long)c * npix + rp.first_s + j];
-      }
-      z[b * n + jr] = make_float2(xn, xs);
-    }
-  }
-  __syncthreads();
-  smem_fft<CB>(z, tw, n, logn, -1.f);
+  const int n = rp.nph, half = n / 2;
   for (int m = threadIdx.x; m <= lmax; m += blockDim.x) {
     int k = m % n;
     const bool cj = k > half;
@@ -309,61 +311,103 @@ __global__ __launch_bounds__(kThreads) void ring_analysis_fft_kernel(const float
     for (int b = 0; b < CB; b++) {
       const int c = cb0 + b;
       if (c >= nch) continue;
-      const float2 zk = z[b * n + k], zm = z[b * n + ((n - k) & (n - 1))];
+      const float2 zk = a[b * stride + k], zm = a[b * stride + (k ? n - k : 0)];
       float2 dn = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
       float2 ds = eq ? make_float2(0.f, 0.f) : make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
       if (cj) {
         dn.y = -dn.y;
         ds.y = -ds.y;
       }
-      const float2 e = make_float2(dn.x + ds.x, dn.y + ds.y), o = make_float2(dn.x - ds.x, dn.y - ds.y);
       const long long base = ((long long)m * R + q) * N2 + 2 * c;
-      *reinterpret_cast<float2 *>(E + base) = make_float2(e.x * ph.x - e.y * ph.y, e.x * ph.y + e.y * ph.x);
-      *reinterpret_cast<float2 *>(O + base) = make_float2(o.x * ph.x - o.y * ph.y, o.x * ph.y + o.y * ph.x);
+      *reinterpret_cast<float2 *>(E + base) = cmul(make_float2(dn.x + ds.x, dn.y + ds.y), ph);
+      *reinterpret_cast<float2 *>(O + base) = cmul(make_float2(dn.x - ds.x, dn.y - ds.y), ph);
     }
   }
 }
 
-// Ring synthesis of the equatorial ring pairs: the Hermitian spectra H of both
-// rings (H_k = Q_k / 2, H_{n-k} = conj Q_k / 2, H_0 = Re Q_0, H_{n/2} = Re Q_{n/2})
-// in one complex inverse FFT of H_north + i H_south, whose real and imaginary
-// parts are the two rings' pixels.
+// The Hermitian-packed synthesis input of frequency k of pair q: with Q_k the
+// folded sums (fold_one), H_k = Q_k / 2 and H_{n-k} = conj Q_k / 2 (0 < k < n/2),
+// H_0 = Re Q_0, H_{n/2} = Re Q_{n/2}; returns H_north,k + i H_south,k per channel
+template <int CB>
+__device__ __forceinline__ void packed_spectrum(const float *__restrict__ Gn, const float *__restrict__ Gs,
+                                                const RingPair &rp, int q, bool eq, int k, int lmax, int R, int N2,
+                                                int nch, int cb0, float2 *out)
+{
+  const int n = rp.nph, half = n / 2, kk = k <= half ? k : n - k;
+  float2 qn[CB], qs[CB];
+  fold_one<CB>(Gn, rp, q, kk, lmax, R, N2, nch, cb0, qn);
+  if (!eq) fold_one<CB>(Gs, rp, q, kk, lmax, R, N2, nch, cb0, qs);
+#pragma unroll
+  for (int b = 0; b < CB; b++) {
+    float2 hn = qn[b], hs = eq ? make_float2(0.f, 0.f) : qs[b];
+    if (k == 0 || k == half) {
+      hn.y = 0.f;
+      hs.y = 0.f;
+    } else {
+      hn = make_float2(0.5f * hn.x, 0.5f * (k < half ? hn.y : -hn.y));
+      hs = make_float2(0.5f * hs.x, 0.5f * (k < half ? hs.y : -hs.y));
+    }
+    out[b] = make_float2(hn.x - hs.y, hn.y + hs.x);
+  }
+}
+
+// Ring analysis of the equatorial ring pairs (q >= nside - 1: n = 4 nside, a power
+// of two) by one complex FFT per channel of z_j = north_j + i south_j, gathered in
+// bit-reversed order from global memory (shared-memory writes stay contiguous).
+template <int CB>
+__global__ __launch_bounds__(kThreads) void ring_analysis_fft_kernel(const float *__restrict__ maps, long long npix,
+                                                                     int nch, const RingPair *__restrict__ rings,
+                                                                     const float2 *__restrict__ tw2, int lmax, int R,
+                                                                     int N2, int q0, float *__restrict__ E,
+                                                                     float *__restrict__ O)
+{
+  extern __shared__ __align__(16) float2 z[];  // [CB][n]
+  const int q = q0 + blockIdx.x, cb0 = blockIdx.y * CB;
+  const RingPair rp = rings[q];
+  const int n = rp.nph, logn = __ffs(n) - 1;
+  const bool eq = (q == R - 1);
+  for (int d = threadIdx.x; d < n; d += blockDim.x) {
+    const int j = bit_reverse(d, logn);
+#pragma unroll
+    for (int b = 0; b < CB; b++) {
+      const int c = cb0 + b;
+      float xn = 0.f, xs = 0.f;
+      if (c < nch) {
+        xn = __ldg(maps + (long long)c * npix + rp.first_n + j);
+        if (!eq) xs = __ldg(maps + (long long)c * npix + rp.first_s + j);
+      }
+      z[b * n + d] = make_float2(xn, xs);
+    }
+  }
+  __syncthreads();
+  fft_dit<CB>(z, tw2, n, logn, -1.f);
+  write_eo<CB>(z, n, rp, q, eq, lmax, R, N2, nch, cb0, E, O);
+}
+
+// Ring synthesis of the equatorial ring pairs: the packed spectra, written in
+// bit-reversed order, through one complex inverse FFT whose real and imaginary
+// parts are the north and south rings' pixels.
 template <int CB>
 __global__ __launch_bounds__(kThreads) void ring_synthesis_fft_kernel(const float *__restrict__ Gn,
                                                                       const float *__restrict__ Gs,
                                                                       const RingPair *__restrict__ rings,
-                                                                      const float2 *__restrict__ tw_all, int lmax,
+                                                                      const float2 *__restrict__ tw2, int lmax,
                                                                       int R, int N2, int nch, int q0,
                                                                       float *__restrict__ maps, long long npix)
 {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(16) float2 z[];  // [CB][n]
   const int q = q0 + blockIdx.x, cb0 = blockIdx.y * CB;
   const RingPair rp = rings[q];
-  const int n = rp.nph, half = n / 2, logn = __ffs(n) - 1;
+  const int n = rp.nph, logn = __ffs(n) - 1;
   const bool eq = (q == R - 1);
-  float2 *tw = reinterpret_cast<float2 *>(smem_raw);
-  float2 *Q = tw + n;                   // [2][half + 1][CB]
-  float2 *z = Q + 2 * (half + 1) * CB;  // [CB][n]
-  for (int j = threadIdx.x; j < n; j += blockDim.x) tw[j] = tw_all[rp.tw_off + j];
-  fold_ring_sums<CB>(Gn, Gs, rp, q, eq, lmax, R, N2, nch, cb0, Q);
-  __syncthreads();
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    const int kk = k <= half ? k : n - k, kr = (int)(__brev((unsigned)k) >> (32 - logn));
+  for (int d = threadIdx.x; d < n; d += blockDim.x) {
+    float2 h[CB];
+    packed_spectrum<CB>(Gn, Gs, rp, q, eq, bit_reverse(d, logn), lmax, R, N2, nch, cb0, h);
 #pragma unroll
-    for (int b = 0; b < CB; b++) {
-      float2 hn = Q[kk * CB + b], hs = eq ? make_float2(0.f, 0.f) : Q[(half + 1 + kk) * CB + b];
-      if (k == 0 || k == half) {
-        hn.y = 0.f;
-        hs.y = 0.f;
-      } else {
-        hn = make_float2(0.5f * hn.x, 0.5f * (k < half ? hn.y : -hn.y));
-        hs = make_float2(0.5f * hs.x, 0.5f * (k < half ? hs.y : -hs.y));
-      }
-      z[b * n + kr] = make_float2(hn.x - hs.y, hn.y + hs.x);
-    }
+    for (int b = 0; b < CB; b++) z[b * n + d] = h[b];
   }
   __syncthreads();
-  smem_fft<CB>(z, tw, n, logn, 1.f);
+  fft_dit<CB>(z, tw2, n, logn, 1.f);
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
 #pragma unroll
     for (int b = 0; b < CB; b++) {
@@ -376,29 +420,6 @@ __global__ __launch_bounds__(kThreads) void ring_synthesis_fft_kernel(const floa
   }
 }
 
-
-// In-place radix-2 decimation-in-frequency FFT (natural order in, bit-reversed
-// out) of CB sequences of length n = 2^logn; tw[t] = e^{2 pi i t/n}.
-template <int CB>
-__device__ void smem_fft_dif(float2 *z, const float2 *tw, int n, int logn, float sign)
-{
-  for (int st = logn - 1; st >= 0; st--) {
-    const int h = 1 << st, step = n >> (st + 1);
-    for (int t = threadIdx.x; t < CB * (n >> 1); t += blockDim.x) {
-      const int b = t >> (logn - 1), u = t & ((n >> 1) - 1);
-      const int jj = u & (h - 1), i0 = ((u >> st) << (st + 1)) + jj;
-      float2 w = tw[jj * step];
-      w.y *= sign;
-      float2 *zb = z + b * n;
-      const float2 a = zb[i0], c = zb[i0 + h];
-      const float2 d = make_float2(a.x - c.x, a.y - c.y);
-      zb[i0] = make_float2(a.x + c.x, a.y + c.y);
-      zb[i0 + h] = make_float2(d.x * w.x - d.y * w.y, d.x * w.y + d.y * w.x);
-    }
-    __syncthreads();
-  }
-}
-
 // e^{-i pi j^2 / n}, the Bluestein chirp, with j^2 reduced exactly modulo 2n
 __device__ __forceinline__ float2 chirp(int j, int n)
 {
@@ -406,24 +427,24 @@ __device__ __forceinline__ float2 chirp(int j, int n)
   sincospif((float)((long long)j * j % (2 * n)) / (float)n, &sn, &cs);
   return make_float2(cs, -sn);
 }
-__device__ __forceinline__ float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 
 // Bluestein DFT of the CB sequences a[b][j], j < n (zero beyond, length M):
 // Z_k = c_k (a c) (*) conj(c), the convolution by a DIF FFT, the product with
-// the precomputed spectrum of conj(c) (bit-reversed order) and a DIT inverse
-// FFT; on return a[b][k] = Z_k for k < n.
+// the precomputed spectrum of conj(c) (bit-reversed order, global) and a DIT
+// inverse FFT; on return a[b][k] = Z_k for k < n.
 template <int CB>
-__device__ void bluestein(float2 *a, const float2 *Bt, const float2 *tw, int n, int M, int logM)
+__device__ void bluestein(float2 *a, const float2 *__restrict__ Bt, const float2 *__restrict__ tw2, int n, int M,
+                          int logM)
 {
   for (int t = threadIdx.x; t < CB * n; t += blockDim.x) {
     const int b = t / n, j = t - b * n;
     a[b * M + j] = cmul(a[b * M + j], chirp(j, n));
   }
   __syncthreads();
-  smem_fft_dif<CB>(a, tw, M, logM, -1.f);
-  for (int t = threadIdx.x; t < CB * M; t += blockDim.x) a[t] = cmul(a[t], Bt[t & (M - 1)]);
+  fft_dif<CB>(a, tw2, M, logM, -1.f);
+  for (int t = threadIdx.x; t < CB * M; t += blockDim.x) a[t] = cmul(a[t], __ldg(Bt + (t & (M - 1))));
   __syncthreads();
-  smem_fft<CB>(a, tw, M, logM, 1.f);
+  fft_dit<CB>(a, tw2, M, logM, 1.f);
   const float inv = 1.f / (float)M;
   for (int t = threadIdx.x; t < CB * n; t += blockDim.x) {
     const int b = t / n, k = t - b * n;
@@ -434,24 +455,17 @@ __device__ void bluestein(float2 *a, const float2 *Bt, const float2 *tw, int n, 
 }
 
 // Ring analysis of the polar ring pairs (q < nside - 1, n = 4 (q + 1) pixels)
-// by a Bluestein DFT of z_j = north_j + i south_j; then E and O as in
-// ring_analysis_fft_kernel.
+// by a Bluestein DFT of z_j = north_j + i south_j.
 template <int CB>
 __global__ __launch_bounds__(kThreads) void ring_analysis_bluestein_kernel(
     const float *__restrict__ maps, long long npix, int nch, const RingPair *__restrict__ rings,
     const float2 *__restrict__ tw2, const float2 *__restrict__ btab, int lmax, int R, int N2, float *__restrict__ E,
     float *__restrict__ O)
 {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(16) float2 a[];  // [CB][M]
   const int q = blockIdx.x, cb0 = blockIdx.y * CB;
   const RingPair rp = rings[q];
-  const int n = rp.nph, half = n / 2, M = rp.bm, logM = __ffs(M) - 1;
-  float2 *a = reinterpret_cast<float2 *>(smem_raw);  // [CB][M]
-  float2 *Bt = a + CB * M, *tw = Bt + M;
-  for (int t = threadIdx.x; t < M; t += blockDim.x) {
-    tw[t] = tw2[M + t];
-    Bt[t] = btab[rp.b_off + t];
-  }
+  const int n = rp.nph, M = rp.bm, logM = __ffs(M) - 1;
   for (int t = threadIdx.x; t < CB * M; t += blockDim.x) {
     const int b = t / M, j = t - b * M, c = cb0 + b;
     float2 v = make_float2(0.f, 0.f);
@@ -460,74 +474,35 @@ __global__ __launch_bounds__(kThreads) void ring_analysis_bluestein_kernel(
     a[t] = v;
   }
   __syncthreads();
-  bluestein<CB>(a, Bt, tw, n, M, logM);
-  for (int m = threadIdx.x; m <= lmax; m += blockDim.x) {
-    int k = m % n;
-    const bool cj = k > half;
-    if (cj) k = n - k;
-    float sn, cs;
-    sincospif((float)(m % (2 * n)) / (float)n, &sn, &cs);  // polar rings: phi0 = pi / n
-    const float2 ph = make_float2(cs, -sn);
-#pragma unroll
-    for (int b = 0; b < CB; b++) {
-      const int c = cb0 + b;
-      if (c >= nch) continue;
-      const float2 zk = a[b * M + k], zm = a[b * M + (k ? n - k : 0)];
-      float2 dn = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
-      float2 ds = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
-      if (cj) {
-        dn.y = -dn.y;
-        ds.y = -ds.y;
-      }
-      const float2 e = make_float2(dn.x + ds.x, dn.y + ds.y), o = make_float2(dn.x - ds.x, dn.y - ds.y);
-      const long long base = ((long long)m * R + q) * N2 + 2 * c;
-      *reinterpret_cast<float2 *>(E + base) = cmul(e, ph);
-      *reinterpret_cast<float2 *>(O + base) = cmul(o, ph);
-    }
-  }
+  bluestein<CB>(a, btab + rp.b_off, tw2, n, M, logM);
+  write_eo<CB>(a, M, rp, q, false, lmax, R, N2, nch, cb0, E, O);
 }
 
-// Ring synthesis of the polar ring pairs: the Hermitian-packed spectra
-// H_north + i H_south (as in ring_synthesis_fft_kernel) inverse-transformed as
-// conj(DFT(conj(.))) with the Bluestein DFT.
+// Ring synthesis of the polar ring pairs: the packed spectra inverse-transformed
+// as conj(DFT(conj(.))) with the Bluestein DFT.
 template <int CB>
 __global__ __launch_bounds__(kThreads) void ring_synthesis_bluestein_kernel(
     const float *__restrict__ Gn, const float *__restrict__ Gs, const RingPair *__restrict__ rings,
     const float2 *__restrict__ tw2, const float2 *__restrict__ btab, int lmax, int R, int N2, int nch,
     float *__restrict__ maps, long long npix)
 {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(16) float2 a[];  // [CB][M]
   const int q = blockIdx.x, cb0 = blockIdx.y * CB;
   const RingPair rp = rings[q];
-  const int n = rp.nph, half = n / 2, M = rp.bm, logM = __ffs(M) - 1;
-  float2 *a = reinterpret_cast<float2 *>(smem_raw);  // [CB][M]
-  float2 *Bt = a + CB * M, *tw = Bt + M;
-  for (int t = threadIdx.x; t < M; t += blockDim.x) {
-    tw[t] = tw2[M + t];
-    Bt[t] = btab[rp.b_off + t];
-  }
-  for (int t = threadIdx.x; t < CB * M; t += blockDim.x) a[t] = make_float2(0.f, 0.f);
-  __syncthreads();
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    const int kk = k <= half ? k : n - k;
-    float2 qn[CB], qs[CB];
-    fold_one<CB>(Gn, rp, q, kk, lmax, R, N2, nch, cb0, qn);
-    fold_one<CB>(Gs, rp, q, kk, lmax, R, N2, nch, cb0, qs);
+  const int n = rp.nph, M = rp.bm, logM = __ffs(M) - 1;
+  for (int k = threadIdx.x; k < M; k += blockDim.x) {
+    float2 h[CB];
+    if (k < n) {
+      packed_spectrum<CB>(Gn, Gs, rp, q, false, k, lmax, R, N2, nch, cb0, h);
+    } else {
 #pragma unroll
-    for (int b = 0; b < CB; b++) {
-      float2 hn = qn[b], hs = qs[b];
-      if (k == 0 || k == half) {
-        hn.y = 0.f;
-        hs.y = 0.f;
-      } else {
-        hn = make_float2(0.5f * hn.x, 0.5f * (k < half ? hn.y : -hn.y));
-        hs = make_float2(0.5f * hs.x, 0.5f * (k < half ? hs.y : -hs.y));
-      }
-      a[b * M + k] = make_float2(hn.x - hs.y, -(hn.y + hs.x));  // conj(H_north + i H_south)
+      for (int b = 0; b < CB; b++) h[b] = make_float2(0.f, 0.f);
     }
+#pragma unroll
+    for (int b = 0; b < CB; b++) a[b * M + k] = make_float2(h[b].x, -h[b].y);  // conjugated
   }
   __syncthreads();
-  bluestein<CB>(a, Bt, tw, n, M, logM);
+  bluestein<CB>(a, btab + rp.b_off, tw2, n, M, logM);
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
 #pragma unroll
     for (int b = 0; b < CB; b++) {
@@ -810,11 +785,11 @@ int jalloc(T **p, size_t count)
   return GETHI_OK;
 }
 
-size_t analysis_fft_smem(int n, int cb) { return (size_t)cb * n * 8 + (size_t)n * 8; }
-size_t synthesis_fft_smem(int n, int cb) { return (size_t)n * 8 + (size_t)2 * (n / 2 + 1) * cb * 8 + (size_t)cb * n * 8; }
-size_t bluestein_smem(int M, int cb) { return ((size_t)cb * M + 2 * (size_t)M) * 8; }
+size_t analysis_fft_smem(int n, int cb) { return (size_t)cb * n * 8; }
+size_t synthesis_fft_smem(int n, int cb) { return (size_t)cb * n * 8; }
+size_t bluestein_smem(int M, int cb) { return (size_t)cb * M * 8; }
 int ring_cb(long long nside) { return nside <= 512 ? 4 : 2; }        // channels per CTA, equatorial FFTs
-int bluestein_cb(long long nside) { return nside <= 512 ? 4 : 1; }   // channels per CTA, polar Bluestein
+int bluestein_cb(long long nside) { return nside <= 512 ? 2 : 1; }   // channels per CTA, polar Bluestein
 int bluestein_size(int n)  // the power of two >= 2n - 1
 {
   int M = 1;
@@ -996,11 +971,11 @@ int ensure_sht(joint_ctx *c)
     JCK(cudaFuncSetAttribute(ring_synthesis_fft_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)synthesis_fft_smem(ne, 2)));
   }
-  if (bluestein_cb(N) == 4) {
-    JCK(cudaFuncSetAttribute(ring_analysis_bluestein_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)bluestein_smem(mb, 4)));
-    JCK(cudaFuncSetAttribute(ring_synthesis_bluestein_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)bluestein_smem(mb, 4)));
+  if (bluestein_cb(N) == 2) {
+    JCK(cudaFuncSetAttribute(ring_analysis_bluestein_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)bluestein_smem(mb, 2)));
+    JCK(cudaFuncSetAttribute(ring_synthesis_bluestein_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)bluestein_smem(mb, 2)));
   } else {
     JCK(cudaFuncSetAttribute(ring_analysis_bluestein_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)bluestein_smem(mb, 1)));
@@ -1080,7 +1055,7 @@ int sht_analysis(joint_ctx *c, const float *dmaps, int nch, const float *sig2)
     KSpan k(c, 0);
     if (ring_cb(c->p.nside) == 4) launch_ring_analysis<4>(c, dmaps, nch);
     else launch_ring_analysis<2>(c, dmaps, nch);
-    if (bluestein_cb(c->p.nside) == 4) launch_polar_analysis<4>(c, dmaps, nch);
+    if (bluestein_cb(c->p.nside) == 2) launch_polar_analysis<2>(c, dmaps, nch);
     else launch_polar_analysis<1>(c, dmaps, nch);
   }
   JCK(cudaGetLastError());
@@ -1107,7 +1082,7 @@ int sht_synthesis(joint_ctx *c, float *dmaps, int nch)
     KSpan k(c, 3);
     if (ring_cb(c->p.nside) == 4) launch_ring_synthesis<4>(c, dmaps, nch);
     else launch_ring_synthesis<2>(c, dmaps, nch);
-    if (bluestein_cb(c->p.nside) == 4) launch_polar_synthesis<4>(c, dmaps, nch);
+    if (bluestein_cb(c->p.nside) == 2) launch_polar_synthesis<2>(c, dmaps, nch);
     else launch_polar_synthesis<1>(c, dmaps, nch);
   }
   JCK(cudaGetLastError());
