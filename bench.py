@@ -445,19 +445,39 @@ def bench_joint(args):
     nalm = (lmax + 1) * (lmax + 2) // 2
     gemm_bytes = 4.0 * (nalm * R + 2 * (lmax + 1) * R * N2 + nalm * N2)  # Legendre table + E/O + a_lm per batch
     gemm_flops = 2.0 * nalm * R * N2
-    dom = max(("legendre_analysis", "legendre_synthesis"), key=lambda k: kt[k][0])
-    per_launch = kt[dom][0] / kt[dom][1]
     peak_hbm, peak_kind = read_peaks()
-    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12  # TFLOP/s: SMs x FP32 lanes x 2 x max clock (nominal)
-    tflops = gemm_flops / (per_launch / 1e3) / 1e12
-    roof = {"bound": "fp32", "kernel": dom, "achieved": round(tflops, 2), "peak": round(fp32_peak, 1),
-            "unit": "TFLOP/s", "frac": round(tflops / fp32_peak, 3),
-            "peak_source": "nominal FP32 CUDA-core rate (152 SMs x 128 lanes x 2 x 2.07 GHz); no measured figure",
-            "flops_per_launch": gemm_flops, "avg_launch_ms": round(per_launch, 3),
-            "hbm": {"algorithmic_bytes_per_launch": gemm_bytes,
-                    "achieved_gbs": round(gemm_bytes / (per_launch / 1e3) / 1e9, 1), "peak_gbs": peak_hbm,
-                    "frac": round(gemm_bytes / (per_launch / 1e3) / 1e9 / peak_hbm, 3), "peak_source": peak_kind},
-            "traffic": None}
+    if j.uses_tensor_cores:
+        # the analysis GEMM alone (class "legendre_analysis" includes the E/O pack)
+        ms_tc = (kt["legendre_analysis"][0] - kt["legendre_pack"][0]) / kt["legendre_analysis"][1]
+        nkq = -(-R // 32)
+        tiles = sum(-(-((lmax - m) // 2 + 1 if p == 0 else (lmax - m + 1) // 2) // 128) * nkq
+                    for m in range(lmax + 1) for p in (0, 1))
+        packed = 32768.0 * (tiles + 2 * (lmax + 1) * nkq) + 8.0 * nalm * 128  # lambda + E/O tiles read, a_lm written
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            bf16 = float(json.load(f)["bf16_tflops"])
+        achieved = gemm_bytes / (ms_tc / 1e3) / 1e9
+        roof = {"bound": "hbm", "kernel": "tc_legendre_analysis", "achieved": round(achieved, 1),
+                "peak": peak_hbm, "unit": "GB/s", "frac": round(achieved / peak_hbm, 3), "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": gemm_bytes, "avg_launch_ms": round(ms_tc, 3),
+                "traffic": packed,
+                "traffic_source": "bytes of the packed operands per launch (hi and lo TF32 tiles of the Legendre "
+                                  "table and E/O, padded to 128 x 32 tiles, plus the packed a_lm written)",
+                "traffic_gbs": round(packed / (ms_tc / 1e3) / 1e9, 1),
+                "traffic_frac": round(packed / (ms_tc / 1e3) / 1e9 / peak_hbm, 3),
+                "tensor": {"tflops": round(3 * gemm_flops / (ms_tc / 1e3) / 1e12, 1),
+                           "peak_tflops": round(bf16 / 2, 1),
+                           "peak_source": "half the measured dense bf16 burst (TF32 runs at half the bf16 rate)",
+                           "frac": round(3 * gemm_flops / (ms_tc / 1e3) / 1e12 / (bf16 / 2), 3),
+                           "note": "3 TF32 MMAs per product (hi*hi, hi*lo, lo*hi)"}}
+    else:
+        dom = max(("legendre_analysis", "legendre_synthesis"), key=lambda k: kt[k][0])
+        per_launch = kt[dom][0] / kt[dom][1]
+        fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12  # TFLOP/s: SMs x FP32 lanes x 2 x max clock (nominal)
+        tflops = gemm_flops / (per_launch / 1e3) / 1e12
+        roof = {"bound": "fp32", "kernel": dom, "achieved": round(tflops, 2), "peak": round(fp32_peak, 1),
+                "unit": "TFLOP/s", "frac": round(tflops / fp32_peak, 3),
+                "peak_source": "nominal FP32 CUDA-core rate (152 SMs x 128 lanes x 2 x 2.07 GHz); no measured figure",
+                "flops_per_launch": gemm_flops, "avg_launch_ms": round(per_launch, 3), "traffic": None}
     line = {
         "metric": "JoinT map combination throughput (map pixels/s): Nside %d x %d channels, beam + noise + mask" % (
             nside, n_nu),
@@ -473,10 +493,11 @@ def bench_joint(args):
                    "l2": "inputs larger than L2 (maps %.1f GB, Legendre table above)" % (4 * units / 1e9)},
         "stage_ms": dict(zip(("merge", "beam", "noise", "mask"), np.round(stages / args.steps, 3).tolist())),
         "beam_kernels_ms": {k: round(v[0], 3) for k, v in kt.items()},
+        "legendre": "tensor cores (3xTF32, tcgen05)" if j.uses_tensor_cores else "FP32 CUDA cores",
         "roofline": roof,
         "e2e": {"value": whole_job_rate(units, args.steps, ws, e2e_ms), "unit": "pixels/s",
                 "h2d_bytes_per_step": int(4 * units * len(comp)), "d2h_bytes_per_step": int(4 * units)},
-        "gpu_launches": args.steps * (len(comp) + 4 * chunks + 2),
+        "gpu_launches": args.steps * (len(comp) + (7 if j.uses_tensor_cores else 6) * chunks + 2),
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:

@@ -35,6 +35,7 @@
 #include "common.cuh"
 #include "healpix.h"
 #include "host.h"
+#include "tc.cuh"
 
 using namespace gethi;
 
@@ -58,14 +59,29 @@ struct RingPair {
 // ---------------------------------------------------------------------------
 // merge, ud_grade, noise, mask
 // ---------------------------------------------------------------------------
-__global__ void add_kernel(float *__restrict__ acc, const float *__restrict__ src, long long n, double factor,
-                           int scaled)
+// acc += src (first: acc = 0 + src, which turns -0 into +0 exactly as the
+// reference's calloc'ed sum does); scaled: src first becomes (float)(src * factor)
+__device__ __forceinline__ float add_one(float a, float v, double factor, int scaled, int first)
 {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    float v = src[i];
-    if (scaled) v = (float)((double)v * factor);  // src/main_jt.c:181
-    acc[i] = __fadd_rn(acc[i], v);                // src/main_jt.c:94
+  if (scaled) v = (float)((double)v * factor);  // src/main_jt.c:181
+  return first ? __fadd_rn(v, 0.f) : __fadd_rn(a, v);  // src/main_jt.c:94
+}
+__global__ void add_kernel(float *__restrict__ acc, const float *__restrict__ src, long long n, double factor,
+                           int scaled, int first)
+{
+  const long long stride = (long long)gridDim.x * blockDim.x, i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const bool vec = ((reinterpret_cast<uintptr_t>(acc) | reinterpret_cast<uintptr_t>(src)) & 15) == 0;
+  const long long n4 = vec ? n / 4 : 0;
+  for (long long i = i0; i < n4; i += stride) {
+    const float4 v = reinterpret_cast<const float4 *>(src)[i];
+    float4 a = first ? make_float4(0.f, 0.f, 0.f, 0.f) : reinterpret_cast<const float4 *>(acc)[i];
+    a.x = add_one(a.x, v.x, factor, scaled, first);
+    a.y = add_one(a.y, v.y, factor, scaled, first);
+    a.z = add_one(a.z, v.z, factor, scaled, first);
+    a.w = add_one(a.w, v.w, factor, scaled, first);
+    reinterpret_cast<float4 *>(acc)[i] = a;
   }
+  for (long long i = 4 * n4 + i0; i < n; i += stride) acc[i] = add_one(first ? 0.f : acc[i], src[i], factor, scaled, first);
 }
 
 // he_udgrade, nside_in > nside_out: FP64 sum of the NESTED children in order, times 1/ratio
@@ -674,6 +690,342 @@ __global__ __launch_bounds__(kThreads, 2) void legendre_synthesis_kernel(const f
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// Legendre transforms on the tensor cores (3xTF32 on tcgen05)
+//
+// Operands live in HBM already packed as the MMA reads them: tiles of 128 rows
+// x 32 K elements (128 B per row) in the no-swizzle K-major layout (8-row x 16 B
+// core matrices, K-adjacent ones 128 B apart, 8-row groups 1 KB apart), hi
+// tile (16 KB) then lo tile (16 KB), hi = x rounded to TF32, lo = x - hi.  The
+// products hi*hi, hi*lo and lo*hi accumulate in two FP32 TMEM chains (error
+// about 2^-22 per element).  Analysis: D[l'][col] = lambda[l'][q] EO[col][q]
+// (A = the lambda table packed by rows l', B = E or O packed by channel
+// columns).  Synthesis: D[q][col] = lambda[l'][q] alm[col][l'] over both
+// parities (A = the lambda table packed by rows q, B = the a_lm the analysis
+// epilogue packs).  A CTA stages its tiles with 16-byte cp.async copies through
+// three shared-memory stages; one thread issues the MMAs and commits each stage
+// to an mbarrier; every wait is bounded (1 s of the global timer) and sets an
+// error flag the host reads.
+// ---------------------------------------------------------------------------
+namespace tcl {
+constexpr int kRows = 128, kK = 32;
+constexpr uint32_t kHalf = kRows * kK * 4;  // 16 KB: the hi or the lo tile
+constexpr uint32_t kTile = 2 * kHalf;       // 32 KB
+constexpr int kStages = 3;
+constexpr uint32_t kStageBytes = 2 * kTile;  // A and B of one K step
+constexpr size_t kSmem = kStages * kStageBytes;
+constexpr uint32_t kLBO = 128, kSBO = 1024;
+constexpr int kThreads = 128;
+constexpr uint64_t kWaitNs = 1000000000ull;
+}  // namespace tcl
+
+__host__ __device__ inline uint32_t tile_off(int r, int k)
+{
+  return (uint32_t)((r >> 3) * 1024 + (k >> 2) * 128 + (r & 7) * 16 + (k & 3) * 4);
+}
+
+__device__ __forceinline__ void split_tf32(float x, float &hi, float &lo)
+{
+  uint32_t h;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
+  hi = __uint_as_float(h);
+  lo = x - hi;
+}
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc::smem_addr(smem)), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// Pack one 128 x 32 tile: thread r writes row r (32 values of get(r, k)), hi and lo
+template <class Get>
+__device__ __forceinline__ void pack_tile(float *tile, Get get)
+{
+  const int r = threadIdx.x;
+#pragma unroll
+  for (int g = 0; g < 8; g++) {
+    float4 h, l;
+    split_tf32(get(r, 4 * g + 0), h.x, l.x);
+    split_tf32(get(r, 4 * g + 1), h.y, l.y);
+    split_tf32(get(r, 4 * g + 2), h.z, l.z);
+    split_tf32(get(r, 4 * g + 3), h.w, l.w);
+    const uint32_t o = tile_off(r, 4 * g) / 4;
+    *reinterpret_cast<float4 *>(tile + o) = h;
+    *reinterpret_cast<float4 *>(tile + tcl::kHalf / 4 + o) = l;
+  }
+}
+
+// lambda tables packed for the analysis (rows l', K = ring pairs; task = (m, p, l' tile,
+// K tile)) and for the synthesis (rows = ring pairs, K = l'; task = (m, p, q tile, K tile))
+__global__ void __launch_bounds__(tcl::kThreads) pack_lambda_kernel(const float *__restrict__ lam,
+                                                                    const int4 *__restrict__ tasks,
+                                                                    const long long *__restrict__ off, int R, int lmax,
+                                                                    int by_ring, float *__restrict__ out)
+{
+  const int4 t = tasks[blockIdx.x];
+  const int m = t.x, p = t.y;
+  const int ne = (lmax - m) / 2 + 1, M = p ? (lmax - m + 1) / 2 : ne;
+  const float *L = lam + (m_offset(m, lmax) + (p ? ne : 0)) * (long long)R;
+  const int nkq = (R + tcl::kK - 1) / tcl::kK, nkl = (M + tcl::kK - 1) / tcl::kK;
+  float *tile = out + (off[2 * m + p] + (long long)t.z * (by_ring ? nkl : nkq) + t.w) * (tcl::kTile / 4);
+  if (!by_ring) {
+    const int l0 = t.z * tcl::kRows, q0 = t.w * tcl::kK;
+    pack_tile(tile, [&](int r, int k) {
+      return (l0 + r < M && q0 + k < R) ? L[(long long)(l0 + r) * R + q0 + k] : 0.f;
+    });
+  } else {
+    const int qq = t.z * tcl::kRows, l0 = t.w * tcl::kK;
+    pack_tile(tile, [&](int r, int k) {
+      return (qq + r < R && l0 + k < M) ? L[(long long)(l0 + k) * R + qq + r] : 0.f;
+    });
+  }
+}
+
+// E and O packed by channel columns (rows = the 128 columns, K = ring pairs); one
+// CTA per (m, parity, K tile)
+__global__ void __launch_bounds__(tcl::kThreads) pack_eo_kernel(const float *__restrict__ E,
+                                                                const float *__restrict__ O, int R, int N2,
+                                                                float *__restrict__ out)
+{
+  const int nkq = (R + tcl::kK - 1) / tcl::kK;
+  const int kt = blockIdx.x % nkq, mp = blockIdx.x / nkq, m = mp >> 1, p = mp & 1;
+  const float *src = (p ? O : E) + (long long)m * R * N2;
+  const int q0 = kt * tcl::kK;
+  float *tile = out + (long long)blockIdx.x * (tcl::kTile / 4);
+  pack_tile(tile, [&](int r, int k) { return (q0 + k < R && r < N2) ? src[(long long)(q0 + k) * N2 + r] : 0.f; });
+}
+
+// the three MMAs of one K step (4 instructions of K = 8 each per 32-element tile)
+__device__ __forceinline__ void mma3(uint32_t acc0, uint32_t acc1, uint32_t a, uint32_t b, bool first)
+{
+  constexpr uint32_t idesc = tc::idesc_tf32_f32(128, 128);
+#pragma unroll
+  for (int kk = 0; kk < 4; kk++) {
+    const uint64_t ah = tc::smem_desc(a + 256 * kk, tcl::kLBO, tcl::kSBO);
+    const uint64_t al = tc::smem_desc(a + tcl::kHalf + 256 * kk, tcl::kLBO, tcl::kSBO);
+    const uint64_t bh = tc::smem_desc(b + 256 * kk, tcl::kLBO, tcl::kSBO);
+    const uint64_t bl = tc::smem_desc(b + tcl::kHalf + 256 * kk, tcl::kLBO, tcl::kSBO);
+    const uint32_t acc = (first && kk == 0) ? 0u : 1u;
+    tc::mma_tf32(acc0, ah, bh, idesc, acc);
+    tc::mma_tf32(acc1, ah, bl, idesc, acc);
+    tc::mma_tf32(acc1, al, bh, idesc, 1u);
+  }
+}
+
+// The K loop shared by both transforms: tiles kt = 0 .. nk-1, A and B of tile kt
+// at srcA(kt), srcB(kt); chain(kt) selects the accumulator pair and first(kt)
+// whether the tile starts it.  Returns false when an MMA wait expired.
+template <class SrcA, class SrcB, class Chain>
+__device__ bool tc_k_loop(unsigned char *sm, uint64_t *mbar, int nk, SrcA srcA, SrcB srcB, Chain chain, int *fail)
+{
+  const int tid = threadIdx.x;
+  auto load = [&](int kt) {
+    unsigned char *dst = sm + (kt % tcl::kStages) * tcl::kStageBytes;
+    const unsigned char *a = srcA(kt), *b = srcB(kt);
+    for (int i = tid; i < (int)(tcl::kStageBytes / 16); i += tcl::kThreads) {
+      const uint32_t o = 16u * i;
+      cp_async16(dst + o, o < tcl::kTile ? a + o : b + (o - tcl::kTile));
+    }
+  };
+  load(0);
+  cp_async_commit();
+  if (nk > 1) load(1);
+  cp_async_commit();
+  for (int kt = 0; kt < nk; kt++) {
+    const int s = kt % tcl::kStages;
+    cp_async_wait1();  // every group but the newest has landed: tile kt is in stage s
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      const uint32_t a = tc::smem_addr(sm + s * tcl::kStageBytes), b = a + tcl::kTile;
+      uint32_t acc0, acc1;
+      bool first;
+      chain(kt, acc0, acc1, first);
+      mma3(acc0, acc1, a, b, first);
+      tc::mma_commit(&mbar[s]);
+    }
+    if (kt + 2 < nk) {  // refill the stage of tile kt - 1 once its MMAs have completed
+      if (kt >= 1 && !tc::mbar_wait(&mbar[(kt - 1) % tcl::kStages], ((kt - 1) / tcl::kStages) & 1, tcl::kWaitNs))
+        *fail = 1;
+      load(kt + 2);
+    }
+    cp_async_commit();
+  }
+  if (!tc::mbar_wait(&mbar[(nk - 1) % tcl::kStages], ((nk - 1) / tcl::kStages) & 1, tcl::kWaitNs)) *fail = 1;
+  __syncthreads();
+  tc::fence_after_sync();
+  return *fail == 0;
+}
+
+// analysis, one CTA per (m, parity, 128-row l' tile): a_lm of the 128 channel
+// columns, weight and beam applied, written packed for the synthesis
+__global__ void __launch_bounds__(tcl::kThreads, 1)
+    tc_legendre_analysis_kernel(const float *__restrict__ LA, const long long *__restrict__ la_off,
+                                const float *__restrict__ EOp, float *__restrict__ almp,
+                                const long long *__restrict__ alm_off, const int4 *__restrict__ tasks, int R, int lmax,
+                                float w, const float *__restrict__ sig2, int *err)
+{
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ uint64_t mbar[tcl::kStages];
+  __shared__ uint32_t tslot;
+  __shared__ int fail;
+  const int4 t = tasks[blockIdx.x];
+  const int m = t.x, p = t.y, mt = t.z;
+  const int ne = (lmax - m) / 2 + 1, M = p ? (lmax - m + 1) / 2 : ne;
+  const int nkq = (R + tcl::kK - 1) / tcl::kK;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  __shared__ int skip;  // an earlier CTA's MMA wait expired: no new work (decided once for the CTA)
+  if (tid == 0) skip = *(volatile int *)err;
+  __syncthreads();
+  if (skip) return;
+  if (warp == 0) tc::tmem_alloc(&tslot, 256);
+  if (tid == 0) {
+    for (int i = 0; i < tcl::kStages; i++) tc::mbar_init(&mbar[i], 1);
+    fail = 0;
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tm = tslot;
+  const unsigned char *A0 = reinterpret_cast<const unsigned char *>(LA) + (la_off[2 * m + p] + (long long)mt * nkq) * tcl::kTile;
+  const unsigned char *B0 = reinterpret_cast<const unsigned char *>(EOp) + (long long)(2 * m + p) * nkq * tcl::kTile;
+  const bool ok = tc_k_loop(
+      sm, mbar, nkq, [&](int kt) { return A0 + (long long)kt * tcl::kTile; },
+      [&](int kt) { return B0 + (long long)kt * tcl::kTile; },
+      [&](int kt, uint32_t &a0, uint32_t &a1, bool &first) {
+        a0 = tm;
+        a1 = tm + 128;
+        first = kt == 0;
+      },
+      &fail);
+  if (ok) {
+    const int lp = mt * tcl::kRows + 32 * warp + lane;  // this thread's TMEM lane = row l'
+    const bool valid = lp < M;
+    const float l = (float)(m + 2 * lp + p);
+    float *tile = almp + (alm_off[2 * m + p] + (lp >> 5)) * (tcl::kTile / 4);
+    const uint32_t trow = tm + ((uint32_t)(32 * warp) << 16);
+#pragma unroll 1
+    for (int cb = 0; cb < 128; cb += 32) {
+      float v0[32], v1[32];
+      tc::tmem_ld32(trow + cb, v0);
+      tc::tmem_ld32(trow + 128 + cb, v1);
+      if (valid) {
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+          const int col = cb + j;
+          float sc = w;
+          if (sig2) sc *= expf(-0.5f * l * (l + 1.f) * sig2[col >> 1]);
+          float hi, lo;
+          split_tf32((v0[j] + v1[j]) * sc, hi, lo);
+          const uint32_t o = tile_off(col, lp & 31) / 4;
+          tile[o] = hi;
+          tile[tcl::kHalf / 4 + o] = lo;
+        }
+      }
+    }
+  } else {
+    if (tid == 0) atomicExch(err, 1);
+    // MMAs may still be in flight: wait once more (bounded) before freeing their TMEM
+    tc::mbar_wait(&mbar[(nkq - 1) % tcl::kStages], ((nkq - 1) / tcl::kStages) & 1, tcl::kWaitNs);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tm, 256);
+}
+
+// synthesis, one CTA per (m, 128 ring pairs): G_e and G_o over the packed a_lm of
+// both parities; north = G_e + G_o, south = G_e - G_o, FP32 [m][q][col]
+__global__ void __launch_bounds__(tcl::kThreads, 1)
+    tc_legendre_synthesis_kernel(const float *__restrict__ LS, const long long *__restrict__ ls_off,
+                                 const float *__restrict__ almp, const long long *__restrict__ alm_off,
+                                 const int4 *__restrict__ tasks, int R, int lmax, int N2, float *__restrict__ Gn,
+                                 float *__restrict__ Gs, int *err)
+{
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ uint64_t mbar[tcl::kStages];
+  __shared__ uint32_t tslot;
+  __shared__ int fail;
+  const int4 t = tasks[blockIdx.x];
+  const int m = t.x, qt = t.z;
+  const int ne = (lmax - m) / 2 + 1, no = (lmax - m + 1) / 2;
+  const int nke = (ne + tcl::kK - 1) / tcl::kK, nko = (no + tcl::kK - 1) / tcl::kK;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  __shared__ int skip;  // an earlier CTA's MMA wait expired: no new work (decided once for the CTA)
+  if (tid == 0) skip = *(volatile int *)err;
+  __syncthreads();
+  if (skip) return;
+  if (warp == 0) tc::tmem_alloc(&tslot, 512);
+  if (tid == 0) {
+    for (int i = 0; i < tcl::kStages; i++) tc::mbar_init(&mbar[i], 1);
+    fail = 0;
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tm = tslot;
+  const unsigned char *LSb = reinterpret_cast<const unsigned char *>(LS);
+  const unsigned char *Ab = reinterpret_cast<const unsigned char *>(almp);
+  const bool ok = tc_k_loop(
+      sm, mbar, nke + nko,
+      [&](int kt) {
+        const int p = kt >= nke, k = p ? kt - nke : kt, nk = p ? nko : nke;
+        return LSb + (ls_off[2 * m + p] + (long long)qt * nk + k) * tcl::kTile;
+      },
+      [&](int kt) {
+        const int p = kt >= nke, k = p ? kt - nke : kt;
+        return Ab + (alm_off[2 * m + p] + k) * tcl::kTile;
+      },
+      [&](int kt, uint32_t &a0, uint32_t &a1, bool &first) {
+        const int p = kt >= nke;
+        a0 = tm + 256 * p;
+        a1 = a0 + 128;
+        first = kt == 0 || kt == nke;
+      },
+      &fail);
+  if (ok) {
+    const int q = qt * tcl::kRows + 32 * warp + lane;
+    const uint32_t trow = tm + ((uint32_t)(32 * warp) << 16);
+    float *gn = Gn + ((long long)m * R + q) * N2, *gs = Gs + ((long long)m * R + q) * N2;
+#pragma unroll 1
+    for (int cb = 0; cb < 128; cb += 32) {
+      float e0[32], e1[32], o0[32], o1[32];
+      tc::tmem_ld32(trow + cb, e0);
+      tc::tmem_ld32(trow + 128 + cb, e1);
+      tc::tmem_ld32(trow + 256 + cb, o0);
+      tc::tmem_ld32(trow + 384 + cb, o1);
+      if (q < R) {
+#pragma unroll
+        for (int j = 0; j < 32; j += 4) {
+          if (cb + j + 3 >= N2) break;
+          float4 vn, vs;
+          float ev[4], ov[4];
+#pragma unroll
+          for (int i = 0; i < 4; i++) {
+            ev[i] = e0[j + i] + e1[j + i];
+            ov[i] = nko ? o0[j + i] + o1[j + i] : 0.f;
+          }
+          vn = make_float4(ev[0] + ov[0], ev[1] + ov[1], ev[2] + ov[2], ev[3] + ov[3]);
+          vs = make_float4(ev[0] - ov[0], ev[1] - ov[1], ev[2] - ov[2], ev[3] - ov[3]);
+          *reinterpret_cast<float4 *>(gn + cb + j) = vn;
+          *reinterpret_cast<float4 *>(gs + cb + j) = vs;
+        }
+      }
+    }
+  } else {
+    if (tid == 0) atomicExch(err, 1);
+    const int nk = nke + nko;  // MMAs may still be in flight: wait once more (bounded)
+    tc::mbar_wait(&mbar[(nk - 1) % tcl::kStages], ((nk - 1) / tcl::kStages) & 1, tcl::kWaitNs);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tm, 512);
+}
+
 // internal a_lm [m][parity][l'][2c] <-> HEALPix order [c][l + m lmax - m(m-1)/2] (complex)
 __global__ void alm_to_healpix_kernel(const float *__restrict__ alm, float2 *__restrict__ out, int lmax, int N2,
                                       int nch, long long nalm)
@@ -749,15 +1101,22 @@ struct joint_ctx {
   int4 *tasks_a = nullptr, *tasks_s = nullptr;
   int ntasks_a = 0, ntasks_s = 0;
   double *noise_h = nullptr, *noise_d = nullptr;  // mt_validation staging (pinned host, device)
+  // tensor-core Legendre sums: packed tables, offsets (in 32 KB tiles per (m, parity)), task lists
+  bool use_tc = false;
+  float *LA = nullptr, *LS = nullptr, *EOp = nullptr, *almp = nullptr;
+  long long *la_off = nullptr, *ls_off = nullptr, *alm_off = nullptr;
+  int4 *tasks_ta = nullptr, *tasks_ts = nullptr;
+  int ntasks_ta = 0, ntasks_ts = 0;
+  int *tc_err = nullptr;
   cudaEvent_t ev[5] = {};
   float times[4] = {};
   // optional per-kernel-class device times of the beam (joint_gpu_profile):
-  // ring analysis, Legendre analysis, Legendre synthesis, ring synthesis
+  // ring analysis, Legendre analysis, Legendre synthesis, ring synthesis, E/O pack
   int prof = 0;
   std::vector<cudaEvent_t> kev;
   std::vector<int> kcls;
-  double ktime[4] = {};
-  long kcount[4] = {};
+  double ktime[5] = {};
+  long kcount[5] = {};
 };
 
 namespace {
@@ -828,6 +1187,76 @@ void host_fft(std::vector<double> &re, std::vector<double> &im)
         im[a] += vi;
       }
   }
+}
+
+
+// packed lambda tables, offsets and task lists of the tensor-core Legendre sums
+int ensure_tc_tables(joint_ctx *c)
+{
+  const int R = c->R, lmax = c->lmax;
+  const int nkq = (R + tcl::kK - 1) / tcl::kK, nqt = (R + tcl::kRows - 1) / tcl::kRows;
+  std::vector<long long> la(2 * (lmax + 1)), ls(2 * (lmax + 1)), al(2 * (lmax + 1));
+  std::vector<int4> pa, ps, ta, ts;
+  long long na = 0, ns = 0, nl = 0;
+  for (int m = 0; m <= lmax; m++) {
+    for (int p = 0; p < 2; p++) {
+      const int M = p ? (lmax - m + 1) / 2 : (lmax - m) / 2 + 1;
+      const int nmt = (M + tcl::kRows - 1) / tcl::kRows, nkl = (M + tcl::kK - 1) / tcl::kK;
+      la[2 * m + p] = na;
+      ls[2 * m + p] = ns;
+      al[2 * m + p] = nl;
+      for (int mt = 0; mt < nmt; mt++) {
+        ta.push_back(make_int4(m, p, mt, 0));
+        for (int kt = 0; kt < nkq; kt++) pa.push_back(make_int4(m, p, mt, kt));
+      }
+      for (int qt = 0; qt < nqt; qt++)
+        for (int kt = 0; kt < nkl; kt++) ps.push_back(make_int4(m, p, qt, kt));
+      na += (long long)nmt * nkq;
+      ns += (long long)nqt * nkl;
+      nl += nkl;
+    }
+    for (int qt = 0; qt < nqt; qt++) ts.push_back(make_int4(m, 0, qt, 0));
+  }
+  const size_t tw4 = tcl::kTile / 4;
+  int rc;
+  int4 *dpa = nullptr, *dps = nullptr;
+  if ((rc = jalloc(&c->LA, (size_t)na * tw4)) || (rc = jalloc(&c->LS, (size_t)ns * tw4)) ||
+      (rc = jalloc(&c->EOp, (size_t)2 * (lmax + 1) * nkq * tw4)) || (rc = jalloc(&c->almp, (size_t)nl * tw4)) ||
+      (rc = jalloc(&c->la_off, la.size())) || (rc = jalloc(&c->ls_off, ls.size())) ||
+      (rc = jalloc(&c->alm_off, al.size())) || (rc = jalloc(&c->tasks_ta, ta.size())) ||
+      (rc = jalloc(&c->tasks_ts, ts.size())) || (rc = jalloc(&c->tc_err, 1)) || (rc = jalloc(&dpa, pa.size())) ||
+      (rc = jalloc(&dps, ps.size()))) {
+    cudaFree(dpa);
+    for (void **ptr : {(void **)&c->LA, (void **)&c->LS, (void **)&c->EOp, (void **)&c->almp, (void **)&c->la_off,
+                       (void **)&c->ls_off, (void **)&c->alm_off, (void **)&c->tasks_ta, (void **)&c->tasks_ts,
+                       (void **)&c->tc_err}) {
+      cudaFree(*ptr);
+      *ptr = nullptr;
+    }
+    return rc;
+  }
+  c->ntasks_ta = (int)ta.size();
+  c->ntasks_ts = (int)ts.size();
+  JCK(cudaMemcpyAsync(c->la_off, la.data(), sizeof(long long) * la.size(), cudaMemcpyHostToDevice, c->stream));
+  JCK(cudaMemcpyAsync(c->ls_off, ls.data(), sizeof(long long) * ls.size(), cudaMemcpyHostToDevice, c->stream));
+  JCK(cudaMemcpyAsync(c->alm_off, al.data(), sizeof(long long) * al.size(), cudaMemcpyHostToDevice, c->stream));
+  JCK(cudaMemcpyAsync(c->tasks_ta, ta.data(), sizeof(int4) * ta.size(), cudaMemcpyHostToDevice, c->stream));
+  JCK(cudaMemcpyAsync(c->tasks_ts, ts.data(), sizeof(int4) * ts.size(), cudaMemcpyHostToDevice, c->stream));
+  JCK(cudaMemcpyAsync(dpa, pa.data(), sizeof(int4) * pa.size(), cudaMemcpyHostToDevice, c->stream));
+  JCK(cudaMemcpyAsync(dps, ps.data(), sizeof(int4) * ps.size(), cudaMemcpyHostToDevice, c->stream));
+  JCK(cudaMemsetAsync(c->almp, 0, sizeof(float) * nl * tw4, c->stream));  // l' padding stays zero
+  JCK(cudaMemsetAsync(c->tc_err, 0, sizeof(int), c->stream));
+  pack_lambda_kernel<<<(unsigned)pa.size(), tcl::kThreads, 0, c->stream>>>(c->lam, dpa, c->la_off, R, lmax, 0, c->LA);
+  JCK(cudaGetLastError());
+  pack_lambda_kernel<<<(unsigned)ps.size(), tcl::kThreads, 0, c->stream>>>(c->lam, dps, c->ls_off, R, lmax, 1, c->LS);
+  JCK(cudaGetLastError());
+  JCK(cudaFuncSetAttribute(tc_legendre_analysis_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcl::kSmem));
+  JCK(cudaFuncSetAttribute(tc_legendre_synthesis_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcl::kSmem));
+  JCK(cudaStreamSynchronize(c->stream));
+  cudaFree(dpa);
+  cudaFree(dps);
+  c->use_tc = true;
+  return GETHI_OK;
 }
 
 // ring pairs, twiddles and the Legendre table of the context's nside (first transform)
@@ -983,6 +1412,14 @@ int ensure_sht(joint_ctx *c)
                              (int)bluestein_smem(mb, 1)));
   }
   c->bmax = mb;
+  if (c->p.sht_precision == 0 && N <= 512 && c->N2 == 128) {
+    int rt = ensure_tc_tables(c);
+    if (rt == GETHI_E_NOMEM) {  // the packed tables do not fit: FP32 CUDA cores
+      cudaGetLastError();
+      rt = GETHI_OK;
+    }
+    if (rt) return rt;
+  }
   JCK(cudaStreamSynchronize(c->stream));
   return GETHI_OK;
 }
@@ -1036,20 +1473,26 @@ struct KSpan {
   }
 };
 
-void collect_kernel_times(joint_ctx *c)  // after a synchronize
+void collect_kernel_times(joint_ctx *c)  // after a synchronize; spans may nest
 {
-  for (size_t i = 0; i + 1 < c->kev.size(); i += 2) {
-    float ms = 0;
-    cudaEventElapsedTime(&ms, c->kev[i], c->kev[i + 1]);
-    c->ktime[c->kcls[i]] += ms;
-    c->kcount[c->kcls[i]]++;
+  std::vector<size_t> open;
+  for (size_t i = 0; i < c->kev.size(); i++) {
+    if (!open.empty() && c->kcls[open.back()] == c->kcls[i]) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, c->kev[open.back()], c->kev[i]);
+      c->ktime[c->kcls[i]] += ms;
+      c->kcount[c->kcls[i]]++;
+      open.pop_back();
+    } else {
+      open.push_back(i);
+    }
   }
   for (cudaEvent_t e : c->kev) cudaEventDestroy(e);
   c->kev.clear();
   c->kcls.clear();
 }
 
-int sht_analysis(joint_ctx *c, const float *dmaps, int nch, const float *sig2)
+int sht_analysis(joint_ctx *c, const float *dmaps, int nch, const float *sig2, bool tc)
 {
   {
     KSpan k(c, 0);
@@ -1061,21 +1504,35 @@ int sht_analysis(joint_ctx *c, const float *dmaps, int nch, const float *sig2)
   JCK(cudaGetLastError());
   const float w = (float)(4.0 * M_PI / (double)c->npix);
   {
-    KSpan k(c, 1);
-    legendre_analysis_kernel<<<c->ntasks_a, kThreads, 0, c->stream>>>(c->lam, c->E, c->O, c->alm, c->tasks_a, c->R,
-                                                                      c->lmax, c->N2, w, sig2);
+    KSpan k(c, 1);  // the pack's own span (class 4) nests inside: class 1 = pack + GEMM
+    if (tc) {
+      const int nkq = (c->R + tcl::kK - 1) / tcl::kK;
+      {
+        KSpan kp(c, 4);
+        pack_eo_kernel<<<2 * (c->lmax + 1) * nkq, tcl::kThreads, 0, c->stream>>>(c->E, c->O, c->R, c->N2, c->EOp);
+      }
+      tc_legendre_analysis_kernel<<<c->ntasks_ta, tcl::kThreads, tcl::kSmem, c->stream>>>(
+          c->LA, c->la_off, c->EOp, c->almp, c->alm_off, c->tasks_ta, c->R, c->lmax, w, sig2, c->tc_err);
+    } else {
+      legendre_analysis_kernel<<<c->ntasks_a, kThreads, 0, c->stream>>>(c->lam, c->E, c->O, c->alm, c->tasks_a,
+                                                                        c->R, c->lmax, c->N2, w, sig2);
+    }
   }
   JCK(cudaGetLastError());
   return GETHI_OK;
 }
 
 // alm2map of c->alm into nch device maps
-int sht_synthesis(joint_ctx *c, float *dmaps, int nch)
+int sht_synthesis(joint_ctx *c, float *dmaps, int nch, bool tc)
 {
   {
     KSpan k(c, 2);
-    legendre_synthesis_kernel<<<c->ntasks_s, kThreads, 0, c->stream>>>(c->lam, c->alm, c->E, c->O, c->tasks_s,
-                                                                       c->R, c->lmax, c->N2);
+    if (tc)
+      tc_legendre_synthesis_kernel<<<c->ntasks_ts, tcl::kThreads, tcl::kSmem, c->stream>>>(
+          c->LS, c->ls_off, c->almp, c->alm_off, c->tasks_ts, c->R, c->lmax, c->N2, c->E, c->O, c->tc_err);
+    else
+      legendre_synthesis_kernel<<<c->ntasks_s, kThreads, 0, c->stream>>>(c->lam, c->alm, c->E, c->O, c->tasks_s,
+                                                                         c->R, c->lmax, c->N2);
   }
   JCK(cudaGetLastError());
   {
@@ -1167,7 +1624,9 @@ extern "C" void joint_gpu_free(joint_ctx *c)
   for (void *ptr : {(void *)c->maps, (void *)c->acc, (void *)c->stage_buf, (void *)c->dmask, (void *)c->s2,
                     (void *)c->rings, (void *)c->tw2, (void *)c->btab, (void *)c->lam, (void *)c->E, (void *)c->O, (void *)c->alm,
                     (void *)c->sig2, (void *)c->tmp_maps, (void *)c->alm_hp, (void *)c->tasks_a, (void *)c->tasks_s,
-                    (void *)c->noise_d})
+                    (void *)c->noise_d, (void *)c->LA, (void *)c->LS, (void *)c->EOp, (void *)c->almp,
+                    (void *)c->la_off, (void *)c->ls_off, (void *)c->alm_off, (void *)c->tasks_ta,
+                    (void *)c->tasks_ts, (void *)c->tc_err})
     cudaFree(ptr);
   if (c->noise_h) cudaFreeHost(c->noise_h);
   for (cudaEvent_t e : c->kev) cudaEventDestroy(e);
@@ -1205,12 +1664,14 @@ static int add_common(joint_ctx *c, const float *dsrc, long nside_in, double fac
       if (rc) return rc;
       c->acc_cap = n;
     }
-    JCK(cudaMemsetAsync(c->acc, 0, sizeof(float) * n, c->stream));
     c->nside_in = nside_in;
     c->stage = 1;
     c->have_acc = true;
+    add_kernel<<<grid_for(n), kThreads, 0, c->stream>>>(c->acc, dsrc, n, factor, factor != 1.0, 1);
+    JCK(cudaGetLastError());
+    return GETHI_OK;
   }
-  add_kernel<<<grid_for(n), kThreads, 0, c->stream>>>(c->acc, dsrc, n, factor, factor != 1.0);
+  add_kernel<<<grid_for(n), kThreads, 0, c->stream>>>(c->acc, dsrc, n, factor, factor != 1.0, 0);
   JCK(cudaGetLastError());
   return GETHI_OK;
 }
@@ -1295,8 +1756,8 @@ extern "C" int joint_gpu_apply_beam(joint_ctx *c)
     }
     JCK(cudaMemcpyAsync(c->sig2, sg.data(), sizeof(float) * c->chunk, cudaMemcpyHostToDevice, c->stream));
     float *m = c->maps + (long long)c0 * c->npix;
-    if ((rc = sht_analysis(c, m, nch, c->sig2))) return rc;
-    if ((rc = sht_synthesis(c, m, nch))) return rc;
+    if ((rc = sht_analysis(c, m, nch, c->sig2, c->use_tc))) return rc;
+    if ((rc = sht_synthesis(c, m, nch, c->use_tc))) return rc;
   }
   return GETHI_OK;
 }
@@ -1363,6 +1824,20 @@ extern "C" int joint_gpu_apply_mask(joint_ctx *c)
   return GETHI_OK;
 }
 
+// an expired MMA wait in the tensor-core Legendre sums (read after a synchronize)
+static int check_tc(joint_ctx *c)
+{
+  if (!c->tc_err) return GETHI_OK;
+  int e = 0;
+  JCK(cudaMemcpy(&e, c->tc_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) {
+    cudaMemset(c->tc_err, 0, sizeof(int));
+    set_error("tensor-core Legendre sums: an MMA completion wait expired");
+    return GETHI_E_DEVICE;
+  }
+  return GETHI_OK;
+}
+
 extern "C" int joint_gpu_get_maps(joint_ctx *c, float *maps_out)
 {
   if (!c || !maps_out) return GETHI_E_ARG;
@@ -1371,7 +1846,7 @@ extern "C" int joint_gpu_get_maps(joint_ctx *c, float *maps_out)
   JCK(cudaSetDevice(c->device));
   JCK(cudaMemcpyAsync(maps_out, c->maps, sizeof(float) * c->npix * c->p.n_nu, cudaMemcpyDeviceToHost, c->stream));
   JCK(cudaStreamSynchronize(c->stream));
-  return GETHI_OK;
+  return check_tc(c);
 }
 
 extern "C" int joint_gpu_device_maps(const joint_ctx *c, const float **dmaps)
@@ -1402,8 +1877,10 @@ extern "C" int joint_gpu_run(joint_ctx *c, float *maps_out)
   }
   for (int i = 0; i < 4; i++) cudaEventElapsedTime(&c->times[i], c->ev[i], c->ev[i + 1]);
   collect_kernel_times(c);
-  return GETHI_OK;
+  return check_tc(c);
 }
+
+extern "C" int joint_gpu_uses_tensor_cores(const joint_ctx *c) { return c && c->use_tc ? 1 : 0; }
 
 extern "C" int joint_gpu_profile(joint_ctx *c, int on)
 {
@@ -1411,21 +1888,21 @@ extern "C" int joint_gpu_profile(joint_ctx *c, int on)
   JCK(cudaStreamSynchronize(c->stream));
   collect_kernel_times(c);
   c->prof = on ? 1 : 0;
-  for (int i = 0; i < 4; i++) {
+  for (int i = 0; i < 5; i++) {
     c->ktime[i] = 0;
     c->kcount[i] = 0;
   }
   return GETHI_OK;
 }
 
-extern "C" int joint_gpu_kernel_times(joint_ctx *c, double *ms4, long *launches4)
+extern "C" int joint_gpu_kernel_times(joint_ctx *c, double *ms5, long *launches5)
 {
-  if (!c || !ms4) return GETHI_E_ARG;
+  if (!c || !ms5) return GETHI_E_ARG;
   JCK(cudaStreamSynchronize(c->stream));
   collect_kernel_times(c);
-  for (int i = 0; i < 4; i++) {
-    ms4[i] = c->ktime[i];
-    if (launches4) launches4[i] = c->kcount[i];
+  for (int i = 0; i < 5; i++) {
+    ms5[i] = c->ktime[i];
+    if (launches5) launches5[i] = c->kcount[i];
   }
   return GETHI_OK;
 }
@@ -1453,7 +1930,7 @@ static int sht_api(joint_ctx *c, const float *in, int n_maps, float *out, bool a
     if (analysis) {
       JCK(cudaMemcpyAsync(c->tmp_maps, in + (long long)c0 * c->npix, sizeof(float) * nch * c->npix,
                           cudaMemcpyHostToDevice, c->stream));
-      if ((rc = sht_analysis(c, c->tmp_maps, nch, nullptr))) return rc;
+      if ((rc = sht_analysis(c, c->tmp_maps, nch, nullptr, false))) return rc;  // a_lm in the FP32 layout
       alm_to_healpix_kernel<<<grid_for(nalm * nch), kThreads, 0, c->stream>>>(c->alm, c->alm_hp, c->lmax, c->N2, nch,
                                                                               nalm);
       JCK(cudaGetLastError());
@@ -1465,7 +1942,7 @@ static int sht_api(joint_ctx *c, const float *in, int n_maps, float *out, bool a
       alm_from_healpix_kernel<<<grid_for(nalm * nch), kThreads, 0, c->stream>>>(c->alm_hp, c->alm, c->lmax, c->N2,
                                                                                 nch, nalm);
       JCK(cudaGetLastError());
-      if ((rc = sht_synthesis(c, c->tmp_maps, nch))) return rc;
+      if ((rc = sht_synthesis(c, c->tmp_maps, nch, false))) return rc;
       JCK(cudaMemcpyAsync(out + (long long)c0 * c->npix, c->tmp_maps, sizeof(float) * nch * c->npix,
                           cudaMemcpyDeviceToHost, c->stream));
     }

@@ -30,7 +30,7 @@ class JointParams(C.Structure):
     _fields_ = [("nside", C.c_int), ("n_nu", C.c_int), ("nu0", C.c_void_p), ("nuf", C.c_void_p),
                 ("seed", C.c_uint), ("dish_diameter", C.c_double), ("n_dish", C.c_int), ("tsys", C.c_double),
                 ("time_tot", C.c_double), ("mask", C.c_void_p), ("rng", C.c_int),
-                ("omp_threads_for_noise", C.c_int), ("sht_chunk", C.c_int)]
+                ("omp_threads_for_noise", C.c_int), ("sht_chunk", C.c_int), ("sht_precision", C.c_int)]
 
 
 _bound = False
@@ -58,6 +58,7 @@ def lib():
         L.joint_gpu_alm2map.argtypes = [vp, vp, C.c_int, vp]
         L.joint_gpu_stage_times.argtypes = [vp, vp]
         L.joint_gpu_profile.argtypes = [vp, C.c_int]
+        L.joint_gpu_uses_tensor_cores.argtypes = [vp]
         L.joint_gpu_kernel_times.argtypes = [vp, vp, vp]
         L.joint_host_read_map.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_long), vp]
         L.joint_host_read_nutable.argtypes = [C.c_char_p, C.POINTER(C.c_int), vp, vp]
@@ -100,7 +101,7 @@ class JoinT:
     """One JoinT configuration on one GPU (include/joint_gpu.h)."""
 
     def __init__(self, nside, nu0, nuf, seed=1, dish_diameter=-1.0, n_dish=1, tsys=-1.0, time_tot=1.0, mask=None,
-                 rng="philox", omp_threads_for_noise=1, sht_chunk=0, device=0):
+                 rng="philox", omp_threads_for_noise=1, sht_chunk=0, sht_precision="auto", device=0):
         self.nu0 = np.ascontiguousarray(nu0, np.float64)
         self.nuf = np.ascontiguousarray(nuf, np.float64)
         self.mask = None if mask is None else np.ascontiguousarray(mask, np.int32)
@@ -108,7 +109,9 @@ class JoinT:
                         seed=seed, dish_diameter=dish_diameter, n_dish=n_dish, tsys=tsys, time_tot=time_tot,
                         mask=None if self.mask is None else self.mask.ctypes.data,
                         rng=RNG[rng] if isinstance(rng, str) else rng, omp_threads_for_noise=omp_threads_for_noise,
-                        sht_chunk=sht_chunk)
+                        sht_chunk=sht_chunk,
+                        sht_precision={"auto": 0, "fp32": 1}[sht_precision] if isinstance(sht_precision, str)
+                        else sht_precision)
         self.params = p
         self.nside, self.n_nu = nside, len(self.nu0)
         self.npix = 12 * nside * nside
@@ -126,6 +129,10 @@ class JoinT:
             self.close()
         except Exception:
             pass
+
+    @property
+    def uses_tensor_cores(self):
+        return bool(lib().joint_gpu_uses_tensor_cores(self._ctx))
 
     @property
     def fsky(self):
@@ -177,14 +184,14 @@ class JoinT:
         _check(lib().joint_gpu_stage_times(self._ctx, t.ctypes.data))
         return dict(zip(("merge", "beam", "noise", "mask"), t.tolist()))
 
-    BEAM_KERNELS = ("ring_analysis", "legendre_analysis", "legendre_synthesis", "ring_synthesis")
+    BEAM_KERNELS = ("ring_analysis", "legendre_analysis", "legendre_synthesis", "ring_synthesis", "legendre_pack")
 
     def profile(self, on=True):
         _check(lib().joint_gpu_profile(self._ctx, 1 if on else 0))
 
     def kernel_times(self):
         """{class: (device ms, launches)} of the beam while profiling"""
-        ms, n = np.zeros(4), np.zeros(4, np.int64)
+        ms, n = np.zeros(5), np.zeros(5, np.int64)
         _check(lib().joint_gpu_kernel_times(self._ctx, ms.ctypes.data, n.ctypes.data))
         return {k: (float(a), int(b)) for k, a, b in zip(self.BEAM_KERNELS, ms, n)}
 

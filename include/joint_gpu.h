@@ -41,6 +41,8 @@ typedef struct {
   int rng;                   /* JOINT_RNG_* */
   int omp_threads_for_noise; /* JOINT_RNG_MT_VALIDATION: OpenMP threads of the emulated reference run */
   int sht_chunk;             /* channels per spherical-harmonic batch; 0: automatic */
+  int sht_precision;         /* Legendre sums: 0 = tensor cores (3xTF32) where their tables fit (nside <= 512),
+                                else FP32 CUDA cores; 1 = FP32 CUDA cores */
 } joint_params;
 
 typedef struct joint_ctx joint_ctx;
@@ -90,14 +92,17 @@ double joint_gpu_fsky(const joint_ctx *c);
 int joint_gpu_map2alm(joint_ctx *c, const float *maps, int n_maps, float *alms);
 int joint_gpu_alm2map(joint_ctx *c, const float *alms, int n_maps, float *maps);
 
+/* 1 when the context's Legendre sums run on the tensor cores (known after the first transform) */
+int joint_gpu_uses_tensor_cores(const joint_ctx *c);
 /* device time of the last joint_gpu_run per stage (ms): merge, beam, noise, mask */
 int joint_gpu_stage_times(const joint_ctx *c, float *ms4);
 /* Per-kernel-class device times of the beam, accumulated while profiling is on
  * (events around each class; off by default): ring analysis (FFT + Bluestein),
- * Legendre analysis GEMM, Legendre synthesis GEMM, ring synthesis.  Turning
- * profiling on or off resets the sums.  No counterpart in the reference. */
+ * Legendre analysis (including the E/O pack of the tensor-core path), Legendre
+ * synthesis, ring synthesis, E/O pack alone.  Turning profiling on or off resets
+ * the sums.  No counterpart in the reference. */
 int joint_gpu_profile(joint_ctx *c, int on);
-int joint_gpu_kernel_times(joint_ctx *c, double *ms4, long *launches4);
+int joint_gpu_kernel_times(joint_ctx *c, double *ms5, long *launches5);
 
 /* ---- host helpers (no GPU) ---- */
 

@@ -69,15 +69,19 @@ def test_joint_matches_reference_golden(jt, name):
     j.close()
 
 
+@pytest.mark.parametrize("precision", ["auto", "fp32"])
 @pytest.mark.parametrize("nside,dish", [(16, 1.0), (32, 4.0), (64, 8.0)])
-def test_beam_matches_oracle(jt, nside, dish):
+def test_beam_matches_oracle(jt, nside, dish, precision):
+    """the beam with the Legendre sums on the tensor cores (3xTF32, 'auto' at these
+    sizes) and on the FP32 CUDA cores"""
     rng = np.random.default_rng(nside)
     nu0 = np.array([600.0, 800.0, 1000.0])
     nuf = nu0 + 10.0
     maps = (rng.standard_normal((3, 12 * nside * nside)) * 3 + 1).astype(np.float32)
-    j = jt.JoinT(nside, nu0, nuf, dish_diameter=dish)
+    j = jt.JoinT(nside, nu0, nuf, dish_diameter=dish, sht_precision=precision)
     j.add_maps(maps, nside)
     out = j.run()
+    assert j.uses_tensor_cores == (precision == "auto")
     ref = orc.apply_beam(maps, nside, orc.joint_fwhm(nu0, nuf, dish))
     assert rel_l2(out, ref) <= BEAM_L2
     assert np.abs(out - ref).max() <= BEAM_MAX * np.abs(ref).max()
