@@ -50,7 +50,8 @@ struct RingPair {
   long long first_n, first_s;  // first pixel of the north ring and of its south mirror
   int nph;                     // pixels per ring
   int shifted;                 // first pixel at longitude pi / nph (else 0)
-  long long tw_off;            // offset of the ring's twiddles e^{2 pi i t/nph} in the power-of-two table
+  long long tw_off;            // equatorial rings: offset of the twiddles e^{2 pi i t/nph} in the power-of-two
+                               // table; polar rings: offset of the chirps e^{-i pi j^2/nph} in the chirp table
   int bm;                      // polar rings: Bluestein FFT size, the power of two >= 2 nph - 1
   int pad_;
   long long b_off;             // polar rings: offset of the chirp spectrum in the Bluestein table
@@ -59,29 +60,75 @@ struct RingPair {
 // ---------------------------------------------------------------------------
 // merge, ud_grade, noise, mask
 // ---------------------------------------------------------------------------
-// acc += src (first: acc = 0 + src, which turns -0 into +0 exactly as the
-// reference's calloc'ed sum does); scaled: src first becomes (float)(src * factor)
-__device__ __forceinline__ float add_one(float a, float v, double factor, int scaled, int first)
+// out = (((prev or 0) + s_0) + s_1) + ... element by element in FP32, the order in
+// which src/main_jt.c:94 adds the components to its calloc'ed sum; a source with
+// a factor is first scaled as (float)(value * factor) (src/main_jt.c:181)
+constexpr int kMaxSum = 8;
+struct SumSources {
+  const float *p[kMaxSum];
+  double f[kMaxSum];
+  unsigned scaled;  // bit k: source k has a factor
+};
+// NS sources, one float4 (VEC) or one float per thread, the source loop unrolled.
+// The FP64 scaling is compiled in only when some source has a factor (SCALED):
+// FP64 instructions left in the loop, even predicated off, occupy GB300's slow
+// FP64 pipe and cut this kernel from 7.3 to 1.1 TB/s.
+template <int NS, bool VEC, bool SCALED>
+__global__ void sum_kernel(float *__restrict__ out, const float *__restrict__ prev, SumSources s, long long n)
 {
-  if (scaled) v = (float)((double)v * factor);  // src/main_jt.c:181
-  return first ? __fadd_rn(v, 0.f) : __fadd_rn(a, v);  // src/main_jt.c:94
-}
-__global__ void add_kernel(float *__restrict__ acc, const float *__restrict__ src, long long n, double factor,
-                           int scaled, int first)
-{
-  const long long stride = (long long)gridDim.x * blockDim.x, i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  const bool vec = ((reinterpret_cast<uintptr_t>(acc) | reinterpret_cast<uintptr_t>(src)) & 15) == 0;
-  const long long n4 = vec ? n / 4 : 0;
-  for (long long i = i0; i < n4; i += stride) {
-    const float4 v = reinterpret_cast<const float4 *>(src)[i];
-    float4 a = first ? make_float4(0.f, 0.f, 0.f, 0.f) : reinterpret_cast<const float4 *>(acc)[i];
-    a.x = add_one(a.x, v.x, factor, scaled, first);
-    a.y = add_one(a.y, v.y, factor, scaled, first);
-    a.z = add_one(a.z, v.z, factor, scaled, first);
-    a.w = add_one(a.w, v.w, factor, scaled, first);
-    reinterpret_cast<float4 *>(acc)[i] = a;
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (VEC) {
+    if (i >= n / 4) return;
+    float4 a = prev ? reinterpret_cast<const float4 *>(prev)[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+      float4 v = reinterpret_cast<const float4 *>(s.p[k])[i];
+      if (SCALED && (s.scaled & (1u << k))) {
+        v.x = (float)((double)v.x * s.f[k]);
+        v.y = (float)((double)v.y * s.f[k]);
+        v.z = (float)((double)v.z * s.f[k]);
+        v.w = (float)((double)v.w * s.f[k]);
+      }
+      a.x = __fadd_rn(a.x, v.x);
+      a.y = __fadd_rn(a.y, v.y);
+      a.z = __fadd_rn(a.z, v.z);
+      a.w = __fadd_rn(a.w, v.w);
+    }
+    reinterpret_cast<float4 *>(out)[i] = a;
+  } else {
+    if (i >= n) return;
+    float a = prev ? prev[i] : 0.f;
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+      float v = s.p[k][i];
+      if (SCALED && (s.scaled & (1u << k))) v = (float)((double)v * s.f[k]);
+      a = __fadd_rn(a, v);
+    }
+    out[i] = a;
   }
-  for (long long i = 4 * n4 + i0; i < n; i += stride) acc[i] = add_one(first ? 0.f : acc[i], src[i], factor, scaled, first);
+}
+
+template <bool VEC, bool SCALED>
+void launch_sum_t(float *out, const float *prev, const SumSources &s, int ns, long long n, cudaStream_t st)
+{
+  const long long items = VEC ? n / 4 : n;
+  const unsigned blocks = (unsigned)((items + kThreads - 1) / kThreads);
+  switch (ns) {
+    case 1: sum_kernel<1, VEC, SCALED><<<blocks, kThreads, 0, st>>>(out, prev, s, n); break;
+    case 2: sum_kernel<2, VEC, SCALED><<<blocks, kThreads, 0, st>>>(out, prev, s, n); break;
+    case 3: sum_kernel<3, VEC, SCALED><<<blocks, kThreads, 0, st>>>(out, prev, s, n); break;
+    case 4: sum_kernel<4, VEC, SCALED><<<blocks, kThreads, 0, st>>>(out, prev, s, n); break;
+    case 5: sum_kernel<5, VEC, SCALED><<<blocks, kThreads, 0, st>>>(out, prev, s, n); break;
+    case 6: sum_kernel<6, VEC, SCALED><<<blocks, kThreads, 0, st>>>(out, prev, s, n); break;
+    case 7: sum_kernel<7, VEC, SCALED><<<blocks, kThreads, 0, st>>>(out, prev, s, n); break;
+    default: sum_kernel<8, VEC, SCALED><<<blocks, kThreads, 0, st>>>(out, prev, s, n); break;
+  }
+}
+template <bool VEC>
+void launch_sum(float *out, const float *prev, const SumSources &s, int ns, long long n, cudaStream_t st)
+{
+  if (s.scaled) launch_sum_t<VEC, true>(out, prev, s, ns, n, st);
+  else launch_sum_t<VEC, false>(out, prev, s, ns, n, st);
 }
 
 // he_udgrade, nside_in > nside_out: FP64 sum of the NESTED children in order, times 1/ratio
@@ -116,27 +163,43 @@ __global__ void upgrade_kernel(const float *__restrict__ in, long long nside_in,
   }
 }
 
-__global__ void mask_kernel(float *__restrict__ maps, const int *__restrict__ mask, long long npix, int nmaps)
+// blockIdx.y = channel; four pixels per thread (npix = 12 nside^2 is a multiple of 4)
+__global__ void mask_kernel(float *__restrict__ maps, const int *__restrict__ mask, long long npix)
 {
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < npix * nmaps;
-       t += (long long)gridDim.x * blockDim.x)
-    if (mask[t % npix] == 0) maps[t] = 0.f;
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= npix / 4) return;
+  const int4 mk = reinterpret_cast<const int4 *>(mask)[i];
+  if (mk.x && mk.y && mk.z && mk.w) return;
+  float4 *m = reinterpret_cast<float4 *>(maps + (long long)blockIdx.y * npix) + i;
+  float4 v = *m;
+  if (!mk.x) v.x = 0.f;
+  if (!mk.y) v.y = 0.f;
+  if (!mk.z) v.z = 0.f;
+  if (!mk.w) v.w = 0.f;
+  *m = v;
 }
 
-// white noise with Philox4x32-10 draws, key (seed, "JOIN"), counter (pixel, channel):
+// white noise with Philox4x32-10 draws, key (seed, "JOIN"), counter (pixel pair, channel):
+// one call serves pixels 2j (words x, y) and 2j + 1 (z, w);
 // noise = sqrt(-s2 ln(1 - u2)) cos(2 pi u1), the law of src/main_jt.c:304-311
-__global__ void noise_philox_kernel(float *__restrict__ maps, const float *__restrict__ s2, long long npix, int nmaps,
+__device__ __forceinline__ float noise_of(uint32_t w1, uint32_t w2, float s2)
+{
+  const float u1 = (float)(w1 >> 8) * (1.f / 16777216.f), u2 = (float)(w2 >> 8) * (1.f / 16777216.f);
+  return sqrtf(-s2 * log1pf(-u2)) * cospif(2.f * u1);
+}
+__global__ void noise_philox_kernel(float *__restrict__ maps, const float *__restrict__ s2, long long npix,
                                     uint32_t seed)
 {
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < npix * nmaps;
-       t += (long long)gridDim.x * blockDim.x) {
-    const long long c = t / npix, i = t - c * npix;
-    const uint4 r = philox4x32_10(make_uint4((uint32_t)i, (uint32_t)(i >> 32), (uint32_t)c, 0u),
-                                  make_uint2(seed, 0x4A4F494Eu));
-    const float u1 = (float)(r.x >> 8) * (1.f / 16777216.f), u2 = (float)(r.y >> 8) * (1.f / 16777216.f);
-    const float mod = sqrtf(-s2[c] * log1pf(-u2));
-    maps[t] = __fadd_rn(maps[t], mod * cospif(2.f * u1));
-  }
+  const long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;  // pixel pair
+  if (j >= npix / 2) return;
+  const int c = blockIdx.y;
+  const uint4 r = philox4x32_10(make_uint4((uint32_t)j, (uint32_t)(j >> 32), (uint32_t)c, 0u), make_uint2(seed, 0x4A4F494Eu));
+  const float sc = s2[c];
+  float2 *m = reinterpret_cast<float2 *>(maps + (long long)c * npix) + j;
+  float2 v = *m;
+  v.x = __fadd_rn(v.x, noise_of(r.x, r.y, sc));
+  v.y = __fadd_rn(v.y, noise_of(r.z, r.w, sc));
+  *m = v;
 }
 
 // the reference's MT19937 noise (drawn on the host in FP64) added as it adds it:
@@ -436,25 +499,19 @@ __global__ __launch_bounds__(kThreads) void ring_synthesis_fft_kernel(const floa
   }
 }
 
-// e^{-i pi j^2 / n}, the Bluestein chirp, with j^2 reduced exactly modulo 2n
-__device__ __forceinline__ float2 chirp(int j, int n)
-{
-  float sn, cs;
-  sincospif((float)((long long)j * j % (2 * n)) / (float)n, &sn, &cs);
-  return make_float2(cs, -sn);
-}
 
 // Bluestein DFT of the CB sequences a[b][j], j < n (zero beyond, length M):
-// Z_k = c_k (a c) (*) conj(c), the convolution by a DIF FFT, the product with
+// Z_k = c_k (a c) (*) conj(c) with the chirp c_j = e^{-i pi j^2/n} (table ch,
+// FP64-evaluated on the host), the convolution by a DIF FFT, the product with
 // the precomputed spectrum of conj(c) (bit-reversed order, global) and a DIT
 // inverse FFT; on return a[b][k] = Z_k for k < n.
 template <int CB>
-__device__ void bluestein(float2 *a, const float2 *__restrict__ Bt, const float2 *__restrict__ tw2, int n, int M,
-                          int logM)
+__device__ void bluestein(float2 *a, const float2 *__restrict__ Bt, const float2 *__restrict__ tw2,
+                          const float2 *__restrict__ ch, int n, int M, int logM)
 {
   for (int t = threadIdx.x; t < CB * n; t += blockDim.x) {
     const int b = t / n, j = t - b * n;
-    a[b * M + j] = cmul(a[b * M + j], chirp(j, n));
+    a[b * M + j] = cmul(a[b * M + j], __ldg(ch + j));
   }
   __syncthreads();
   fft_dif<CB>(a, tw2, M, logM, -1.f);
@@ -464,7 +521,7 @@ __device__ void bluestein(float2 *a, const float2 *__restrict__ Bt, const float2
   const float inv = 1.f / (float)M;
   for (int t = threadIdx.x; t < CB * n; t += blockDim.x) {
     const int b = t / n, k = t - b * n;
-    const float2 v = cmul(a[b * M + k], chirp(k, n));
+    const float2 v = cmul(a[b * M + k], __ldg(ch + k));
     a[b * M + k] = make_float2(v.x * inv, v.y * inv);
   }
   __syncthreads();
@@ -475,8 +532,8 @@ __device__ void bluestein(float2 *a, const float2 *__restrict__ Bt, const float2
 template <int CB>
 __global__ __launch_bounds__(kThreads) void ring_analysis_bluestein_kernel(
     const float *__restrict__ maps, long long npix, int nch, const RingPair *__restrict__ rings,
-    const float2 *__restrict__ tw2, const float2 *__restrict__ btab, int lmax, int R, int N2, float *__restrict__ E,
-    float *__restrict__ O)
+    const float2 *__restrict__ tw2, const float2 *__restrict__ btab, const float2 *__restrict__ chirps, int lmax, int R,
+    int N2, float *__restrict__ E, float *__restrict__ O)
 {
   extern __shared__ __align__(16) float2 a[];  // [CB][M]
   const int q = blockIdx.x, cb0 = blockIdx.y * CB;
@@ -490,7 +547,7 @@ __global__ __launch_bounds__(kThreads) void ring_analysis_bluestein_kernel(
     a[t] = v;
   }
   __syncthreads();
-  bluestein<CB>(a, btab + rp.b_off, tw2, n, M, logM);
+  bluestein<CB>(a, btab + rp.b_off, tw2, chirps + rp.tw_off, n, M, logM);
   write_eo<CB>(a, M, rp, q, false, lmax, R, N2, nch, cb0, E, O);
 }
 
@@ -499,8 +556,8 @@ __global__ __launch_bounds__(kThreads) void ring_analysis_bluestein_kernel(
 template <int CB>
 __global__ __launch_bounds__(kThreads) void ring_synthesis_bluestein_kernel(
     const float *__restrict__ Gn, const float *__restrict__ Gs, const RingPair *__restrict__ rings,
-    const float2 *__restrict__ tw2, const float2 *__restrict__ btab, int lmax, int R, int N2, int nch,
-    float *__restrict__ maps, long long npix)
+    const float2 *__restrict__ tw2, const float2 *__restrict__ btab, const float2 *__restrict__ chirps, int lmax, int R,
+    int N2, int nch, float *__restrict__ maps, long long npix)
 {
   extern __shared__ __align__(16) float2 a[];  // [CB][M]
   const int q = blockIdx.x, cb0 = blockIdx.y * CB;
@@ -518,7 +575,7 @@ __global__ __launch_bounds__(kThreads) void ring_synthesis_bluestein_kernel(
     for (int b = 0; b < CB; b++) a[b * M + k] = make_float2(h[b].x, -h[b].y);  // conjugated
   }
   __syncthreads();
-  bluestein<CB>(a, btab + rp.b_off, tw2, n, M, logM);
+  bluestein<CB>(a, btab + rp.b_off, tw2, chirps + rp.tw_off, n, M, logM);
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
 #pragma unroll
     for (int b = 0; b < CB; b++) {
@@ -1089,11 +1146,14 @@ struct joint_ctx {
   int *dmask = nullptr;
   float *s2 = nullptr;     // per channel noise variance (Philox path)
   int stage = 0;           // 0 nothing added, 1 adding components, 2 merged (maps valid)
-  bool have_acc = false;   // acc holds the sum of the components added since the last merge
+  bool have_acc = false;   // a component was added since the combination began
+  bool acc_valid = false;  // acc holds the sum of the components before those still pending
+  std::vector<std::pair<const float *, double>> pend;  // device components not summed yet, in order
   // spherical harmonic transform
   RingPair *rings = nullptr;
   float2 *tw2 = nullptr;   // e^{2 pi i t/M} at [M + t] for every power of two M
   float2 *btab = nullptr;  // polar rings: spectra of the conjugate Bluestein chirps (bit-reversed)
+  float2 *chirps = nullptr;  // polar rings: the chirps e^{-i pi j^2/n}, at 2 i (i - 1) for n = 4 i
   float *lam = nullptr;
   int chunk = 0, N2 = 0, bmax = 0;
   float *E = nullptr, *O = nullptr, *alm = nullptr, *sig2 = nullptr, *tmp_maps = nullptr;
@@ -1293,7 +1353,7 @@ int ensure_sht(joint_ctx *c)
       r.first_n = ncap + (i - N) * 4 * N;
     }
     r.first_s = npix - r.nph - r.first_n;
-    r.tw_off = r.nph;  // equatorial rings: tw2[nph + t]
+    r.tw_off = i < N ? 2 * i * (i - 1) : r.nph;  // polar: chirp table offset; equatorial: tw2[nph + t]
     r.bm = i < N ? bluestein_size(r.nph) : 0;
     r.pad_ = 0;
     r.b_off = 0;
@@ -1316,6 +1376,14 @@ int ensure_sht(joint_ctx *c)
       const double a = 2.0 * M_PI * (double)t / (double)M;
       tw2[M + t] = make_float2((float)std::cos(a), (float)std::sin(a));
     }
+  std::vector<float2> chirps(std::max<long long>(2 * N * (N - 1), 1));
+  for (int q = 0; q < N - 1; q++) {
+    const int n = rp[q].nph;
+    for (int j = 0; j < n; j++) {
+      const double a = M_PI * (double)(((long long)j * j) % (2 * n)) / (double)n;
+      chirps[rp[q].tw_off + j] = make_float2((float)std::cos(a), (float)-std::sin(a));
+    }
+  }
   std::vector<float2> btab;
   for (int q = 0; q < N - 1; q++) {
     const int n = rp[q].nph, M = rp[q].bm, logM = __builtin_ctz((unsigned)M);
@@ -1341,6 +1409,7 @@ int ensure_sht(joint_ctx *c)
   int rc;
   const size_t lam_elems = (size_t)m_offset(lmax + 1, lmax) * R;
   if ((rc = jalloc(&c->rings, R)) || (rc = jalloc(&c->tw2, tw2.size())) || (rc = jalloc(&c->btab, btab.size())) ||
+      (rc = jalloc(&c->chirps, chirps.size())) ||
       (rc = jalloc(&c->lam, lam_elems)))
     return rc;
   double *dz = nullptr, *dl = nullptr, *dm = nullptr;
@@ -1353,6 +1422,7 @@ int ensure_sht(joint_ctx *c)
   JCK(cudaMemcpyAsync(c->tw2, tw2.data(), sizeof(float2) * tw2.size(), cudaMemcpyHostToDevice, c->stream));
   if (!btab.empty())
     JCK(cudaMemcpyAsync(c->btab, btab.data(), sizeof(float2) * btab.size(), cudaMemcpyHostToDevice, c->stream));
+  JCK(cudaMemcpyAsync(c->chirps, chirps.data(), sizeof(float2) * chirps.size(), cudaMemcpyHostToDevice, c->stream));
   JCK(cudaMemcpyAsync(dz, z.data(), sizeof(double) * R, cudaMemcpyHostToDevice, c->stream));
   JCK(cudaMemcpyAsync(dl, lsin.data(), sizeof(double) * R, cudaMemcpyHostToDevice, c->stream));
   JCK(cudaMemcpyAsync(dm, lmm0.data(), sizeof(double) * (lmax + 1), cudaMemcpyHostToDevice, c->stream));
@@ -1438,7 +1508,7 @@ void launch_polar_analysis(joint_ctx *c, const float *dmaps, int nch)
   const int N = c->p.nside, nb = (nch + CB - 1) / CB;
   if (N > 1)  // polar ring pairs q < N - 1
     ring_analysis_bluestein_kernel<CB><<<dim3(N - 1, nb), kThreads, bluestein_smem(c->bmax, CB), c->stream>>>(
-        dmaps, c->npix, nch, c->rings, c->tw2, c->btab, c->lmax, c->R, c->N2, c->E, c->O);
+        dmaps, c->npix, nch, c->rings, c->tw2, c->btab, c->chirps, c->lmax, c->R, c->N2, c->E, c->O);
 }
 template <int CB>
 void launch_ring_synthesis(joint_ctx *c, float *dmaps, int nch)
@@ -1453,7 +1523,7 @@ void launch_polar_synthesis(joint_ctx *c, float *dmaps, int nch)
   const int N = c->p.nside, nb = (nch + CB - 1) / CB;
   if (N > 1)
     ring_synthesis_bluestein_kernel<CB><<<dim3(N - 1, nb), kThreads, bluestein_smem(c->bmax, CB), c->stream>>>(
-        c->E, c->O, c->rings, c->tw2, c->btab, c->lmax, c->R, c->N2, nch, dmaps, c->npix);
+        c->E, c->O, c->rings, c->tw2, c->btab, c->chirps, c->lmax, c->R, c->N2, nch, dmaps, c->npix);
 }
 
 // events around one kernel class when profiling (joint_gpu_profile)
@@ -1622,7 +1692,7 @@ extern "C" void joint_gpu_free(joint_ctx *c)
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (void *ptr : {(void *)c->maps, (void *)c->acc, (void *)c->stage_buf, (void *)c->dmask, (void *)c->s2,
-                    (void *)c->rings, (void *)c->tw2, (void *)c->btab, (void *)c->lam, (void *)c->E, (void *)c->O, (void *)c->alm,
+                    (void *)c->rings, (void *)c->tw2, (void *)c->btab, (void *)c->chirps, (void *)c->lam, (void *)c->E, (void *)c->O, (void *)c->alm,
                     (void *)c->sig2, (void *)c->tmp_maps, (void *)c->alm_hp, (void *)c->tasks_a, (void *)c->tasks_s,
                     (void *)c->noise_d, (void *)c->LA, (void *)c->LS, (void *)c->EOp, (void *)c->almp,
                     (void *)c->la_off, (void *)c->ls_off, (void *)c->alm_off, (void *)c->tasks_ta,
@@ -1648,31 +1718,70 @@ extern "C" int joint_gpu_set_stream(joint_ctx *c, void *stream)
 
 extern "C" double joint_gpu_fsky(const joint_ctx *c) { return c ? c->fsky : -1.0; }
 
+// launch sums of `prev` and up to kMaxSum pending components at a time into out
+static int sum_into(joint_ctx *c, float *out, const float *prev, const std::pair<const float *, double> *src, int ns,
+                    long long n)
+{
+  do {
+    SumSources ss;
+    const int k_n = std::min(ns, kMaxSum);
+    uintptr_t al = reinterpret_cast<uintptr_t>(out) | reinterpret_cast<uintptr_t>(prev);
+    ss.scaled = 0;
+    for (int k = 0; k < kMaxSum; k++) {
+      ss.p[k] = k < k_n ? src[k].first : nullptr;
+      ss.f[k] = k < k_n ? src[k].second : 1.0;
+      if (k < k_n) {
+        al |= reinterpret_cast<uintptr_t>(src[k].first);
+        if (src[k].second != 1.0) ss.scaled |= 1u << k;
+      }
+    }
+    if ((al & 15) == 0 && n % 4 == 0) launch_sum<true>(out, prev, ss, k_n, n, c->stream);
+    else launch_sum<false>(out, prev, ss, k_n, n, c->stream);
+    JCK(cudaGetLastError());
+    prev = out;
+    src += k_n;
+    ns -= k_n;
+  } while (ns > 0);
+  return GETHI_OK;
+}
+
+// the components still pending -> acc (in order after what acc already holds)
+static int flush_pending(joint_ctx *c)
+{
+  if (c->pend.empty()) return GETHI_OK;
+  const long long n = 12LL * c->nside_in * c->nside_in * c->p.n_nu;
+  if (n > c->acc_cap) {
+    JCK(cudaStreamSynchronize(c->stream));
+    cudaFree(c->acc);
+    c->acc = nullptr;
+    int rc = jalloc(&c->acc, n);
+    if (rc) return rc;
+    c->acc_cap = n;
+  }
+  int rc = sum_into(c, c->acc, c->acc_valid ? c->acc : nullptr, c->pend.data(), (int)c->pend.size(), n);
+  if (rc) return rc;
+  c->acc_valid = true;
+  c->pend.clear();
+  return GETHI_OK;
+}
+
+// record one component (device memory valid until the merge); a new combination
+// starts with the first component after a merge
 static int add_common(joint_ctx *c, const float *dsrc, long nside_in, double factor)
 {
-  const long long npix_in = 12LL * nside_in * nside_in, n = npix_in * c->p.n_nu;
   if (c->stage == 1 && nside_in != c->nside_in) {
     set_error("read nside is not the same as provided : " + std::to_string(c->nside_in) +
               " != " + std::to_string(nside_in));  // src/main_jt.c:74-81
     return GETHI_E_ARG;
   }
-  if (c->stage != 1) {  // the first component of a new combination
-    if (n > c->acc_cap) {
-      cudaFree(c->acc);
-      c->acc = nullptr;
-      int rc = jalloc(&c->acc, n);
-      if (rc) return rc;
-      c->acc_cap = n;
-    }
+  if (c->stage != 1) {
     c->nside_in = nside_in;
     c->stage = 1;
     c->have_acc = true;
-    add_kernel<<<grid_for(n), kThreads, 0, c->stream>>>(c->acc, dsrc, n, factor, factor != 1.0, 1);
-    JCK(cudaGetLastError());
-    return GETHI_OK;
+    c->acc_valid = false;
+    c->pend.clear();
   }
-  add_kernel<<<grid_for(n), kThreads, 0, c->stream>>>(c->acc, dsrc, n, factor, factor != 1.0, 0);
-  JCK(cudaGetLastError());
+  c->pend.push_back({dsrc, factor});
   return GETHI_OK;
 }
 
@@ -1694,7 +1803,8 @@ extern "C" int joint_gpu_add_maps(joint_ctx *c, const float *maps, long nside_in
   JCK(cudaMemcpyAsync(c->stage_buf, maps, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
   int rc = add_common(c, c->stage_buf, nside_in, factor);
   if (rc) return rc;
-  JCK(cudaStreamSynchronize(c->stream));  // the caller may reuse `maps`
+  if ((rc = flush_pending(c))) return rc;  // the staging buffer is reused by the next host component
+  JCK(cudaStreamSynchronize(c->stream));   // the caller may reuse `maps`
   return GETHI_OK;
 }
 
@@ -1712,7 +1822,14 @@ extern "C" int joint_gpu_merge(joint_ctx *c)
   const long long N = c->p.nside, n = c->npix * c->p.n_nu;
   if (!c->have_acc) {  // no component: the reference leaves the calloc'ed maps at zero
     JCK(cudaMemsetAsync(c->maps, 0, sizeof(float) * n, c->stream));
+  } else if (c->nside_in == N && !c->pend.empty()) {
+    // same resolution: the pending components are summed straight into the maps (the
+    // list is kept, so a repeated run sums them again)
+    int rc = sum_into(c, c->maps, c->acc_valid ? c->acc : nullptr, c->pend.data(), (int)c->pend.size(), n);
+    if (rc) return rc;
   } else {  // (again) from the sum, so a repeated run starts from the merged components
+    int rc = flush_pending(c);
+    if (rc) return rc;
     if (c->nside_in == N)
       JCK(cudaMemcpyAsync(c->maps, c->acc, sizeof(float) * n, cudaMemcpyDeviceToDevice, c->stream));
     else if (c->nside_in > N)
@@ -1774,8 +1891,8 @@ extern "C" int joint_gpu_add_noise(joint_ctx *c)
   }
   const long long npix = c->npix;
   if (c->p.rng == JOINT_RNG_PHILOX) {
-    noise_philox_kernel<<<grid_for(npix * c->p.n_nu), kThreads, 0, c->stream>>>(c->maps, c->s2, npix, c->p.n_nu,
-                                                                                 c->p.seed);
+    noise_philox_kernel<<<dim3((unsigned)((npix / 2 + kThreads - 1) / kThreads), c->p.n_nu), kThreads, 0,
+                          c->stream>>>(c->maps, c->s2, npix, c->p.seed);
     JCK(cudaGetLastError());
     return GETHI_OK;
   }
@@ -1819,7 +1936,8 @@ extern "C" int joint_gpu_apply_mask(joint_ctx *c)
   if (rc) return rc;
   JCK(cudaSetDevice(c->device));
   if (!c->dmask) return GETHI_OK;  // "none"/"default": every pixel kept
-  mask_kernel<<<grid_for(c->npix * c->p.n_nu), kThreads, 0, c->stream>>>(c->maps, c->dmask, c->npix, c->p.n_nu);
+  mask_kernel<<<dim3((unsigned)((c->npix / 4 + kThreads - 1) / kThreads), c->p.n_nu), kThreads, 0, c->stream>>>(
+      c->maps, c->dmask, c->npix);
   JCK(cudaGetLastError());
   return GETHI_OK;
 }

@@ -62,7 +62,11 @@ int joint_gpu_set_stream(joint_ctx *c, void *stream);
  * added in call order in FP32, as the reference adds them. */
 int joint_gpu_add_maps(joint_ctx *c, const float *maps, long nside_in, double factor);
 /* The same from device memory of this context's device, e.g. the maps a GetHI
- * context left there (gethi_gpu_device_maps); no host round trip. */
+ * context left there (gethi_gpu_device_maps); no host round trip.  The sum is
+ * deferred: the memory must stay valid and unchanged until joint_gpu_merge (or
+ * joint_gpu_run) has returned, and, for a repeated run of the same combination,
+ * until then too.  Consecutive device components are summed in one pass (at the
+ * output resolution straight into the maps). */
 int joint_gpu_add_maps_device(joint_ctx *c, const float *dmaps, long nside_in, double factor);
 /* he_udgrade of the sum to the output nside (src/healpix_extra.c:318-388,
  * RING in and out, degrading by the FP64 mean of the NESTED children). */
