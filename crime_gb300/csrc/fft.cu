@@ -30,6 +30,7 @@
 
 #include "common.cuh"
 #include "fft.h"
+#include "dfloat.cuh"
 #include "modes.cuh"
 
 namespace gethi {
@@ -245,9 +246,9 @@ __global__ void __launch_bounds__(RW *(M / P), EPI == 2 ? 512 / (RW * (M / P)) :
   } else {
     float2 *grow = in.main[0] + row * (long)M;
     row_c2r<M, P, RW, Rad>(v, srow, grow, active ? in.nyq[0][row] : make_float2(0.f, 0.f), active, t, twN, twM);
-    double s1 = 0, s2 = 0;
+    df s1 = df_f(0.f), s2 = df_f(0.f);
     if (active) {
-      // per-thread sums in FP32 with Neumaier compensation, carried to FP64
+      // per-thread sums in FP32 with Neumaier compensation, carried as double-float pairs
       float a1 = 0.f, c1 = 0.f, a2 = 0.f, c2 = 0.f;
       auto nsum = [](float &acc, float &comp, float val) {
         float s = acc + val;
@@ -268,27 +269,33 @@ __global__ void __launch_bounds__(RW *(M / P), EPI == 2 ? 512 / (RW * (M / P)) :
             nsum(a2, c2, x.y * x.y);
           }
         }
-      s1 = (double)a1 + (double)c1;
-      s2 = (double)a2 + (double)c2;
+      s1 = two_sum(a1, c1);
+      s2 = two_sum(a2, c2);
     }
     if constexpr (EPI == 0) {
-      __shared__ double red[2][32];
+      // warp reduction in double-float (FP32 TwoSum, ~48 bits); FP64 only for the block's
+      // final sum (on GB300 a per-thread FP64 reduction cost the pass ~1.5 ms at 1024^3)
+      __shared__ float red[4][32];
       for (int o = 16; o > 0; o >>= 1) {
-        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
-        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        const df t1 = {__shfl_xor_sync(0xffffffffu, s1.hi, o), __shfl_xor_sync(0xffffffffu, s1.lo, o)};
+        const df t2 = {__shfl_xor_sync(0xffffffffu, s2.hi, o), __shfl_xor_sync(0xffffffffu, s2.lo, o)};
+        s1 = df_add(s1, t1);
+        s2 = df_add(s2, t2);
       }
       const int w = tid >> 5, lane = tid & 31, nw = (RW * T + 31) >> 5;
       __syncthreads();
       if (lane == 0) {
-        red[0][w] = s1;
-        red[1][w] = s2;
+        red[0][w] = s1.hi;
+        red[1][w] = s1.lo;
+        red[2][w] = s2.hi;
+        red[3][w] = s2.lo;
       }
       __syncthreads();
       if (tid == 0) {
         double a = 0, b = 0;
         for (int i = 0; i < nw; i++) {
-          a += red[0][i];
-          b += red[1][i];
+          a += (double)red[0][i] + (double)red[1][i];
+          b += (double)red[2][i] + (double)red[3][i];
         }
         partials[blockIdx.x] = make_double2(a, b);
       }

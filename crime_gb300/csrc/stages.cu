@@ -607,11 +607,26 @@ __global__ void fixup_kernel(DevCfg c, const FallbackEntry *__restrict__ fq, con
 }
 
 // maps *= M2T / (r(nu_c)^2 dnu) per channel, src/pixelize.c:399-414
+// blockIdx.y = channel; VEC: four pixels per thread (npix = 12 nside^2 is a multiple
+// of 4; maps 16-byte aligned), else one
+template <bool VEC>
 __global__ void scale_maps_kernel(DevCfg c, float *maps)
 {
-  const long total = c.npix * (long)c.n_nu;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x)
-    maps[i] *= __ldg(&c.prefac[i / c.npix]);
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const float f = __ldg(&c.prefac[blockIdx.y]);
+  float *mc = maps + (long)blockIdx.y * c.npix;
+  if (VEC) {
+    if (i >= c.npix / 4) return;
+    float4 *m = reinterpret_cast<float4 *>(mc) + i;
+    float4 v = *m;
+    v.x *= f;
+    v.y *= f;
+    v.z *= f;
+    v.w *= f;
+    *m = v;
+  } else if (i < c.npix) {
+    mc[i] *= f;
+  }
 }
 
 // per-sample keys (validation): exact FP64, or fast FP32 with FP64 fallback
@@ -753,7 +768,10 @@ cudaError_t fixup(const DevCfg &c, const void *fq, const int *counters, long fq_
 
 cudaError_t scale_maps(const DevCfg &c, float *maps, cudaStream_t st)
 {
-  scale_maps_kernel<<<grid_for(c.npix * (long)c.n_nu, 256), 256, 0, st>>>(c, maps);
+  if ((reinterpret_cast<uintptr_t>(maps) & 15) == 0)
+    scale_maps_kernel<true><<<dim3((unsigned)((c.npix / 4 + 255) / 256), c.n_nu), 256, 0, st>>>(c, maps);
+  else
+    scale_maps_kernel<false><<<dim3((unsigned)((c.npix + 255) / 256), c.n_nu), 256, 0, st>>>(c, maps);
   return cudaGetLastError();
 }
 
