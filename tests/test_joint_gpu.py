@@ -204,3 +204,50 @@ def test_cli_matches_reference_golden(jt, tmp_path):
         assert int(h["NSIDE"]) == int(g["cfg_nside"]) and h["ORDERING"] == "RING"
         np.testing.assert_array_equal(d, g["maps"][i])
     np.testing.assert_array_equal(np.loadtxt(tmp_path / "out_instrument.dat", ndmin=2), g["instrument"])
+
+
+def _bandlimited(jt, j, nside, lmax_in, seed):
+    """a map synthesised from random a_lm with l <= lmax_in (HEALPix order) and those a_lm"""
+    lmax = 3 * nside - 1
+    rng = np.random.default_rng(seed)
+    alm = np.zeros(orc.nalms(lmax), np.complex64)
+    for m in range(lmax_in + 1):
+        i0 = m * (2 * lmax + 1 - m) // 2 + m  # index of (l = m, m): l + m lmax - m(m-1)/2
+        cnt = lmax_in - m + 1
+        alm[i0:i0 + cnt] = rng.standard_normal(cnt) + (1j * rng.standard_normal(cnt) if m else 0)
+    return j.alm2map(alm)[0], alm
+
+
+@pytest.mark.parametrize("nside", [512, 1024])
+def test_beam_of_bandlimited_map_large_nside(jt, nside):
+    """At Nside 512 (tensor cores) and 1024 (FP32 CUDA cores: 2-channel equatorial
+    FFT blocks, 1-channel Bluestein at M = 8192): the beam of a band-limited map
+    (l <= 48) equals the synthesis of b_l a_lm, to the HEALPix quadrature error."""
+    lmax = 3 * nside - 1
+    nu = np.array([800.0])
+    j = jt.JoinT(nside, nu, nu + 10.0, dish_diameter=15.0)
+    m, alm = _bandlimited(jt, j, nside, 48, nside)
+    j.add_maps(m[None, :], nside)
+    out = j.run()[0]
+    assert j.uses_tensor_cores == (nside <= 512)
+    b = orc.beam_window(lmax, orc.joint_fwhm([800.0], [810.0], 15.0)[0])
+    l_of = np.concatenate([np.arange(mm, lmax + 1) for mm in range(lmax + 1)])
+    ref = j.alm2map((alm * b[l_of]).astype(np.complex64))[0]
+    assert rel_l2(out, ref) < 1e-4
+    assert rel_l2(out, m) > 1e-3  # the beam changed the map
+
+
+def test_tensor_and_fp32_legendre_agree_at_nside_512(jt):
+    """the two Legendre paths on white-noise maps at Nside 512 (1024-term ring-pair
+    sums, 2048-point ring FFTs): both FP32-accumulated, each within ~2-3e-6 of the
+    exact beam, so they agree to 1e-5"""
+    rng = np.random.default_rng(5)
+    nu0 = np.array([700.0, 900.0])
+    maps = rng.standard_normal((2, 12 * 512 * 512)).astype(np.float32)
+    outs = []
+    for prec in ("auto", "fp32"):
+        j = jt.JoinT(512, nu0, nu0 + 5.0, dish_diameter=20.0, sht_precision=prec)
+        j.add_maps(maps, 512)
+        outs.append(j.run())
+        j.close()
+    assert rel_l2(outs[0], outs[1]) < 1e-5
