@@ -347,21 +347,69 @@ __device__ __forceinline__ void fft_stage(float2 *z, const float2 *__restrict__ 
   }
 }
 
-// radix-2 FFT, bit-reversed order in, natural order out (sign -1: e^{-2 pi i jk/n})
+// Two radix-2 stages fused into radix-4 groups (h = 2^st): DIT does stages st and
+// st + 1, DIF stages st + 1 and st, on the four elements base + {0, h, 2h, 3h} in
+// registers (one shared-memory pass and one barrier instead of two).  Twiddles:
+// w = e^{sign 2 pi i jj/(2h)}, w2 = e^{sign 2 pi i jj/(4h)}, w3 = w2 e^{sign i pi/2}.
+template <int CB, bool DIT>
+__device__ __forceinline__ void fft_stage4(float2 *z, const float2 *__restrict__ tw2, int n, int logn, int st,
+                                           float sign)
+{
+  const int h = 1 << st, total = CB * (n >> 2);
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    const int b = t >> (logn - 2), u = t & ((n >> 2) - 1), jj = u & (h - 1);
+    float2 *zb = z + b * n + ((u >> st) << (st + 2)) + jj;
+    const float2 x0 = zb[0], x1 = zb[h], x2 = zb[2 * h], x3 = zb[3 * h];
+    float2 w = __ldg(tw2 + 2 * h + jj), w2 = __ldg(tw2 + 4 * h + jj);
+    w.y *= sign;
+    w2.y *= sign;
+    const float2 w3 = make_float2(-sign * w2.y, sign * w2.x);
+    if (DIT) {
+      const float2 v1 = cmul(x1, w), v3 = cmul(x3, w);
+      const float2 a0 = make_float2(x0.x + v1.x, x0.y + v1.y), a1 = make_float2(x0.x - v1.x, x0.y - v1.y);
+      const float2 a2 = make_float2(x2.x + v3.x, x2.y + v3.y), a3 = make_float2(x2.x - v3.x, x2.y - v3.y);
+      const float2 u2 = cmul(a2, w2), u3 = cmul(a3, w3);
+      zb[0] = make_float2(a0.x + u2.x, a0.y + u2.y);
+      zb[2 * h] = make_float2(a0.x - u2.x, a0.y - u2.y);
+      zb[h] = make_float2(a1.x + u3.x, a1.y + u3.y);
+      zb[3 * h] = make_float2(a1.x - u3.x, a1.y - u3.y);
+    } else {
+      const float2 a0 = make_float2(x0.x + x2.x, x0.y + x2.y), a1 = make_float2(x1.x + x3.x, x1.y + x3.y);
+      const float2 a2 = cmul(make_float2(x0.x - x2.x, x0.y - x2.y), w2);
+      const float2 a3 = cmul(make_float2(x1.x - x3.x, x1.y - x3.y), w3);
+      zb[0] = make_float2(a0.x + a1.x, a0.y + a1.y);
+      zb[h] = cmul(make_float2(a0.x - a1.x, a0.y - a1.y), w);
+      zb[2 * h] = make_float2(a2.x + a3.x, a2.y + a3.y);
+      zb[3 * h] = cmul(make_float2(a2.x - a3.x, a2.y - a3.y), w);
+    }
+  }
+}
+
+// radix-2/4 FFT, bit-reversed order in, natural order out (sign -1: e^{-2 pi i jk/n})
 template <int CB>
 __device__ void fft_dit(float2 *z, const float2 *__restrict__ tw2, int n, int logn, float sign)
 {
-  for (int st = 0; st < logn; st++) {
-    fft_stage<CB, true>(z, tw2, n, logn, st, sign);
+  int st = 0;
+  if (logn & 1) {
+    fft_stage<CB, true>(z, tw2, n, logn, 0, sign);
+    __syncthreads();
+    st = 1;
+  }
+  for (; st < logn; st += 2) {
+    fft_stage4<CB, true>(z, tw2, n, logn, st, sign);
     __syncthreads();
   }
 }
-// radix-2 FFT, natural order in, bit-reversed order out
+// radix-2/4 FFT, natural order in, bit-reversed order out
 template <int CB>
 __device__ void fft_dif(float2 *z, const float2 *__restrict__ tw2, int n, int logn, float sign)
 {
-  for (int st = logn - 1; st >= 0; st--) {
-    fft_stage<CB, false>(z, tw2, n, logn, st, sign);
+  for (int st = logn - 2; st >= (logn & 1); st -= 2) {
+    fft_stage4<CB, false>(z, tw2, n, logn, st, sign);
+    __syncthreads();
+  }
+  if (logn & 1) {
+    fft_stage<CB, false>(z, tw2, n, logn, 0, sign);
     __syncthreads();
   }
 }
