@@ -497,7 +497,9 @@ def bench_joint(args):
         "roofline": roof,
         "e2e": {"value": whole_job_rate(units, args.steps, ws, e2e_ms), "unit": "pixels/s",
                 "h2d_bytes_per_step": int(4 * units * len(comp)), "d2h_bytes_per_step": int(4 * units)},
-        "gpu_launches": args.steps * (len(comp) + (7 if j.uses_tensor_cores else 6) * chunks + 2),
+        # per step: one sum of the device components, per batch the ring (FFT + Bluestein) and Legendre
+        # kernels (+ the E/O pack on the tensor-core path), noise, mask
+        "gpu_launches": args.steps * (1 + (7 if j.uses_tensor_cores else 6) * chunks + 2),
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:
