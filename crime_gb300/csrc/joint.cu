@@ -45,6 +45,7 @@ constexpr double kPrefacFwhm = 1030610.55;               // src/main_jt.c:26
 constexpr double kPrefacTnu = 3.6e9;                     // src/main_jt.c:25
 constexpr double kFwhm2Sigma = 0.00012352884853326381;  // src/healpix_extra.c:388
 constexpr int kThreads = 256;
+constexpr int kRingThreads = 512;  // ring transforms: latency-bound stages; 512 beat 256 and 1024
 
 struct RingPair {
   long long first_n, first_s;  // first pixel of the north ring and of its south mirror
@@ -482,7 +483,7 @@ __device__ __forceinline__ void packed_spectrum(const float *__restrict__ Gn, co
 // of two) by one complex FFT per channel of z_j = north_j + i south_j, gathered in
 // bit-reversed order from global memory (shared-memory writes stay contiguous).
 template <int CB>
-__global__ __launch_bounds__(kThreads) void ring_analysis_fft_kernel(const float *__restrict__ maps, long long npix,
+__global__ __launch_bounds__(kRingThreads) void ring_analysis_fft_kernel(const float *__restrict__ maps, long long npix,
                                                                      int nch, const RingPair *__restrict__ rings,
                                                                      const float2 *__restrict__ tw2, int lmax, int R,
                                                                      int N2, int q0, float *__restrict__ E,
@@ -515,7 +516,7 @@ __global__ __launch_bounds__(kThreads) void ring_analysis_fft_kernel(const float
 // bit-reversed order, through one complex inverse FFT whose real and imaginary
 // parts are the north and south rings' pixels.
 template <int CB>
-__global__ __launch_bounds__(kThreads) void ring_synthesis_fft_kernel(const float *__restrict__ Gn,
+__global__ __launch_bounds__(kRingThreads) void ring_synthesis_fft_kernel(const float *__restrict__ Gn,
                                                                       const float *__restrict__ Gs,
                                                                       const RingPair *__restrict__ rings,
                                                                       const float2 *__restrict__ tw2, int lmax,
@@ -578,7 +579,7 @@ __device__ void bluestein(float2 *a, const float2 *__restrict__ Bt, const float2
 // Ring analysis of the polar ring pairs (q < nside - 1, n = 4 (q + 1) pixels)
 // by a Bluestein DFT of z_j = north_j + i south_j.
 template <int CB>
-__global__ __launch_bounds__(kThreads) void ring_analysis_bluestein_kernel(
+__global__ __launch_bounds__(kRingThreads) void ring_analysis_bluestein_kernel(
     const float *__restrict__ maps, long long npix, int nch, const RingPair *__restrict__ rings,
     const float2 *__restrict__ tw2, const float2 *__restrict__ btab, const float2 *__restrict__ chirps, int lmax, int R,
     int N2, float *__restrict__ E, float *__restrict__ O)
@@ -602,7 +603,7 @@ __global__ __launch_bounds__(kThreads) void ring_analysis_bluestein_kernel(
 // Ring synthesis of the polar ring pairs: the packed spectra inverse-transformed
 // as conj(DFT(conj(.))) with the Bluestein DFT.
 template <int CB>
-__global__ __launch_bounds__(kThreads) void ring_synthesis_bluestein_kernel(
+__global__ __launch_bounds__(kRingThreads) void ring_synthesis_bluestein_kernel(
     const float *__restrict__ Gn, const float *__restrict__ Gs, const RingPair *__restrict__ rings,
     const float2 *__restrict__ tw2, const float2 *__restrict__ btab, const float2 *__restrict__ chirps, int lmax, int R,
     int N2, int nch, float *__restrict__ maps, long long npix)
@@ -1547,7 +1548,7 @@ template <int CB>
 void launch_ring_analysis(joint_ctx *c, const float *dmaps, int nch)
 {
   const int N = c->p.nside, nb = (nch + CB - 1) / CB;
-  ring_analysis_fft_kernel<CB><<<dim3(N + 1, nb), kThreads, analysis_fft_smem(4 * N, CB), c->stream>>>(
+  ring_analysis_fft_kernel<CB><<<dim3(N + 1, nb), kRingThreads, analysis_fft_smem(4 * N, CB), c->stream>>>(
       dmaps, c->npix, nch, c->rings, c->tw2, c->lmax, c->R, c->N2, N - 1, c->E, c->O);
 }
 template <int CB>
@@ -1555,14 +1556,14 @@ void launch_polar_analysis(joint_ctx *c, const float *dmaps, int nch)
 {
   const int N = c->p.nside, nb = (nch + CB - 1) / CB;
   if (N > 1)  // polar ring pairs q < N - 1
-    ring_analysis_bluestein_kernel<CB><<<dim3(N - 1, nb), kThreads, bluestein_smem(c->bmax, CB), c->stream>>>(
+    ring_analysis_bluestein_kernel<CB><<<dim3(N - 1, nb), kRingThreads, bluestein_smem(c->bmax, CB), c->stream>>>(
         dmaps, c->npix, nch, c->rings, c->tw2, c->btab, c->chirps, c->lmax, c->R, c->N2, c->E, c->O);
 }
 template <int CB>
 void launch_ring_synthesis(joint_ctx *c, float *dmaps, int nch)
 {
   const int N = c->p.nside, nb = (nch + CB - 1) / CB;
-  ring_synthesis_fft_kernel<CB><<<dim3(N + 1, nb), kThreads, synthesis_fft_smem(4 * N, CB), c->stream>>>(
+  ring_synthesis_fft_kernel<CB><<<dim3(N + 1, nb), kRingThreads, synthesis_fft_smem(4 * N, CB), c->stream>>>(
       c->E, c->O, c->rings, c->tw2, c->lmax, c->R, c->N2, nch, N - 1, dmaps, c->npix);
 }
 template <int CB>
@@ -1570,7 +1571,7 @@ void launch_polar_synthesis(joint_ctx *c, float *dmaps, int nch)
 {
   const int N = c->p.nside, nb = (nch + CB - 1) / CB;
   if (N > 1)
-    ring_synthesis_bluestein_kernel<CB><<<dim3(N - 1, nb), kThreads, bluestein_smem(c->bmax, CB), c->stream>>>(
+    ring_synthesis_bluestein_kernel<CB><<<dim3(N - 1, nb), kRingThreads, bluestein_smem(c->bmax, CB), c->stream>>>(
         c->E, c->O, c->rings, c->tw2, c->btab, c->chirps, c->lmax, c->R, c->N2, nch, dmaps, c->npix);
 }
 
