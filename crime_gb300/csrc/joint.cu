@@ -16,14 +16,15 @@
 //           batch; the same buffers then hold the synthesised north and south
 //           ring sums
 //   alm     per m, [parity][l'][2 c] float
-// A transform is, per batch of channels: ring DFTs (one CTA per ring pair: the
-// 2 nside + 1 equatorial rings, 4 nside pixels each, by a shared-memory radix-2
-// FFT of north + i south; the polar rings, 4 i pixels, by direct sums with
-// shared-memory twiddles), the
+// A transform is, per batch of channels: ring DFTs (one CTA per ring pair and a
+// few channels: the 2 nside + 1 equatorial rings, 4 nside pixels each, by a
+// register-resident radix-16 Stockham FFT of north + i south; the polar rings,
+// 4 i pixels, by Bluestein's DFT over the same FFTs), the
 // Legendre sums as FP32 GEMMs per (m, parity) on the CUDA cores (the beam
 // factor exp(-l(l+1) sigma_c^2 / 2) and the quadrature weight 4 pi / npix
 // applied in the epilogue), the transposed GEMMs back, and the inverse ring
 // sums.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -35,9 +36,11 @@
 #include "common.cuh"
 #include "healpix.h"
 #include "host.h"
+#include "stockham.cuh"
 #include "tc.cuh"
 
 using namespace gethi;
+using namespace stockham;
 
 namespace {
 
@@ -45,7 +48,9 @@ constexpr double kPrefacFwhm = 1030610.55;               // src/main_jt.c:26
 constexpr double kPrefacTnu = 3.6e9;                     // src/main_jt.c:25
 constexpr double kFwhm2Sigma = 0.00012352884853326381;  // src/healpix_extra.c:388
 constexpr int kThreads = 256;
-constexpr int kRingThreads = 512;  // ring transforms: latency-bound stages; 512 beat 256 and 1024
+constexpr int kRingThreads = 512;  // ring transforms: threads per block (16 points each)
+// shared-memory row pitch (float2) of one ring sequence of n points: padded, odd
+__host__ __device__ constexpr int ring_pitch(int n) { return stockham::padded_len(n) | 1; }
 
 struct RingPair {
   long long first_n, first_s;  // first pixel of the north ring and of its south mirror
@@ -264,376 +269,287 @@ __global__ void lambda_kernel(const double *__restrict__ ring_z, const double *_
   }
 }
 
-// Q_k of ring s (0 north, 1 south) of pair q for CB channels (see fold_ring_sums)
-template <int CB>
-__device__ __forceinline__ void fold_one(const float *__restrict__ G, const RingPair &rp, int q, int k, int lmax, int R,
-                                         int N2, int nch, int cb0, float2 *acc)
+// ---- ring transforms --------------------------------------------------------
+// One launch per direction covers every ring pair of a channel batch through a
+// task list: task (q, c0, S) is ring pair q with the channels c0 .. c0 + S - 1,
+// S = threads / max(1, M/16) sequences of M points (M = the ring length for the
+// equatorial rings, the Bluestein size for the polar rings; a power of two, held
+// as log2 in the task's w), so that every ring size fills the block.  Tasks are ordered by decreasing work.  The sequences'
+// shared-memory rows have an odd pitch (in float2), so that threads of
+// consecutive channels at the same frequency fall in different banks.
+
+struct SeqLayout {
+  int n, L, TS, PL, b, t;
+  bool active;
+};
+__device__ __forceinline__ SeqLayout seq_layout(int n, int S)
 {
-  const int n = rp.nph, half = n / 2;
-#pragma unroll
-  for (int b = 0; b < CB; b++) acc[b] = make_float2(0.f, 0.f);
-  for (int pass = 0; pass < 2; pass++) {
-    if (pass == 1 && (k == 0 || k == half)) break;
-    const float sg = pass ? -1.f : 1.f;
-    for (int m = pass ? n - k : k; m <= lmax; m += n) {
-      float2 ph = make_float2(1.f, 0.f);
-      if (rp.shifted) {
-        float sn, cs;
-        sincospif((float)(m % (2 * n)) / (float)n, &sn, &cs);
-        ph = make_float2(cs, sn);
-      }
-      const float cm = m ? 2.f : 1.f;
-#pragma unroll
-      for (int b = 0; b < CB; b++) {
-        if (cb0 + b >= nch) continue;
-        const float2 g = *reinterpret_cast<const float2 *>(G + ((long long)m * R + q) * N2 + 2 * (cb0 + b));
-        acc[b].x += cm * (g.x * ph.x - g.y * ph.y);
-        acc[b].y += sg * cm * (g.x * ph.y + g.y * ph.x);
-      }
+  SeqLayout sl;
+  sl.n = n;
+  sl.L = __ffs(n) - 1;
+  sl.TS = n >= 16 ? n >> 4 : 1;
+  sl.PL = ring_pitch(n);
+  sl.b = threadIdx.x / sl.TS;
+  sl.t = threadIdx.x - sl.b * sl.TS;
+  sl.active = sl.b < S;
+  return sl;
+}
+
+// Folded sums Q_k (0 <= k <= n/2) of the north (Gn) and south (Gs) ring of pair q,
+// channel c: the alias sum over m = +-k (mod n), m <= lmax, of c_m G_m e^{i m phi0},
+// with c_m = 2 for m > 0 (real map) and the negative frequencies as conjugates.
+// For a ring whose first pixel sits at phi0 = pi/n, e^{i m pi/n} =
+// e^{i pi k/n} (-1)^j for m = k + j n, so the alternating sums are taken first
+// and the phase ph = e^{i pi k/n} applied once.  Both rings share the m loop.
+__device__ __forceinline__ void fold_pair(const float *__restrict__ Gn, const float *__restrict__ Gs,
+                                          long long mstride, int k, int n, int lmax, bool shifted, float2 ph,
+                                          float2 &qn, float2 &qs)
+{
+  const float flip = shifted ? -1.f : 1.f;
+  float4 A = make_float4(0.f, 0.f, 0.f, 0.f), B = A;  // (north, south) of +k and of -k
+  float sg = k ? 2.f : 1.f;                            // c_0 = 1
+  for (int m = k; m <= lmax; m += n) {
+    const float2 gn = *reinterpret_cast<const float2 *>(Gn + m * mstride);
+    const float2 gs = *reinterpret_cast<const float2 *>(Gs + m * mstride);
+    A.x += sg * gn.x;
+    A.y += sg * gn.y;
+    A.z += sg * gs.x;
+    A.w += sg * gs.y;
+    sg = (m ? sg : 2.f) * flip;
+  }
+  if (k != 0 && 2 * k != n) {
+    sg = 2.f;
+    for (int m = n - k; m <= lmax; m += n) {
+      const float2 gn = *reinterpret_cast<const float2 *>(Gn + m * mstride);
+      const float2 gs = *reinterpret_cast<const float2 *>(Gs + m * mstride);
+      B.x += sg * gn.x;
+      B.y += sg * gn.y;
+      B.z += sg * gs.x;
+      B.w += sg * gs.y;
+      sg *= flip;
     }
+  }
+  if (shifted) {  // ph (A - conj B)
+    qn = cmul(ph, make_float2(A.x - B.x, A.y + B.y));
+    qs = cmul(ph, make_float2(A.z - B.z, A.w + B.w));
+  } else {        // A + conj B
+    qn = make_float2(A.x + B.x, A.y - B.y);
+    qs = make_float2(A.z + B.z, A.w - B.w);
   }
 }
 
-__device__ __forceinline__ float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
-__device__ __forceinline__ int bit_reverse(int v, int bits) { return (int)(__brev((unsigned)v) >> (32 - bits)); }
-
-// One radix-2 stage (butterflies i0, i0 + h) over CB sequences of length n = 2^logn
-// stored one after the other in z, decimation in time (DIT) or in frequency.  The
-// twiddle e^{sign 2 pi i jj/(2h)} comes from the power-of-two table, tw2[2h + jj]
-// (contiguous in jj, read-only path); four butterflies per thread are in flight.
-template <int CB, bool DIT>
-__device__ __forceinline__ void fft_stage(float2 *z, const float2 *__restrict__ tw2, int n, int logn, int st,
-                                          float sign)
-{
-  const int h = 1 << st, total = CB * (n >> 1), nt = blockDim.x;
-  const float2 *twp = tw2 + 2 * h;
-  int t = threadIdx.x;
-  for (; t + 3 * nt < total; t += 4 * nt) {
-    int i0[4];
-    float2 a[4], c[4], w[4];
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-      const int tt = t + r * nt, b = tt >> (logn - 1), u = tt & ((n >> 1) - 1), jj = u & (h - 1);
-      i0[r] = b * n + ((u >> st) << (st + 1)) + jj;
-      w[r] = __ldg(twp + jj);
-      a[r] = z[i0[r]];
-      c[r] = z[i0[r] + h];
-    }
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-      const float2 ww = make_float2(w[r].x, sign * w[r].y);
-      if (DIT) {
-        const float2 v = cmul(c[r], ww);
-        z[i0[r]] = make_float2(a[r].x + v.x, a[r].y + v.y);
-        z[i0[r] + h] = make_float2(a[r].x - v.x, a[r].y - v.y);
-      } else {
-        z[i0[r]] = make_float2(a[r].x + c[r].x, a[r].y + c[r].y);
-        z[i0[r] + h] = cmul(make_float2(a[r].x - c[r].x, a[r].y - c[r].y), ww);
-      }
-    }
-  }
-  for (; t < total; t += nt) {
-    const int b = t >> (logn - 1), u = t & ((n >> 1) - 1), jj = u & (h - 1);
-    const int i0 = b * n + ((u >> st) << (st + 1)) + jj;
-    const float2 w = __ldg(twp + jj), ww = make_float2(w.x, sign * w.y);
-    const float2 a = z[i0], c = z[i0 + h];
-    if (DIT) {
-      const float2 v = cmul(c, ww);
-      z[i0] = make_float2(a.x + v.x, a.y + v.y);
-      z[i0 + h] = make_float2(a.x - v.x, a.y - v.y);
-    } else {
-      z[i0] = make_float2(a.x + c.x, a.y + c.y);
-      z[i0 + h] = cmul(make_float2(a.x - c.x, a.y - c.y), ww);
-    }
-  }
-}
-
-// Two radix-2 stages fused into radix-4 groups (h = 2^st): DIT does stages st and
-// st + 1, DIF stages st + 1 and st, on the four elements base + {0, h, 2h, 3h} in
-// registers (one shared-memory pass and one barrier instead of two).  Twiddles:
-// w = e^{sign 2 pi i jj/(2h)}, w2 = e^{sign 2 pi i jj/(4h)}, w3 = w2 e^{sign i pi/2}.
-template <int CB, bool DIT>
-__device__ __forceinline__ void fft_stage4(float2 *z, const float2 *__restrict__ tw2, int n, int logn, int st,
-                                           float sign)
-{
-  const int h = 1 << st, total = CB * (n >> 2);
-  for (int t = threadIdx.x; t < total; t += blockDim.x) {
-    const int b = t >> (logn - 2), u = t & ((n >> 2) - 1), jj = u & (h - 1);
-    float2 *zb = z + b * n + ((u >> st) << (st + 2)) + jj;
-    const float2 x0 = zb[0], x1 = zb[h], x2 = zb[2 * h], x3 = zb[3 * h];
-    float2 w = __ldg(tw2 + 2 * h + jj), w2 = __ldg(tw2 + 4 * h + jj);
-    w.y *= sign;
-    w2.y *= sign;
-    const float2 w3 = make_float2(-sign * w2.y, sign * w2.x);
-    if (DIT) {
-      const float2 v1 = cmul(x1, w), v3 = cmul(x3, w);
-      const float2 a0 = make_float2(x0.x + v1.x, x0.y + v1.y), a1 = make_float2(x0.x - v1.x, x0.y - v1.y);
-      const float2 a2 = make_float2(x2.x + v3.x, x2.y + v3.y), a3 = make_float2(x2.x - v3.x, x2.y - v3.y);
-      const float2 u2 = cmul(a2, w2), u3 = cmul(a3, w3);
-      zb[0] = make_float2(a0.x + u2.x, a0.y + u2.y);
-      zb[2 * h] = make_float2(a0.x - u2.x, a0.y - u2.y);
-      zb[h] = make_float2(a1.x + u3.x, a1.y + u3.y);
-      zb[3 * h] = make_float2(a1.x - u3.x, a1.y - u3.y);
-    } else {
-      const float2 a0 = make_float2(x0.x + x2.x, x0.y + x2.y), a1 = make_float2(x1.x + x3.x, x1.y + x3.y);
-      const float2 a2 = cmul(make_float2(x0.x - x2.x, x0.y - x2.y), w2);
-      const float2 a3 = cmul(make_float2(x1.x - x3.x, x1.y - x3.y), w3);
-      zb[0] = make_float2(a0.x + a1.x, a0.y + a1.y);
-      zb[h] = cmul(make_float2(a0.x - a1.x, a0.y - a1.y), w);
-      zb[2 * h] = make_float2(a2.x + a3.x, a2.y + a3.y);
-      zb[3 * h] = cmul(make_float2(a2.x - a3.x, a2.y - a3.y), w);
-    }
-  }
-}
-
-// radix-2/4 FFT, bit-reversed order in, natural order out (sign -1: e^{-2 pi i jk/n})
-template <int CB>
-__device__ void fft_dit(float2 *z, const float2 *__restrict__ tw2, int n, int logn, float sign)
-{
-  int st = 0;
-  if (logn & 1) {
-    fft_stage<CB, true>(z, tw2, n, logn, 0, sign);
-    __syncthreads();
-    st = 1;
-  }
-  for (; st < logn; st += 2) {
-    fft_stage4<CB, true>(z, tw2, n, logn, st, sign);
-    __syncthreads();
-  }
-}
-// radix-2/4 FFT, natural order in, bit-reversed order out
-template <int CB>
-__device__ void fft_dif(float2 *z, const float2 *__restrict__ tw2, int n, int logn, float sign)
-{
-  for (int st = logn - 2; st >= (logn & 1); st -= 2) {
-    fft_stage4<CB, false>(z, tw2, n, logn, st, sign);
-    __syncthreads();
-  }
-  if (logn & 1) {
-    fft_stage<CB, false>(z, tw2, n, logn, 0, sign);
-    __syncthreads();
-  }
-}
-
-// E and O of pair q for m = 0 .. lmax from the DFT Z of z_j = north_j + i south_j
-// (held in a[b * stride + k], k < n): D_north,k = (Z_k + conj Z_{n-k}) / 2,
-// D_south,k = (Z_k - conj Z_{n-k}) / 2i, F_m = e^{-i m phi0} D_{m mod n} with
-// D_{n-k} = conj D_k, E = F_north + F_south, O = F_north - F_south.
-template <int CB>
-__device__ __forceinline__ void write_eo(const float2 *a, int stride, const RingPair &rp, int q, bool eq, int lmax,
-                                         int R, int N2, int nch, int cb0, float *__restrict__ E,
-                                         float *__restrict__ O)
-{
-  const int n = rp.nph, half = n / 2;
-  for (int m = threadIdx.x; m <= lmax; m += blockDim.x) {
-    int k = m % n;
-    const bool cj = k > half;
-    if (cj) k = n - k;
-    float2 ph = make_float2(1.f, 0.f);
-    if (rp.shifted) {
-      float sn, cs;
-      sincospif((float)(m % (2 * n)) / (float)n, &sn, &cs);
-      ph = make_float2(cs, -sn);
-    }
-#pragma unroll
-    for (int b = 0; b < CB; b++) {
-      const int c = cb0 + b;
-      if (c >= nch) continue;
-      const float2 zk = a[b * stride + k], zm = a[b * stride + (k ? n - k : 0)];
-      float2 dn = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
-      float2 ds = eq ? make_float2(0.f, 0.f) : make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
-      if (cj) {
-        dn.y = -dn.y;
-        ds.y = -ds.y;
-      }
-      const long long base = ((long long)m * R + q) * N2 + 2 * c;
-      *reinterpret_cast<float2 *>(E + base) = cmul(make_float2(dn.x + ds.x, dn.y + ds.y), ph);
-      *reinterpret_cast<float2 *>(O + base) = cmul(make_float2(dn.x - ds.x, dn.y - ds.y), ph);
-    }
-  }
-}
-
-// The Hermitian-packed synthesis input of frequency k of pair q: with Q_k the
-// folded sums (fold_one), H_k = Q_k / 2 and H_{n-k} = conj Q_k / 2 (0 < k < n/2),
-// H_0 = Re Q_0, H_{n/2} = Re Q_{n/2}; returns H_north,k + i H_south,k per channel
-template <int CB>
-__device__ __forceinline__ void packed_spectrum(const float *__restrict__ Gn, const float *__restrict__ Gs,
-                                                const RingPair &rp, int q, bool eq, int k, int lmax, int R, int N2,
-                                                int nch, int cb0, float2 *out)
+// The Hermitian-packed synthesis input of frequency k of pair q, channel c:
+// H_k = Q_k / 2 and H_{n-k} = conj Q_k / 2 (0 < k < n/2), H_0 = Re Q_0,
+// H_{n/2} = Re Q_{n/2}; returns H_north,k + i H_south,k (south zero on the equator)
+__device__ __forceinline__ float2 packed_value(const float *__restrict__ Gn, const float *__restrict__ Gs,
+                                              const RingPair &rp, const float2 *__restrict__ phtab, int q, bool eq,
+                                              int k, int lmax, int R, int N2, int c)
 {
   const int n = rp.nph, half = n / 2, kk = k <= half ? k : n - k;
-  float2 qn[CB], qs[CB];
-  fold_one<CB>(Gn, rp, q, kk, lmax, R, N2, nch, cb0, qn);
-  if (!eq) fold_one<CB>(Gs, rp, q, kk, lmax, R, N2, nch, cb0, qs);
-#pragma unroll
-  for (int b = 0; b < CB; b++) {
-    float2 hn = qn[b], hs = eq ? make_float2(0.f, 0.f) : qs[b];
-    if (k == 0 || k == half) {
-      hn.y = 0.f;
-      hs.y = 0.f;
-    } else {
-      hn = make_float2(0.5f * hn.x, 0.5f * (k < half ? hn.y : -hn.y));
-      hs = make_float2(0.5f * hs.x, 0.5f * (k < half ? hs.y : -hs.y));
-    }
-    out[b] = make_float2(hn.x - hs.y, hn.y + hs.x);
+  const long long mstride = (long long)R * N2, off = (long long)q * N2 + 2 * c;
+  const float2 ph = rp.shifted ? __ldg(phtab + rp.first_n + kk) : make_float2(1.f, 0.f);
+  float2 hn, hs;
+  fold_pair(Gn + off, Gs + off, mstride, kk, n, lmax, rp.shifted, ph, hn, hs);
+  if (eq) hs = make_float2(0.f, 0.f);
+  if (k == 0 || k == half) {
+    hn.y = 0.f;
+    hs.y = 0.f;
+  } else {
+    hn = make_float2(0.5f * hn.x, 0.5f * (k < half ? hn.y : -hn.y));
+    hs = make_float2(0.5f * hs.x, 0.5f * (k < half ? hs.y : -hs.y));
   }
+  return make_float2(hn.x - hs.y, hn.y + hs.x);
 }
 
-// Ring analysis of the equatorial ring pairs (q >= nside - 1: n = 4 nside, a power
-// of two) by one complex FFT per channel of z_j = north_j + i south_j, gathered in
-// bit-reversed order from global memory (shared-memory writes stay contiguous).
-template <int CB>
-__global__ __launch_bounds__(kRingThreads) void ring_analysis_fft_kernel(const float *__restrict__ maps, long long npix,
-                                                                     int nch, const RingPair *__restrict__ rings,
-                                                                     const float2 *__restrict__ tw2, int lmax, int R,
-                                                                     int N2, int q0, float *__restrict__ E,
-                                                                     float *__restrict__ O)
+// E and O of pair q for m = 0 .. lmax from the DFTs Z of z_j = north_j + i south_j
+// of S channels (z[b * PL + spad(k)], k < n): D_north,k = (Z_k + conj Z_{n-k}) / 2,
+// D_south,k = (Z_k - conj Z_{n-k}) / 2i, F_m = e^{-i m phi0} D_{m mod n} with
+// D_{n-k} = conj D_k, E = F_north + F_south, O = F_north - F_south.  One item per
+// (m, channel), channels fastest: consecutive threads store consecutive channels.
+// S = 2^lS divides the block; a thread keeps its channel and steps m, with
+// (j, k) = divmod(m, n) kept up to date without divisions.
+__device__ __forceinline__ void write_eo(const float2 *z, int PL, const RingPair &rp, const float2 *__restrict__ phtab,
+                                         int q, bool eq, int lmax, int R, int N2, int nch, int c0, int lS,
+                                         float *__restrict__ E, float *__restrict__ O)
 {
-  extern __shared__ __align__(16) float2 z[];  // [CB][n]
-  const int q = q0 + blockIdx.x, cb0 = blockIdx.y * CB;
-  const RingPair rp = rings[q];
-  const int n = rp.nph, logn = __ffs(n) - 1;
-  const bool eq = (q == R - 1);
-  for (int d = threadIdx.x; d < n; d += blockDim.x) {
-    const int j = bit_reverse(d, logn);
-#pragma unroll
-    for (int b = 0; b < CB; b++) {
-      const int c = cb0 + b;
-      float xn = 0.f, xs = 0.f;
-      if (c < nch) {
-        xn = __ldg(maps + (long long)c * npix + rp.first_n + j);
-        if (!eq) xs = __ldg(maps + (long long)c * npix + rp.first_s + j);
-      }
-      z[b * n + d] = make_float2(xn, xs);
+  const int n = rp.nph, half = n / 2, b = threadIdx.x & ((1 << lS) - 1), c = c0 + b;
+  if (c >= nch) return;
+  const int mstep = blockDim.x >> lS, jstep = mstep / n, kstep = mstep - jstep * n;
+  int m = threadIdx.x >> lS, j = m / n, kj = m - j * n;
+  for (; m <= lmax; m += mstep, kj += kstep, j += jstep) {
+    if (kj >= n) {
+      kj -= n;
+      j++;
     }
-  }
-  __syncthreads();
-  fft_dit<CB>(z, tw2, n, logn, -1.f);
-  write_eo<CB>(z, n, rp, q, eq, lmax, R, N2, nch, cb0, E, O);
-}
-
-// Ring synthesis of the equatorial ring pairs: the packed spectra, written in
-// bit-reversed order, through one complex inverse FFT whose real and imaginary
-// parts are the north and south rings' pixels.
-template <int CB>
-__global__ __launch_bounds__(kRingThreads) void ring_synthesis_fft_kernel(const float *__restrict__ Gn,
-                                                                      const float *__restrict__ Gs,
-                                                                      const RingPair *__restrict__ rings,
-                                                                      const float2 *__restrict__ tw2, int lmax,
-                                                                      int R, int N2, int nch, int q0,
-                                                                      float *__restrict__ maps, long long npix)
-{
-  extern __shared__ __align__(16) float2 z[];  // [CB][n]
-  const int q = q0 + blockIdx.x, cb0 = blockIdx.y * CB;
-  const RingPair rp = rings[q];
-  const int n = rp.nph, logn = __ffs(n) - 1;
-  const bool eq = (q == R - 1);
-  for (int d = threadIdx.x; d < n; d += blockDim.x) {
-    float2 h[CB];
-    packed_spectrum<CB>(Gn, Gs, rp, q, eq, bit_reverse(d, logn), lmax, R, N2, nch, cb0, h);
-#pragma unroll
-    for (int b = 0; b < CB; b++) z[b * n + d] = h[b];
-  }
-  __syncthreads();
-  fft_dit<CB>(z, tw2, n, logn, 1.f);
-  for (int j = threadIdx.x; j < n; j += blockDim.x) {
-#pragma unroll
-    for (int b = 0; b < CB; b++) {
-      const int c = cb0 + b;
-      if (c >= nch) continue;
-      const float2 v = z[b * n + j];
-      maps[(long long)c * npix + rp.first_n + j] = v.x;
-      if (!eq) maps[(long long)c * npix + rp.first_s + j] = v.y;
+    int k = kj;
+    float2 ph = make_float2(1.f, 0.f);
+    if (rp.shifted) {  // e^{-i pi m/n} = conj(e^{i pi k/n}) (-1)^j
+      const float2 t = __ldg(phtab + rp.first_n + k);
+      ph = (j & 1) ? make_float2(-t.x, t.y) : make_float2(t.x, -t.y);
     }
+    const bool cj = k > half;
+    if (cj) k = n - k;
+    const float2 zk = z[b * PL + spad(k)], zm = z[b * PL + spad(k ? n - k : 0)];
+    float2 dn = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+    float2 ds = eq ? make_float2(0.f, 0.f) : make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
+    if (cj) {
+      dn.y = -dn.y;
+      ds.y = -ds.y;
+    }
+    const long long base = ((long long)m * R + q) * N2 + 2 * c;
+    *reinterpret_cast<float2 *>(E + base) = cmul(make_float2(dn.x + ds.x, dn.y + ds.y), ph);
+    *reinterpret_cast<float2 *>(O + base) = cmul(make_float2(dn.x - ds.x, dn.y - ds.y), ph);
   }
 }
 
-
-// Bluestein DFT of the CB sequences a[b][j], j < n (zero beyond, length M):
-// Z_k = c_k (a c) (*) conj(c) with the chirp c_j = e^{-i pi j^2/n} (table ch,
-// FP64-evaluated on the host), the convolution by a DIF FFT, the product with
-// the precomputed spectrum of conj(c) (bit-reversed order, global) and a DIT
-// inverse FFT; on return a[b][k] = Z_k for k < n.
-template <int CB>
-__device__ void bluestein(float2 *a, const float2 *__restrict__ Bt, const float2 *__restrict__ tw2,
-                          const float2 *__restrict__ ch, int n, int M, int logM)
-{
-  for (int t = threadIdx.x; t < CB * n; t += blockDim.x) {
-    const int b = t / n, j = t - b * n;
-    a[b * M + j] = cmul(a[b * M + j], __ldg(ch + j));
-  }
-  __syncthreads();
-  fft_dif<CB>(a, tw2, M, logM, -1.f);
-  for (int t = threadIdx.x; t < CB * M; t += blockDim.x) a[t] = cmul(a[t], __ldg(Bt + (t & (M - 1))));
-  __syncthreads();
-  fft_dit<CB>(a, tw2, M, logM, 1.f);
-  const float inv = 1.f / (float)M;
-  for (int t = threadIdx.x; t < CB * n; t += blockDim.x) {
-    const int b = t / n, k = t - b * n;
-    const float2 v = cmul(a[b * M + k], __ldg(ch + k));
-    a[b * M + k] = make_float2(v.x * inv, v.y * inv);
-  }
-  __syncthreads();
-}
-
-// Ring analysis of the polar ring pairs (q < nside - 1, n = 4 (q + 1) pixels)
-// by a Bluestein DFT of z_j = north_j + i south_j.
-template <int CB>
-__global__ __launch_bounds__(kRingThreads) void ring_analysis_bluestein_kernel(
+// Ring analysis of one task.  Equatorial ring pairs (q >= nside - 1, n = 4 nside):
+// one FFT per channel of z_j = north_j + i south_j, loaded from global memory
+// straight into the first pass's registers.  Polar ring pairs (q < nside - 1,
+// n = 4 (q + 1)): Bluestein's DFT, Z_k = c_k sum_j (z_j c_j) b_{k-j} with the chirp
+// c_j = e^{-i pi j^2/n} (table ch, FP64-evaluated on the host) and b = conj(c),
+// the convolution as a forward FFT of M >= 2n - 1 points, the product with the
+// spectrum of b (table Bt) and an inverse FFT that takes the forward one's output
+// in registers.  Then E and O of every m.
+__global__ __launch_bounds__(kRingThreads, 2) void ring_analysis_kernel(
     const float *__restrict__ maps, long long npix, int nch, const RingPair *__restrict__ rings,
-    const float2 *__restrict__ tw2, const float2 *__restrict__ btab, const float2 *__restrict__ chirps, int lmax, int R,
-    int N2, float *__restrict__ E, float *__restrict__ O)
+    const int4 *__restrict__ tasks, const float2 *__restrict__ tw2, const float2 *__restrict__ btab,
+    const float2 *__restrict__ chirps, const float2 *__restrict__ phtab, int lmax, int R, int N2,
+    float *__restrict__ E, float *__restrict__ O)
 {
-  extern __shared__ __align__(16) float2 a[];  // [CB][M]
-  const int q = blockIdx.x, cb0 = blockIdx.y * CB;
+  extern __shared__ __align__(16) float2 z[];  // [S][pitch]
+  const int4 tk = tasks[blockIdx.x];
+  const int q = tk.x, c0 = tk.y, S = tk.z;
+  if (c0 >= nch) return;  // a task of channels beyond this batch (block-uniform)
   const RingPair rp = rings[q];
-  const int n = rp.nph, M = rp.bm, logM = __ffs(M) - 1;
-  for (int t = threadIdx.x; t < CB * M; t += blockDim.x) {
-    const int b = t / M, j = t - b * M, c = cb0 + b;
-    float2 v = make_float2(0.f, 0.f);
-    if (j < n && c < nch)
-      v = make_float2(maps[(long long)c * npix + rp.first_n + j], maps[(long long)c * npix + rp.first_s + j]);
-    a[t] = v;
+  const int n = rp.nph;
+  const bool blue = rp.bm > 0, eq = (q == R - 1);
+  const SeqLayout sl = seq_layout(blue ? rp.bm : n, S);
+  const int c = c0 + sl.b;
+  const bool live = sl.active && c < nch;
+  const float2 *ch = chirps + rp.tw_off, *Bt = btab + rp.b_off;
+  float2 *s = z + (sl.active ? sl.b : 0) * sl.PL;
+  float2 u[16];
+  if (sl.active) {
+    const float *mn = maps + (long long)(live ? c : 0) * npix + rp.first_n;
+    const float *ms = maps + (long long)(live ? c : 0) * npix + rp.first_s;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+      const int j = sl.t + sl.TS * i;
+      float2 v = make_float2(0.f, 0.f);
+      if (live && j < n) {
+        v.x = __ldg(mn + j);
+        if (!eq) v.y = __ldg(ms + j);
+        if (blue) v = cmul(v, __ldg(ch + j));
+      }
+      u[i] = v;
+    }
+  }
+  fft_run<-1, false>(u, s, tw2, sl.n, sl.L, sl.t, sl.TS, sl.active);
+  if (blue) {
+    if (sl.active) {
+#pragma unroll
+      for (int i = 0; i < 16; i++) {
+        const int j = sl.t + sl.TS * i;
+        if (j < sl.n) u[i] = cmul(u[i], __ldg(Bt + j));
+      }
+    }
+    fft_run<1, true>(u, s, tw2, sl.n, sl.L, sl.t, sl.TS, sl.active);
+  }
+  __syncthreads();  // every read of the last pass is done
+  if (sl.active) {
+    const float inv = 1.f / (float)sl.n;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+      const int k = sl.t + sl.TS * i;
+      if (k >= n) continue;
+      float2 v = u[i];
+      if (blue) {
+        v = cmul(v, __ldg(ch + k));
+        v = make_float2(v.x * inv, v.y * inv);
+      }
+      s[spad(k)] = v;
+    }
   }
   __syncthreads();
-  bluestein<CB>(a, btab + rp.b_off, tw2, chirps + rp.tw_off, n, M, logM);
-  write_eo<CB>(a, M, rp, q, false, lmax, R, N2, nch, cb0, E, O);
+  write_eo(z, sl.PL, rp, phtab, q, eq, lmax, R, N2, nch, c0, tk.w, E, O);
 }
 
-// Ring synthesis of the polar ring pairs: the packed spectra inverse-transformed
-// as conj(DFT(conj(.))) with the Bluestein DFT.
-template <int CB>
-__global__ __launch_bounds__(kRingThreads) void ring_synthesis_bluestein_kernel(
+// Ring synthesis of one task: the packed spectra (one item per (k, channel),
+// channels fastest, into shared memory), then for the equatorial ring pairs one
+// complex inverse FFT whose real and imaginary parts are the north and south
+// rings' pixels, for the polar ring pairs conj(DFT(conj(.))) by Bluestein's DFT;
+// the pixels are stored from the registers of the last pass.
+__global__ __launch_bounds__(kRingThreads, 2) void ring_synthesis_kernel(
     const float *__restrict__ Gn, const float *__restrict__ Gs, const RingPair *__restrict__ rings,
-    const float2 *__restrict__ tw2, const float2 *__restrict__ btab, const float2 *__restrict__ chirps, int lmax, int R,
-    int N2, int nch, float *__restrict__ maps, long long npix)
+    const int4 *__restrict__ tasks, const float2 *__restrict__ tw2, const float2 *__restrict__ btab,
+    const float2 *__restrict__ chirps, const float2 *__restrict__ phtab, int lmax, int R, int N2, int nch,
+    float *__restrict__ maps, long long npix)
 {
-  extern __shared__ __align__(16) float2 a[];  // [CB][M]
-  const int q = blockIdx.x, cb0 = blockIdx.y * CB;
+  extern __shared__ __align__(16) float2 z[];  // [S][pitch]
+  const int4 tk = tasks[blockIdx.x];
+  const int q = tk.x, c0 = tk.y, S = tk.z;
+  if (c0 >= nch) return;
   const RingPair rp = rings[q];
-  const int n = rp.nph, M = rp.bm, logM = __ffs(M) - 1;
-  for (int k = threadIdx.x; k < M; k += blockDim.x) {
-    float2 h[CB];
-    if (k < n) {
-      packed_spectrum<CB>(Gn, Gs, rp, q, false, k, lmax, R, N2, nch, cb0, h);
-    } else {
-#pragma unroll
-      for (int b = 0; b < CB; b++) h[b] = make_float2(0.f, 0.f);
+  const int n = rp.nph;
+  const bool blue = rp.bm > 0, eq = (q == R - 1);
+  const SeqLayout sl = seq_layout(blue ? rp.bm : n, S);
+  const float2 *ch = chirps + rp.tw_off, *Bt = btab + rp.b_off;
+  {  // one item per (k, channel), channels fastest (S = 2^lS divides the block)
+    const int b = threadIdx.x & (S - 1), c = c0 + b;
+    for (int k = threadIdx.x >> tk.w; k < sl.n; k += blockDim.x >> tk.w) {
+      float2 h = make_float2(0.f, 0.f);
+      if (k < n && c < nch) {
+        h = packed_value(Gn, Gs, rp, phtab, q, eq, k, lmax, R, N2, c);
+        if (blue) h = cmul(make_float2(h.x, -h.y), __ldg(ch + k));  // conjugated, times the chirp
+      }
+      z[b * sl.PL + spad(k)] = h;
     }
-#pragma unroll
-    for (int b = 0; b < CB; b++) a[b * M + k] = make_float2(h[b].x, -h[b].y);  // conjugated
   }
   __syncthreads();
-  bluestein<CB>(a, btab + rp.b_off, tw2, chirps + rp.tw_off, n, M, logM);
-  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+  const int c = c0 + sl.b;
+  float2 *s = z + (sl.active ? sl.b : 0) * sl.PL;
+  float2 u[16];
+  slots_load(u, s, sl.n, sl.t, sl.TS);  // all threads (idle ones read row 0): keeps u in registers
+  if (blue) {  // the forward FFT of Bluestein's convolution and the product with Bt
+    fft_run<-1, false>(u, s, tw2, sl.n, sl.L, sl.t, sl.TS, sl.active);
+    if (sl.active) {
 #pragma unroll
-    for (int b = 0; b < CB; b++) {
-      const int c = cb0 + b;
-      if (c >= nch) continue;
-      const float2 v = a[b * M + j];  // conj of the pixel pair (north + i south)
-      maps[(long long)c * npix + rp.first_n + j] = v.x;
-      maps[(long long)c * npix + rp.first_s + j] = -v.y;
+      for (int i = 0; i < 16; i++) {
+        const int j = sl.t + sl.TS * i;
+        if (j < sl.n) u[i] = cmul(u[i], __ldg(Bt + j));
+      }
     }
+  }
+  // the inverse FFT: the equatorial rings' transform, or the end of the convolution
+  // (the reversed plan, whose first pass takes the forward FFT's last in registers)
+  fft_run<1, true>(u, s, tw2, sl.n, sl.L, sl.t, sl.TS, sl.active);
+  if (sl.active && c < nch) {
+    float *mn = maps + (long long)c * npix + rp.first_n, *msr = maps + (long long)c * npix + rp.first_s;
+    const float inv = 1.f / (float)sl.n;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+      const int j = sl.t + sl.TS * i;
+      if (j >= n) continue;
+      if (blue) {
+        const float2 v = cmul(u[i], __ldg(ch + j));  // conj of the pixel pair (north + i south), times M
+        mn[j] = v.x * inv;
+        msr[j] = -v.y * inv;
+      } else {
+        mn[j] = u[i].x;
+        if (!eq) msr[j] = u[i].y;
+      }
+    }
+  }
+}
+
+// e^{i pi k/n} of every ring pair q at tab[first_n + k], k < n (FP64-evaluated)
+__global__ void ring_phase_kernel(const RingPair *__restrict__ rings, float2 *__restrict__ tab)
+{
+  const RingPair rp = rings[blockIdx.x];
+  for (int k = threadIdx.x; k < rp.nph; k += blockDim.x) {
+    double sn, cs;
+    sincospi((double)k / (double)rp.nph, &sn, &cs);
+    tab[rp.first_n + k] = make_float2((float)cs, (float)sn);
   }
 }
 
@@ -1204,7 +1120,7 @@ struct joint_ctx {
   float2 *btab = nullptr;  // polar rings: spectra of the conjugate Bluestein chirps (bit-reversed)
   float2 *chirps = nullptr;  // polar rings: the chirps e^{-i pi j^2/n}, at 2 i (i - 1) for n = 4 i
   float *lam = nullptr;
-  int chunk = 0, N2 = 0, bmax = 0;
+  int chunk = 0, N2 = 0;
   float *E = nullptr, *O = nullptr, *alm = nullptr, *sig2 = nullptr, *tmp_maps = nullptr;
   float2 *alm_hp = nullptr;
   int4 *tasks_a = nullptr, *tasks_s = nullptr;
@@ -1219,6 +1135,11 @@ struct joint_ctx {
   int *tc_err = nullptr;
   cudaEvent_t ev[5] = {};
   float times[4] = {};
+  // ring-transform tasks (q, c0, S) in decreasing work, e^{i pi k/n} per ring, block shared memory
+  int4 *rtasks = nullptr;
+  int nrtasks = 0;
+  float2 *phtab = nullptr;
+  size_t ring_smem = 0;
   // optional per-kernel-class device times of the beam (joint_gpu_profile):
   // ring analysis, Legendre analysis, Legendre synthesis, ring synthesis, E/O pack
   int prof = 0;
@@ -1253,11 +1174,6 @@ int jalloc(T **p, size_t count)
   return GETHI_OK;
 }
 
-size_t analysis_fft_smem(int n, int cb) { return (size_t)cb * n * 8; }
-size_t synthesis_fft_smem(int n, int cb) { return (size_t)cb * n * 8; }
-size_t bluestein_smem(int M, int cb) { return (size_t)cb * M * 8; }
-int ring_cb(long long nside) { return nside <= 512 ? 4 : 2; }        // channels per CTA, equatorial FFTs
-int bluestein_cb(long long nside) { return nside <= 512 ? 2 : 1; }   // channels per CTA, polar Bluestein
 int bluestein_size(int n)  // the power of two >= 2n - 1
 {
   int M = 1;
@@ -1435,7 +1351,7 @@ int ensure_sht(joint_ctx *c)
   }
   std::vector<float2> btab;
   for (int q = 0; q < N - 1; q++) {
-    const int n = rp[q].nph, M = rp[q].bm, logM = __builtin_ctz((unsigned)M);
+    const int n = rp[q].nph, M = rp[q].bm;
     std::vector<double> re(M, 0.0), im(M, 0.0);
     for (int t = 0; t < n; t++) {
       const double a = M_PI * (double)(((long long)t * t) % (2 * n)) / (double)n;
@@ -1449,11 +1365,7 @@ int ensure_sht(joint_ctx *c)
     host_fft(re, im);
     rp[q].b_off = (long long)btab.size();
     btab.resize(btab.size() + M);
-    for (int t = 0; t < M; t++) {
-      unsigned r = 0;
-      for (int bit = 0; bit < logM; bit++) r |= ((t >> bit) & 1u) << (logM - 1 - bit);
-      btab[rp[q].b_off + r] = make_float2((float)re[t], (float)im[t]);
-    }
+    for (int t = 0; t < M; t++) btab[rp[q].b_off + t] = make_float2((float)re[t], (float)im[t]);
   }
   int rc;
   const size_t lam_elems = (size_t)m_offset(lmax + 1, lmax) * R;
@@ -1507,30 +1419,36 @@ int ensure_sht(joint_ctx *c)
     return rc;
   JCK(cudaMemcpyAsync(c->tasks_a, ta.data(), sizeof(int4) * ta.size(), cudaMemcpyHostToDevice, c->stream));
   JCK(cudaMemcpyAsync(c->tasks_s, ts.data(), sizeof(int4) * ts.size(), cudaMemcpyHostToDevice, c->stream));
-  const int mb = Mmax, ne = (int)(4 * N);  // largest Bluestein size, equatorial ring length
-  if (ring_cb(N) == 4) {
-    JCK(cudaFuncSetAttribute(ring_analysis_fft_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)analysis_fft_smem(ne, 4)));
-    JCK(cudaFuncSetAttribute(ring_synthesis_fft_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)synthesis_fft_smem(ne, 4)));
-  } else {
-    JCK(cudaFuncSetAttribute(ring_analysis_fft_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)analysis_fft_smem(ne, 2)));
-    JCK(cudaFuncSetAttribute(ring_synthesis_fft_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)synthesis_fft_smem(ne, 2)));
+  // ring-transform tasks: per ring pair, blocks of S = threads / max(1, M/16) channels
+  // (M: ring length, or Bluestein size for the polar rings), largest work first
+  {
+    struct T {
+      int4 t;
+      double w;
+    };
+    std::vector<T> tl;
+    size_t smem = 0;
+    for (int q = 0; q < R; q++) {
+      const int M = rp[q].bm > 0 ? rp[q].bm : rp[q].nph, TS = std::max(1, M / 16);
+      int S = kRingThreads / TS;
+      while (S > c->chunk && S > 1) S >>= 1;  // a power of two, at most the batch (or 1)
+      smem = std::max(smem, (size_t)S * ring_pitch(M) * sizeof(float2));
+      const double w = (rp[q].bm > 0 ? 2.0 : 1.0) * S * M * std::max(1, __builtin_ctz((unsigned)M));
+      for (int c0 = 0; c0 < c->chunk; c0 += S) tl.push_back({make_int4(q, c0, S, __builtin_ctz((unsigned)S)), w});
+    }
+    std::stable_sort(tl.begin(), tl.end(), [](const T &x, const T &y) { return x.w > y.w; });
+    std::vector<int4> tv(tl.size());
+    for (size_t i = 0; i < tl.size(); i++) tv[i] = tl[i].t;
+    c->nrtasks = (int)tv.size();
+    c->ring_smem = smem;
+    const size_t nph = (size_t)(rp[R - 1].first_n + rp[R - 1].nph);
+    if ((rc = jalloc(&c->rtasks, tv.size())) || (rc = jalloc(&c->phtab, nph))) return rc;
+    JCK(cudaMemcpyAsync(c->rtasks, tv.data(), sizeof(int4) * tv.size(), cudaMemcpyHostToDevice, c->stream));
+    ring_phase_kernel<<<R, 256, 0, c->stream>>>(c->rings, c->phtab);
+    JCK(cudaGetLastError());
+    JCK(cudaFuncSetAttribute(ring_analysis_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    JCK(cudaFuncSetAttribute(ring_synthesis_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }
-  if (bluestein_cb(N) == 2) {
-    JCK(cudaFuncSetAttribute(ring_analysis_bluestein_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)bluestein_smem(mb, 2)));
-    JCK(cudaFuncSetAttribute(ring_synthesis_bluestein_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)bluestein_smem(mb, 2)));
-  } else {
-    JCK(cudaFuncSetAttribute(ring_analysis_bluestein_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)bluestein_smem(mb, 1)));
-    JCK(cudaFuncSetAttribute(ring_synthesis_bluestein_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)bluestein_smem(mb, 1)));
-  }
-  c->bmax = mb;
   if (c->p.sht_precision == 0 && N <= 512 && c->N2 == 128) {
     int rt = ensure_tc_tables(c);
     if (rt == GETHI_E_NOMEM) {  // the packed tables do not fit: FP32 CUDA cores
@@ -1541,38 +1459,6 @@ int ensure_sht(joint_ctx *c)
   }
   JCK(cudaStreamSynchronize(c->stream));
   return GETHI_OK;
-}
-
-// map2alm of nch (<= chunk) device maps into c->alm (beam factors when sig2 != null)
-template <int CB>
-void launch_ring_analysis(joint_ctx *c, const float *dmaps, int nch)
-{
-  const int N = c->p.nside, nb = (nch + CB - 1) / CB;
-  ring_analysis_fft_kernel<CB><<<dim3(N + 1, nb), kRingThreads, analysis_fft_smem(4 * N, CB), c->stream>>>(
-      dmaps, c->npix, nch, c->rings, c->tw2, c->lmax, c->R, c->N2, N - 1, c->E, c->O);
-}
-template <int CB>
-void launch_polar_analysis(joint_ctx *c, const float *dmaps, int nch)
-{
-  const int N = c->p.nside, nb = (nch + CB - 1) / CB;
-  if (N > 1)  // polar ring pairs q < N - 1
-    ring_analysis_bluestein_kernel<CB><<<dim3(N - 1, nb), kRingThreads, bluestein_smem(c->bmax, CB), c->stream>>>(
-        dmaps, c->npix, nch, c->rings, c->tw2, c->btab, c->chirps, c->lmax, c->R, c->N2, c->E, c->O);
-}
-template <int CB>
-void launch_ring_synthesis(joint_ctx *c, float *dmaps, int nch)
-{
-  const int N = c->p.nside, nb = (nch + CB - 1) / CB;
-  ring_synthesis_fft_kernel<CB><<<dim3(N + 1, nb), kRingThreads, synthesis_fft_smem(4 * N, CB), c->stream>>>(
-      c->E, c->O, c->rings, c->tw2, c->lmax, c->R, c->N2, nch, N - 1, dmaps, c->npix);
-}
-template <int CB>
-void launch_polar_synthesis(joint_ctx *c, float *dmaps, int nch)
-{
-  const int N = c->p.nside, nb = (nch + CB - 1) / CB;
-  if (N > 1)
-    ring_synthesis_bluestein_kernel<CB><<<dim3(N - 1, nb), kRingThreads, bluestein_smem(c->bmax, CB), c->stream>>>(
-        c->E, c->O, c->rings, c->tw2, c->btab, c->chirps, c->lmax, c->R, c->N2, nch, dmaps, c->npix);
 }
 
 // events around one kernel class when profiling (joint_gpu_profile)
@@ -1615,10 +1501,9 @@ int sht_analysis(joint_ctx *c, const float *dmaps, int nch, const float *sig2, b
 {
   {
     KSpan k(c, 0);
-    if (ring_cb(c->p.nside) == 4) launch_ring_analysis<4>(c, dmaps, nch);
-    else launch_ring_analysis<2>(c, dmaps, nch);
-    if (bluestein_cb(c->p.nside) == 2) launch_polar_analysis<2>(c, dmaps, nch);
-    else launch_polar_analysis<1>(c, dmaps, nch);
+    ring_analysis_kernel<<<c->nrtasks, kRingThreads, c->ring_smem, c->stream>>>(
+        dmaps, c->npix, nch, c->rings, c->rtasks, c->tw2, c->btab, c->chirps, c->phtab, c->lmax, c->R, c->N2, c->E,
+        c->O);
   }
   JCK(cudaGetLastError());
   const float w = (float)(4.0 * M_PI / (double)c->npix);
@@ -1656,10 +1541,9 @@ int sht_synthesis(joint_ctx *c, float *dmaps, int nch, bool tc)
   JCK(cudaGetLastError());
   {
     KSpan k(c, 3);
-    if (ring_cb(c->p.nside) == 4) launch_ring_synthesis<4>(c, dmaps, nch);
-    else launch_ring_synthesis<2>(c, dmaps, nch);
-    if (bluestein_cb(c->p.nside) == 2) launch_polar_synthesis<2>(c, dmaps, nch);
-    else launch_polar_synthesis<1>(c, dmaps, nch);
+    ring_synthesis_kernel<<<c->nrtasks, kRingThreads, c->ring_smem, c->stream>>>(
+        c->E, c->O, c->rings, c->rtasks, c->tw2, c->btab, c->chirps, c->phtab, c->lmax, c->R, c->N2, nch, dmaps,
+        c->npix);
   }
   JCK(cudaGetLastError());
   return GETHI_OK;
@@ -1745,7 +1629,7 @@ extern "C" void joint_gpu_free(joint_ctx *c)
                     (void *)c->sig2, (void *)c->tmp_maps, (void *)c->alm_hp, (void *)c->tasks_a, (void *)c->tasks_s,
                     (void *)c->noise_d, (void *)c->LA, (void *)c->LS, (void *)c->EOp, (void *)c->almp,
                     (void *)c->la_off, (void *)c->ls_off, (void *)c->alm_off, (void *)c->tasks_ta,
-                    (void *)c->tasks_ts, (void *)c->tc_err})
+                    (void *)c->tasks_ts, (void *)c->tc_err, (void *)c->rtasks, (void *)c->phtab})
     cudaFree(ptr);
   if (c->noise_h) cudaFreeHost(c->noise_h);
   for (cudaEvent_t e : c->kev) cudaEventDestroy(e);
