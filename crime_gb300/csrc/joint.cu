@@ -806,18 +806,19 @@ __global__ void __launch_bounds__(tcl::kThreads) pack_lambda_kernel(const float 
   }
 }
 
-// E and O packed by channel columns (rows = the 128 columns, K = ring pairs); one
-// CTA per (m, parity, K tile)
+// E and O packed by channel columns (rows = 128 columns of column tile ct, K = ring
+// pairs); one CTA per (m, parity, column tile, K tile), tile index
+// ((2 m + parity) NT + ct) nkq + kt
 __global__ void __launch_bounds__(tcl::kThreads) pack_eo_kernel(const float *__restrict__ E,
                                                                 const float *__restrict__ O, int R, int N2,
                                                                 float *__restrict__ out)
 {
-  const int nkq = (R + tcl::kK - 1) / tcl::kK;
-  const int kt = blockIdx.x % nkq, mp = blockIdx.x / nkq, m = mp >> 1, p = mp & 1;
-  const float *src = (p ? O : E) + (long long)m * R * N2;
+  const int nkq = (R + tcl::kK - 1) / tcl::kK, NT = N2 / tcl::kRows;
+  const int kt = blockIdx.x % nkq, rest = blockIdx.x / nkq, ct = rest % NT, mp = rest / NT, m = mp >> 1, p = mp & 1;
+  const float *src = (p ? O : E) + (long long)m * R * N2 + ct * tcl::kRows;
   const int q0 = kt * tcl::kK;
   float *tile = out + (long long)blockIdx.x * (tcl::kTile / 4);
-  pack_tile(tile, [&](int r, int k) { return (q0 + k < R && r < N2) ? src[(long long)(q0 + k) * N2 + r] : 0.f; });
+  pack_tile(tile, [&](int r, int k) { return q0 + k < R ? src[(long long)(q0 + k) * N2 + r] : 0.f; });
 }
 
 // the three MMAs of one K step (4 instructions of K = 8 each per 32-element tile)
@@ -884,20 +885,23 @@ __device__ bool tc_k_loop(unsigned char *sm, uint64_t *mbar, int nk, SrcA srcA, 
   return *fail == 0;
 }
 
-// analysis, one CTA per (m, parity, 128-row l' tile): a_lm of the 128 channel
-// columns, weight and beam applied, written packed for the synthesis
+// analysis, one CTA per (m, parity, 128-row l' tile, column tile ct): a_lm of the 128
+// channel columns of ct, weight and beam applied, written packed for the synthesis
+// (tile (alm_off + l'/32) NT + ct).  The column tiles of one l' tile are consecutive
+// tasks, so that the CTAs streaming the same lambda tiles run together and share
+// them through L2.
 __global__ void __launch_bounds__(tcl::kThreads, 1)
     tc_legendre_analysis_kernel(const float *__restrict__ LA, const long long *__restrict__ la_off,
                                 const float *__restrict__ EOp, float *__restrict__ almp,
                                 const long long *__restrict__ alm_off, const int4 *__restrict__ tasks, int R, int lmax,
-                                float w, const float *__restrict__ sig2, int *err)
+                                int NT, float w, const float *__restrict__ sig2, int *err)
 {
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ uint64_t mbar[tcl::kStages];
   __shared__ uint32_t tslot;
   __shared__ int fail;
   const int4 t = tasks[blockIdx.x];
-  const int m = t.x, p = t.y, mt = t.z;
+  const int m = t.x, p = t.y, mt = t.z, ct = t.w;
   const int ne = (lmax - m) / 2 + 1, M = p ? (lmax - m + 1) / 2 : ne;
   const int nkq = (R + tcl::kK - 1) / tcl::kK;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -915,7 +919,8 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
   tc::fence_after_sync();
   const uint32_t tm = tslot;
   const unsigned char *A0 = reinterpret_cast<const unsigned char *>(LA) + (la_off[2 * m + p] + (long long)mt * nkq) * tcl::kTile;
-  const unsigned char *B0 = reinterpret_cast<const unsigned char *>(EOp) + (long long)(2 * m + p) * nkq * tcl::kTile;
+  const unsigned char *B0 =
+      reinterpret_cast<const unsigned char *>(EOp) + ((long long)(2 * m + p) * NT + ct) * nkq * tcl::kTile;
   const bool ok = tc_k_loop(
       sm, mbar, nkq, [&](int kt) { return A0 + (long long)kt * tcl::kTile; },
       [&](int kt) { return B0 + (long long)kt * tcl::kTile; },
@@ -929,7 +934,7 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
     const int lp = mt * tcl::kRows + 32 * warp + lane;  // this thread's TMEM lane = row l'
     const bool valid = lp < M;
     const float l = (float)(m + 2 * lp + p);
-    float *tile = almp + (alm_off[2 * m + p] + (lp >> 5)) * (tcl::kTile / 4);
+    float *tile = almp + ((alm_off[2 * m + p] + (lp >> 5)) * NT + ct) * (tcl::kTile / 4);
     const uint32_t trow = tm + ((uint32_t)(32 * warp) << 16);
 #pragma unroll 1
     for (int cb = 0; cb < 128; cb += 32) {
@@ -941,7 +946,7 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
         for (int j = 0; j < 32; j++) {
           const int col = cb + j;
           float sc = w;
-          if (sig2) sc *= expf(-0.5f * l * (l + 1.f) * sig2[col >> 1]);
+          if (sig2) sc *= expf(-0.5f * l * (l + 1.f) * sig2[(ct * tcl::kRows + col) >> 1]);
           float hi, lo;
           split_tf32((v0[j] + v1[j]) * sc, hi, lo);
           const uint32_t o = tile_off(col, lp & 31) / 4;
@@ -960,8 +965,8 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
   if (warp == 0) tc::tmem_dealloc(tm, 256);
 }
 
-// synthesis, one CTA per (m, 128 ring pairs): G_e and G_o over the packed a_lm of
-// both parities; north = G_e + G_o, south = G_e - G_o, FP32 [m][q][col]
+// synthesis, one CTA per (m, 128 ring pairs, column tile ct): G_e and G_o over the
+// packed a_lm of both parities; north = G_e + G_o, south = G_e - G_o, FP32 [m][q][col]
 __global__ void __launch_bounds__(tcl::kThreads, 1)
     tc_legendre_synthesis_kernel(const float *__restrict__ LS, const long long *__restrict__ ls_off,
                                  const float *__restrict__ almp, const long long *__restrict__ alm_off,
@@ -973,7 +978,7 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
   __shared__ uint32_t tslot;
   __shared__ int fail;
   const int4 t = tasks[blockIdx.x];
-  const int m = t.x, qt = t.z;
+  const int m = t.x, qt = t.z, ct = t.w, NT = N2 / tcl::kRows;
   const int ne = (lmax - m) / 2 + 1, no = (lmax - m + 1) / 2;
   const int nke = (ne + tcl::kK - 1) / tcl::kK, nko = (no + tcl::kK - 1) / tcl::kK;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -1000,7 +1005,7 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
       },
       [&](int kt) {
         const int p = kt >= nke, k = p ? kt - nke : kt;
-        return Ab + (alm_off[2 * m + p] + k) * tcl::kTile;
+        return Ab + ((alm_off[2 * m + p] + k) * NT + ct) * tcl::kTile;
       },
       [&](int kt, uint32_t &a0, uint32_t &a1, bool &first) {
         const int p = kt >= nke;
@@ -1012,7 +1017,7 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
   if (ok) {
     const int q = qt * tcl::kRows + 32 * warp + lane;
     const uint32_t trow = tm + ((uint32_t)(32 * warp) << 16);
-    float *gn = Gn + ((long long)m * R + q) * N2, *gs = Gs + ((long long)m * R + q) * N2;
+    float *gn = Gn + ((long long)m * R + q) * N2 + ct * tcl::kRows, *gs = Gs + ((long long)m * R + q) * N2 + ct * tcl::kRows;
 #pragma unroll 1
     for (int cb = 0; cb < 128; cb += 32) {
       float e0[32], e1[32], o0[32], o1[32];
@@ -1023,7 +1028,6 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
       if (q < R) {
 #pragma unroll
         for (int j = 0; j < 32; j += 4) {
-          if (cb + j + 3 >= N2) break;
           float4 vn, vs;
           float ev[4], ov[4];
 #pragma unroll
@@ -1218,7 +1222,7 @@ void host_fft(std::vector<double> &re, std::vector<double> &im)
 // packed lambda tables, offsets and task lists of the tensor-core Legendre sums
 int ensure_tc_tables(joint_ctx *c)
 {
-  const int R = c->R, lmax = c->lmax;
+  const int R = c->R, lmax = c->lmax, NT = c->N2 / tcl::kRows;
   const int nkq = (R + tcl::kK - 1) / tcl::kK, nqt = (R + tcl::kRows - 1) / tcl::kRows;
   std::vector<long long> la(2 * (lmax + 1)), ls(2 * (lmax + 1)), al(2 * (lmax + 1));
   std::vector<int4> pa, ps, ta, ts;
@@ -1231,7 +1235,7 @@ int ensure_tc_tables(joint_ctx *c)
       ls[2 * m + p] = ns;
       al[2 * m + p] = nl;
       for (int mt = 0; mt < nmt; mt++) {
-        ta.push_back(make_int4(m, p, mt, 0));
+        for (int ct = 0; ct < NT; ct++) ta.push_back(make_int4(m, p, mt, ct));
         for (int kt = 0; kt < nkq; kt++) pa.push_back(make_int4(m, p, mt, kt));
       }
       for (int qt = 0; qt < nqt; qt++)
@@ -1240,13 +1244,15 @@ int ensure_tc_tables(joint_ctx *c)
       ns += (long long)nqt * nkl;
       nl += nkl;
     }
-    for (int qt = 0; qt < nqt; qt++) ts.push_back(make_int4(m, 0, qt, 0));
+    for (int qt = 0; qt < nqt; qt++)
+      for (int ct = 0; ct < NT; ct++) ts.push_back(make_int4(m, 0, qt, ct));
   }
   const size_t tw4 = tcl::kTile / 4;
   int rc;
   int4 *dpa = nullptr, *dps = nullptr;
   if ((rc = jalloc(&c->LA, (size_t)na * tw4)) || (rc = jalloc(&c->LS, (size_t)ns * tw4)) ||
-      (rc = jalloc(&c->EOp, (size_t)2 * (lmax + 1) * nkq * tw4)) || (rc = jalloc(&c->almp, (size_t)nl * tw4)) ||
+      (rc = jalloc(&c->EOp, (size_t)2 * (lmax + 1) * NT * nkq * tw4)) ||
+      (rc = jalloc(&c->almp, (size_t)nl * NT * tw4)) ||
       (rc = jalloc(&c->la_off, la.size())) || (rc = jalloc(&c->ls_off, ls.size())) ||
       (rc = jalloc(&c->alm_off, al.size())) || (rc = jalloc(&c->tasks_ta, ta.size())) ||
       (rc = jalloc(&c->tasks_ts, ts.size())) || (rc = jalloc(&c->tc_err, 1)) || (rc = jalloc(&dpa, pa.size())) ||
@@ -1269,7 +1275,7 @@ int ensure_tc_tables(joint_ctx *c)
   JCK(cudaMemcpyAsync(c->tasks_ts, ts.data(), sizeof(int4) * ts.size(), cudaMemcpyHostToDevice, c->stream));
   JCK(cudaMemcpyAsync(dpa, pa.data(), sizeof(int4) * pa.size(), cudaMemcpyHostToDevice, c->stream));
   JCK(cudaMemcpyAsync(dps, ps.data(), sizeof(int4) * ps.size(), cudaMemcpyHostToDevice, c->stream));
-  JCK(cudaMemsetAsync(c->almp, 0, sizeof(float) * nl * tw4, c->stream));  // l' padding stays zero
+  JCK(cudaMemsetAsync(c->almp, 0, sizeof(float) * nl * NT * tw4, c->stream));  // l' padding stays zero
   JCK(cudaMemsetAsync(c->tc_err, 0, sizeof(int), c->stream));
   pack_lambda_kernel<<<(unsigned)pa.size(), tcl::kThreads, 0, c->stream>>>(c->lam, dpa, c->la_off, R, lmax, 0, c->LA);
   JCK(cudaGetLastError());
@@ -1396,7 +1402,13 @@ int ensure_sht(joint_ctx *c)
   cudaFree(dl);
   cudaFree(dm);
   // channel batches and the GEMM tile lists
-  c->chunk = c->p.sht_chunk > 0 ? c->p.sht_chunk : 64;
+  // channels per batch: the tensor-core path reads the whole Legendre table once per
+  // batch and direction, so it takes every channel at once (columns in tiles of 64
+  // channels, up to 256); the CUDA-core path batches 64
+  const bool tc_ok = c->p.sht_precision == 0 && N <= 512;
+  c->chunk = c->p.sht_chunk > 0 ? c->p.sht_chunk
+             : tc_ok            ? std::min(256, 64 * ((c->p.n_nu + 63) / 64))
+                                : 64;
   c->N2 = 2 * c->chunk;
   const int tcol = (c->N2 + BN - 1) / BN;
   std::vector<int4> ta, ts;
@@ -1417,6 +1429,9 @@ int ensure_sht(joint_ctx *c)
       (rc = jalloc(&c->O, eo)) || (rc = jalloc(&c->alm, (size_t)m_offset(lmax + 1, lmax) * c->N2)) ||
       (rc = jalloc(&c->sig2, c->chunk)))
     return rc;
+  // columns of channels beyond a batch are never written by the ring transforms: zero
+  JCK(cudaMemsetAsync(c->E, 0, sizeof(float) * eo, c->stream));
+  JCK(cudaMemsetAsync(c->O, 0, sizeof(float) * eo, c->stream));
   JCK(cudaMemcpyAsync(c->tasks_a, ta.data(), sizeof(int4) * ta.size(), cudaMemcpyHostToDevice, c->stream));
   JCK(cudaMemcpyAsync(c->tasks_s, ts.data(), sizeof(int4) * ts.size(), cudaMemcpyHostToDevice, c->stream));
   // ring-transform tasks: per ring pair, blocks of S = threads / max(1, M/16) channels
@@ -1449,7 +1464,7 @@ int ensure_sht(joint_ctx *c)
     JCK(cudaFuncSetAttribute(ring_analysis_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     JCK(cudaFuncSetAttribute(ring_synthesis_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }
-  if (c->p.sht_precision == 0 && N <= 512 && c->N2 == 128) {
+  if (tc_ok && c->N2 % tcl::kRows == 0) {
     int rt = ensure_tc_tables(c);
     if (rt == GETHI_E_NOMEM) {  // the packed tables do not fit: FP32 CUDA cores
       cudaGetLastError();
@@ -1513,10 +1528,12 @@ int sht_analysis(joint_ctx *c, const float *dmaps, int nch, const float *sig2, b
       const int nkq = (c->R + tcl::kK - 1) / tcl::kK;
       {
         KSpan kp(c, 4);
-        pack_eo_kernel<<<2 * (c->lmax + 1) * nkq, tcl::kThreads, 0, c->stream>>>(c->E, c->O, c->R, c->N2, c->EOp);
+        pack_eo_kernel<<<2 * (c->lmax + 1) * (c->N2 / tcl::kRows) * nkq, tcl::kThreads, 0, c->stream>>>(
+            c->E, c->O, c->R, c->N2, c->EOp);
       }
       tc_legendre_analysis_kernel<<<c->ntasks_ta, tcl::kThreads, tcl::kSmem, c->stream>>>(
-          c->LA, c->la_off, c->EOp, c->almp, c->alm_off, c->tasks_ta, c->R, c->lmax, w, sig2, c->tc_err);
+          c->LA, c->la_off, c->EOp, c->almp, c->alm_off, c->tasks_ta, c->R, c->lmax, c->N2 / tcl::kRows, w, sig2,
+          c->tc_err);
     } else {
       legendre_analysis_kernel<<<c->ntasks_a, kThreads, 0, c->stream>>>(c->lam, c->E, c->O, c->alm, c->tasks_a,
                                                                         c->R, c->lmax, c->N2, w, sig2);

@@ -251,3 +251,26 @@ def test_tensor_and_fp32_legendre_agree_at_nside_512(jt):
         outs.append(j.run())
         j.close()
     assert rel_l2(outs[0], outs[1]) < 1e-5
+
+
+def test_tensor_core_column_tiles_match_fp32(jt):
+    """150 channels with 150 beam widths: the tensor-core path takes them as one batch
+    of three 64-channel column tiles (the last padded), the FP32 path in batches of 64;
+    per channel the two agree, and channels of each column tile match the oracle"""
+    nside = 32
+    rng = np.random.default_rng(150)
+    nu0 = np.linspace(500.0, 1300.0, 150)
+    nuf = nu0 + 5.0
+    maps = (rng.standard_normal((150, 12 * nside * nside)) * 2 + 1).astype(np.float32)
+    outs = []
+    for prec in ("auto", "fp32"):
+        j = jt.JoinT(nside, nu0, nuf, dish_diameter=6.0, sht_precision=prec)
+        j.add_maps(maps, nside)
+        outs.append(j.run())
+        assert j.uses_tensor_cores == (prec == "auto")
+        j.close()
+    for ch in range(150):
+        assert rel_l2(outs[0][ch], outs[1][ch]) < 1e-5, ch
+    sel = [0, 70, 149]
+    ref = orc.apply_beam(maps[sel], nside, orc.joint_fwhm(nu0[sel], nuf[sel], 6.0))
+    assert rel_l2(outs[0][sel], ref) <= BEAM_L2
