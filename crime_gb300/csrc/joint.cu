@@ -755,12 +755,6 @@ __device__ __forceinline__ void split_tf32(float x, float &hi, float &lo)
   lo = x - hi;
 }
 
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
-{
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc::smem_addr(smem)), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
 // Pack one 128 x 32 tile: thread r writes row r (32 values of get(r, k)), hi and lo
 template <class Get>
@@ -839,47 +833,60 @@ __device__ __forceinline__ void mma3(uint32_t acc0, uint32_t acc1, uint32_t a, u
 }
 
 // The K loop shared by both transforms: tiles kt = 0 .. nk-1, A and B of tile kt
-// at srcA(kt), srcB(kt); chain(kt) selects the accumulator pair and first(kt)
-// whether the tile starts it.  Returns false when an MMA wait expired.
+// (32 KB each, contiguous in global memory) at srcA(kt), srcB(kt); chain(kt)
+// selects the accumulator pair and first(kt) whether the tile starts it.  One
+// thread drives it: each stage is filled by two bulk copies completing on
+// full[s] and released by the commit of its MMAs to empty[s]; the stage of tile
+// kt - 1 is refilled once its MMAs are done, while those of tile kt are queued.
+// Every wait is bounded; on an expired wait the copies and MMAs in flight are
+// waited for (bounded again) and false is returned.
 template <class SrcA, class SrcB, class Chain>
-__device__ bool tc_k_loop(unsigned char *sm, uint64_t *mbar, int nk, SrcA srcA, SrcB srcB, Chain chain, int *fail)
+__device__ bool tc_k_loop(unsigned char *sm, uint64_t *full, uint64_t *empty, int nk, SrcA srcA, SrcB srcB,
+                          Chain chain, int *fail)
 {
-  const int tid = threadIdx.x;
-  auto load = [&](int kt) {
-    unsigned char *dst = sm + (kt % tcl::kStages) * tcl::kStageBytes;
-    const unsigned char *a = srcA(kt), *b = srcB(kt);
-    for (int i = tid; i < (int)(tcl::kStageBytes / 16); i += tcl::kThreads) {
-      const uint32_t o = 16u * i;
-      cp_async16(dst + o, o < tcl::kTile ? a + o : b + (o - tcl::kTile));
-    }
-  };
-  load(0);
-  cp_async_commit();
-  if (nk > 1) load(1);
-  cp_async_commit();
-  for (int kt = 0; kt < nk; kt++) {
-    const int s = kt % tcl::kStages;
-    cp_async_wait1();  // every group but the newest has landed: tile kt is in stage s
-    tc::fence_proxy_async();
-    tc::fence_before_sync();
-    __syncthreads();
-    if (tid == 0) {
+  constexpr int S = tcl::kStages;
+  if (threadIdx.x == 0) {
+    auto load = [&](int kt) {
+      const int s = kt % S;
+      unsigned char *dst = sm + s * tcl::kStageBytes;
+      tc::mbar_arrive_expect_tx(&full[s], tcl::kStageBytes);
+      tc::bulk_g2s(dst, srcA(kt), tcl::kTile, &full[s]);
+      tc::bulk_g2s(dst + tcl::kTile, srcB(kt), tcl::kTile, &full[s]);
+    };
+    int issued = 0, done = 0;  // tiles whose copies were issued / consumed by MMAs
+    bool ok = true;
+    for (; issued < nk && issued < S; issued++) load(issued);
+    for (int kt = 0; kt < nk; kt++) {
+      const int s = kt % S;
+      if (!tc::mbar_wait(&full[s], (kt / S) & 1, tcl::kWaitNs)) {
+        ok = false;
+        break;
+      }
       tc::fence_after_sync();
       const uint32_t a = tc::smem_addr(sm + s * tcl::kStageBytes), b = a + tcl::kTile;
       uint32_t acc0, acc1;
       bool first;
       chain(kt, acc0, acc1, first);
       mma3(acc0, acc1, a, b, first);
-      tc::mma_commit(&mbar[s]);
+      tc::mma_commit(&empty[s]);
+      done = kt + 1;
+      if (kt >= 1 && issued < nk) {  // refill the stage of tile kt - 1 with tile kt - 1 + S
+        const int sp = (kt - 1) % S;
+        if (!tc::mbar_wait(&empty[sp], ((kt - 1) / S) & 1, tcl::kWaitNs)) {
+          ok = false;
+          break;
+        }
+        load(issued++);
+      }
     }
-    if (kt + 2 < nk) {  // refill the stage of tile kt - 1 once its MMAs have completed
-      if (kt >= 1 && !tc::mbar_wait(&mbar[(kt - 1) % tcl::kStages], ((kt - 1) / tcl::kStages) & 1, tcl::kWaitNs))
-        *fail = 1;
-      load(kt + 2);
+    if (ok) {
+      ok = tc::mbar_wait(&empty[(nk - 1) % S], ((nk - 1) / S) & 1, tcl::kWaitNs);
+    } else {  // drain: copies of unconsumed tiles, then the last committed MMAs (bounded)
+      for (int kt = done; kt < issued; kt++) tc::mbar_wait(&full[kt % S], (kt / S) & 1, tcl::kWaitNs);
+      if (done > 0) tc::mbar_wait(&empty[(done - 1) % S], ((done - 1) / S) & 1, tcl::kWaitNs);
     }
-    cp_async_commit();
+    if (!ok) *fail = 1;
   }
-  if (!tc::mbar_wait(&mbar[(nk - 1) % tcl::kStages], ((nk - 1) / tcl::kStages) & 1, tcl::kWaitNs)) *fail = 1;
   __syncthreads();
   tc::fence_after_sync();
   return *fail == 0;
@@ -897,7 +904,7 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
                                 int NT, float w, const float *__restrict__ sig2, int *err)
 {
   extern __shared__ __align__(1024) unsigned char sm[];
-  __shared__ uint64_t mbar[tcl::kStages];
+  __shared__ uint64_t full[tcl::kStages], empty[tcl::kStages];
   __shared__ uint32_t tslot;
   __shared__ int fail;
   const int4 t = tasks[blockIdx.x];
@@ -911,7 +918,10 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
   if (skip) return;
   if (warp == 0) tc::tmem_alloc(&tslot, 256);
   if (tid == 0) {
-    for (int i = 0; i < tcl::kStages; i++) tc::mbar_init(&mbar[i], 1);
+    for (int i = 0; i < tcl::kStages; i++) {
+      tc::mbar_init(&full[i], 1);
+      tc::mbar_init(&empty[i], 1);
+    }
     fail = 0;
   }
   tc::fence_before_sync();
@@ -922,7 +932,7 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
   const unsigned char *B0 =
       reinterpret_cast<const unsigned char *>(EOp) + ((long long)(2 * m + p) * NT + ct) * nkq * tcl::kTile;
   const bool ok = tc_k_loop(
-      sm, mbar, nkq, [&](int kt) { return A0 + (long long)kt * tcl::kTile; },
+      sm, full, empty, nkq, [&](int kt) { return A0 + (long long)kt * tcl::kTile; },
       [&](int kt) { return B0 + (long long)kt * tcl::kTile; },
       [&](int kt, uint32_t &a0, uint32_t &a1, bool &first) {
         a0 = tm;
@@ -955,10 +965,8 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
         }
       }
     }
-  } else {
-    if (tid == 0) atomicExch(err, 1);
-    // MMAs may still be in flight: wait once more (bounded) before freeing their TMEM
-    tc::mbar_wait(&mbar[(nkq - 1) % tcl::kStages], ((nkq - 1) / tcl::kStages) & 1, tcl::kWaitNs);
+  } else if (tid == 0) {
+    atomicExch(err, 1);  // the K loop has drained its copies and MMAs
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -974,7 +982,7 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
                                  float *__restrict__ Gs, int *err)
 {
   extern __shared__ __align__(1024) unsigned char sm[];
-  __shared__ uint64_t mbar[tcl::kStages];
+  __shared__ uint64_t full[tcl::kStages], empty[tcl::kStages];
   __shared__ uint32_t tslot;
   __shared__ int fail;
   const int4 t = tasks[blockIdx.x];
@@ -988,7 +996,10 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
   if (skip) return;
   if (warp == 0) tc::tmem_alloc(&tslot, 512);
   if (tid == 0) {
-    for (int i = 0; i < tcl::kStages; i++) tc::mbar_init(&mbar[i], 1);
+    for (int i = 0; i < tcl::kStages; i++) {
+      tc::mbar_init(&full[i], 1);
+      tc::mbar_init(&empty[i], 1);
+    }
     fail = 0;
   }
   tc::fence_before_sync();
@@ -998,7 +1009,7 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
   const unsigned char *LSb = reinterpret_cast<const unsigned char *>(LS);
   const unsigned char *Ab = reinterpret_cast<const unsigned char *>(almp);
   const bool ok = tc_k_loop(
-      sm, mbar, nke + nko,
+      sm, full, empty, nke + nko,
       [&](int kt) {
         const int p = kt >= nke, k = p ? kt - nke : kt, nk = p ? nko : nke;
         return LSb + (ls_off[2 * m + p] + (long long)qt * nk + k) * tcl::kTile;
@@ -1042,10 +1053,8 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
         }
       }
     }
-  } else {
-    if (tid == 0) atomicExch(err, 1);
-    const int nk = nke + nko;  // MMAs may still be in flight: wait once more (bounded)
-    tc::mbar_wait(&mbar[(nk - 1) % tcl::kStages], ((nk - 1) / tcl::kStages) & 1, tcl::kWaitNs);
+  } else if (tid == 0) {
+    atomicExch(err, 1);  // the K loop has drained its copies and MMAs
   }
   tc::fence_before_sync();
   __syncthreads();

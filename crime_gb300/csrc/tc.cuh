@@ -103,6 +103,22 @@ __device__ __forceinline__ uint64_t global_ns()
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
+// one arrival on the mbarrier that also expects `bytes` of asynchronous copies
+// to complete on it (the phase completes when both have happened)
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *mbar, uint32_t bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(mbar)), "r"(bytes)
+               : "memory");
+}
+// bulk copy of `bytes` (a multiple of 16, both addresses 16-byte aligned) from
+// global to this CTA's shared memory, completing on mbar
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *mbar)
+{
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(mbar))
+      : "memory");
+}
 // bounded wait: false when the phase did not complete within limit_ns of the
 // GPU's global timer (try_wait may suspend the thread, so the bound is on time,
 // not on the number of polls)
