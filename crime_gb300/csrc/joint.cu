@@ -444,7 +444,7 @@ __global__ __launch_bounds__(kRingThreads, 2) void ring_analysis_kernel(
       u[i] = v;
     }
   }
-  fft_run<-1, false>(u, s, tw2, sl.n, sl.L, sl.t, sl.TS, sl.active);
+  fft_any<-1, false>(u, s, tw2, sl.n, sl.L, sl.t, sl.TS, sl.active);
   if (blue) {
     if (sl.active) {
 #pragma unroll
@@ -453,7 +453,7 @@ __global__ __launch_bounds__(kRingThreads, 2) void ring_analysis_kernel(
         if (j < sl.n) u[i] = cmul(u[i], __ldg(Bt + j));
       }
     }
-    fft_run<1, true>(u, s, tw2, sl.n, sl.L, sl.t, sl.TS, sl.active);
+    fft_any<1, true>(u, s, tw2, sl.n, sl.L, sl.t, sl.TS, sl.active);
   }
   __syncthreads();  // every read of the last pass is done
   if (sl.active) {
@@ -511,7 +511,7 @@ __global__ __launch_bounds__(kRingThreads, 2) void ring_synthesis_kernel(
   float2 u[16];
   slots_load(u, s, sl.n, sl.t, sl.TS);  // all threads (idle ones read row 0): keeps u in registers
   if (blue) {  // the forward FFT of Bluestein's convolution and the product with Bt
-    fft_run<-1, false>(u, s, tw2, sl.n, sl.L, sl.t, sl.TS, sl.active);
+    fft_any<-1, false>(u, s, tw2, sl.n, sl.L, sl.t, sl.TS, sl.active);
     if (sl.active) {
 #pragma unroll
       for (int i = 0; i < 16; i++) {
@@ -522,7 +522,7 @@ __global__ __launch_bounds__(kRingThreads, 2) void ring_synthesis_kernel(
   }
   // the inverse FFT: the equatorial rings' transform, or the end of the convolution
   // (the reversed plan, whose first pass takes the forward FFT's last in registers)
-  fft_run<1, true>(u, s, tw2, sl.n, sl.L, sl.t, sl.TS, sl.active);
+  fft_any<1, true>(u, s, tw2, sl.n, sl.L, sl.t, sl.TS, sl.active);
   if (sl.active && c < nch) {
     float *mn = maps + (long long)c * npix + rp.first_n, *msr = maps + (long long)c * npix + rp.first_s;
     const float inv = 1.f / (float)sl.n;

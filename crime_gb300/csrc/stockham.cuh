@@ -190,4 +190,66 @@ __device__ __forceinline__ void fft_run(float2 (&u)[16], float2 *s, const float2
   }
 }
 
+// log2 of the radix of pass p in the plan for 2^L points (L > 4), and the product
+// Ns of the radices before it
+__host__ __device__ constexpr int plan_lr(int L, int p, bool rev)
+{
+  return (rev ? p == (L + 3) / 4 - 1 : p == 0) ? L - 4 * ((L + 3) / 4 - 1) : 4;
+}
+__host__ __device__ constexpr int plan_ns(int L, int p, bool rev)
+{
+  int ns = 1;
+  for (int i = 0; i < p; i++) ns <<= plan_lr(L, i, rev);
+  return ns;
+}
+
+// pass P0 and the following ones of fft_fixed
+template <int L, int SIGN, bool REV, int P0>
+__device__ __forceinline__ void fixed_passes(float2 (&u)[16], float2 *s, const float2 *__restrict__ tw2, int t,
+                                             bool active)
+{
+  constexpr int P = (L + 3) / 4, TS = 1 << (L - 4);
+  if constexpr (P0 < P) {
+    constexpr int lr = plan_lr(L, P0, REV), R = 1 << lr, G = 16 / R, Ns = plan_ns(L, P0, REV);
+    if (active && P0 > 0) {
+#pragma unroll
+      for (int i = 0; i < 16; i++) u[i] = s[spad(t + TS * i)];
+    }
+    if (active) stockham_pass<R, G, SIGN>(u, t, TS, Ns, tw2);
+    if constexpr (P0 < P - 1) {
+      __syncthreads();
+      if (active) stockham_store<R, G>(u, s, t, TS, Ns);
+      __syncthreads();
+    }
+    fixed_passes<L, SIGN, REV, P0 + 1>(u, s, tw2, t, active);
+  }
+}
+
+// fft_run for a compile-time size 2^L (L > 4): the plan's radices, Ns and the
+// threads per sequence are constants, so the shared-memory and twiddle addresses
+// reduce to per-thread bases plus immediate offsets
+template <int L, int SIGN, bool REV>
+__device__ __forceinline__ void fft_fixed(float2 (&u)[16], float2 *s, const float2 *__restrict__ tw2, int t,
+                                          bool active)
+{
+  static_assert(L > 4 && L <= 13, "fft_fixed: 32 .. 8192 points");
+  fixed_passes<L, SIGN, REV, 0>(u, s, tw2, t, active);
+}
+
+// fft_run with the sizes 2^9 .. 2^13 (the equatorial rings and the larger
+// Bluestein convolutions) dispatched to fft_fixed
+template <int SIGN, bool REV>
+__device__ __forceinline__ void fft_any(float2 (&u)[16], float2 *s, const float2 *__restrict__ tw2, int n, int L, int t,
+                                        int TS, bool active)
+{
+  switch (L) {
+    case 9: fft_fixed<9, SIGN, REV>(u, s, tw2, t, active); break;
+    case 10: fft_fixed<10, SIGN, REV>(u, s, tw2, t, active); break;
+    case 11: fft_fixed<11, SIGN, REV>(u, s, tw2, t, active); break;
+    case 12: fft_fixed<12, SIGN, REV>(u, s, tw2, t, active); break;
+    case 13: fft_fixed<13, SIGN, REV>(u, s, tw2, t, active); break;
+    default: fft_run<SIGN, REV>(u, s, tw2, n, L, t, TS, active); break;
+  }
+}
+
 }  // namespace stockham
