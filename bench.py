@@ -435,13 +435,16 @@ def bench_joint(args):
         jt._check(jt.lib().joint_gpu_run(j._ctx, out.data_ptr()))
     e2e_ms = max_over_ranks(1e3 * (time.perf_counter() - t0), ws)
     assert np.isfinite(out.numpy()).all()
-    chunks = -(-n_nu // 64)
+    # channels per spherical-harmonic batch: every channel at once on the tensor-core path
+    # (column tiles of 64 channels, up to 256), batches of 64 on the CUDA cores
+    batch = min(256, 64 * -(-n_nu // 64)) if j.uses_tensor_cores else 64
+    chunks = -(-n_nu // batch)
     # per-kernel-class device time of the beam over one more profiled step
     j.profile(True)
     step()
     kt = j.kernel_times()
     j.profile(False)
-    lmax, R, N2 = 3 * nside - 1, 2 * nside, 2 * min(64, n_nu)
+    lmax, R, N2 = 3 * nside - 1, 2 * nside, 2 * min(batch, n_nu)  # N2: real columns of the first batch
     nalm = (lmax + 1) * (lmax + 2) // 2
     gemm_bytes = 4.0 * (nalm * R + 2 * (lmax + 1) * R * N2 + nalm * N2)  # Legendre table + E/O + a_lm per batch
     gemm_flops = 2.0 * nalm * R * N2
@@ -449,10 +452,12 @@ def bench_joint(args):
     if j.uses_tensor_cores:
         # the analysis GEMM alone (class "legendre_analysis" includes the E/O pack)
         ms_tc = (kt["legendre_analysis"][0] - kt["legendre_pack"][0]) / kt["legendre_analysis"][1]
-        nkq = -(-R // 32)
+        nkq, nt = -(-R // 32), batch // 64
         tiles = sum(-(-((lmax - m) // 2 + 1 if p == 0 else (lmax - m + 1) // 2) // 128) * nkq
                     for m in range(lmax + 1) for p in (0, 1))
-        packed = 32768.0 * (tiles + 2 * (lmax + 1) * nkq) + 8.0 * nalm * 128  # lambda + E/O tiles read, a_lm written
+        # lambda tiles read once (their column tiles share them through L2), the E/O tiles
+        # of every column tile read, the packed a_lm written
+        packed = 32768.0 * (tiles + 2 * (lmax + 1) * nkq * nt) + 8.0 * nalm * 128 * nt
         with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
             bf16 = float(json.load(f)["bf16_tflops"])
         achieved = gemm_bytes / (ms_tc / 1e3) / 1e9
@@ -461,7 +466,9 @@ def bench_joint(args):
                 "algorithmic_bytes_per_launch": gemm_bytes, "avg_launch_ms": round(ms_tc, 3),
                 "traffic": packed,
                 "traffic_source": "bytes of the packed operands per launch (hi and lo TF32 tiles of the Legendre "
-                                  "table and E/O, padded to 128 x 32 tiles, plus the packed a_lm written)",
+                                  "table read once and of E/O for every 64-channel column tile, padded to "
+                                  "128 x 32 tiles, plus the packed a_lm written)",
+                "batch_channels": batch,
                 "traffic_gbs": round(packed / (ms_tc / 1e3) / 1e9, 1),
                 "traffic_frac": round(packed / (ms_tc / 1e3) / 1e9 / peak_hbm, 3),
                 "tensor": {"tflops": round(3 * gemm_flops / (ms_tc / 1e3) / 1e12, 1),
@@ -497,9 +504,9 @@ def bench_joint(args):
         "roofline": roof,
         "e2e": {"value": whole_job_rate(units, args.steps, ws, e2e_ms), "unit": "pixels/s",
                 "h2d_bytes_per_step": int(4 * units * len(comp)), "d2h_bytes_per_step": int(4 * units)},
-        # per step: one sum of the device components, per batch the ring (FFT + Bluestein) and Legendre
-        # kernels (+ the E/O pack on the tensor-core path), noise, mask
-        "gpu_launches": args.steps * (1 + (7 if j.uses_tensor_cores else 6) * chunks + 2),
+        # per step: one sum of the device components, per batch the ring analysis and synthesis and
+        # the two Legendre kernels (+ the E/O pack on the tensor-core path), noise, mask
+        "gpu_launches": args.steps * (1 + (5 if j.uses_tensor_cores else 4) * chunks + 2),
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:
