@@ -731,20 +731,30 @@ __global__ __launch_bounds__(kThreads, 2) void legendre_synthesis_kernel(const f
 // error flag the host reads.
 // ---------------------------------------------------------------------------
 namespace tcl {
-constexpr int kRows = 128, kK = 32;
-constexpr uint32_t kHalf = kRows * kK * 4;  // 16 KB: the hi or the lo tile
-constexpr uint32_t kTile = 2 * kHalf;       // 32 KB
-constexpr int kStages = 3;
-constexpr uint32_t kStageBytes = 2 * kTile;  // A and B of one K step
-constexpr size_t kSmem = kStages * kStageBytes;
-constexpr uint32_t kLBO = 128, kSBO = 1024;
+// operand tiles: 128 rows x KK elements of K, hi then lo; the analysis operands
+// (lambda by l' rows, E/O) use KK = 16, the synthesis operands (lambda by ring
+// rows, the packed a_lm) KK = 32
+constexpr int kRows = 128, kKA = 16, kKS = 32;
+template <int KK>
+struct Geo {
+  static constexpr uint32_t kHalf = kRows * KK * 4;  // the hi or the lo tile
+  static constexpr uint32_t kTile = 2 * kHalf;
+  static constexpr uint32_t kStage = 2 * kTile;      // A and B of one K step
+  static constexpr uint32_t kSBO = 8 * KK * 4;       // stride of the 8-row core-matrix groups
+};
+// stages in flight: the analysis (256 TMEM columns) runs two CTAs per SM with three
+// 32 KB stages each, the synthesis (all 512 columns) one CTA with three 64 KB stages
+constexpr int kStagesA = 3, kStagesS = 3;
+constexpr size_t kSmemA = kStagesA * Geo<kKA>::kStage, kSmemS = kStagesS * Geo<kKS>::kStage;
+constexpr uint32_t kLBO = 128;  // K-adjacent core matrices
 constexpr int kThreads = 128;
 constexpr uint64_t kWaitNs = 1000000000ull;
 }  // namespace tcl
 
+template <int KK>
 __host__ __device__ inline uint32_t tile_off(int r, int k)
 {
-  return (uint32_t)((r >> 3) * 1024 + (k >> 2) * 128 + (r & 7) * 16 + (k & 3) * 4);
+  return (uint32_t)((r >> 3) * tcl::Geo<KK>::kSBO + (k >> 2) * 128 + (r & 7) * 16 + (k & 3) * 4);
 }
 
 __device__ __forceinline__ void split_tf32(float x, float &hi, float &lo)
@@ -756,26 +766,27 @@ __device__ __forceinline__ void split_tf32(float x, float &hi, float &lo)
 }
 
 
-// Pack one 128 x 32 tile: thread r writes row r (32 values of get(r, k)), hi and lo
-template <class Get>
+// Pack one 128 x KK tile: thread r writes row r (KK values of get(r, k)), hi and lo
+template <int KK, class Get>
 __device__ __forceinline__ void pack_tile(float *tile, Get get)
 {
   const int r = threadIdx.x;
 #pragma unroll
-  for (int g = 0; g < 8; g++) {
+  for (int g = 0; g < KK / 4; g++) {
     float4 h, l;
     split_tf32(get(r, 4 * g + 0), h.x, l.x);
     split_tf32(get(r, 4 * g + 1), h.y, l.y);
     split_tf32(get(r, 4 * g + 2), h.z, l.z);
     split_tf32(get(r, 4 * g + 3), h.w, l.w);
-    const uint32_t o = tile_off(r, 4 * g) / 4;
+    const uint32_t o = tile_off<KK>(r, 4 * g) / 4;
     *reinterpret_cast<float4 *>(tile + o) = h;
-    *reinterpret_cast<float4 *>(tile + tcl::kHalf / 4 + o) = l;
+    *reinterpret_cast<float4 *>(tile + tcl::Geo<KK>::kHalf / 4 + o) = l;
   }
 }
 
 // lambda tables packed for the analysis (rows l', K = ring pairs; task = (m, p, l' tile,
 // K tile)) and for the synthesis (rows = ring pairs, K = l'; task = (m, p, q tile, K tile))
+template <int KK>
 __global__ void __launch_bounds__(tcl::kThreads) pack_lambda_kernel(const float *__restrict__ lam,
                                                                     const int4 *__restrict__ tasks,
                                                                     const long long *__restrict__ off, int R, int lmax,
@@ -785,16 +796,16 @@ __global__ void __launch_bounds__(tcl::kThreads) pack_lambda_kernel(const float 
   const int m = t.x, p = t.y;
   const int ne = (lmax - m) / 2 + 1, M = p ? (lmax - m + 1) / 2 : ne;
   const float *L = lam + (m_offset(m, lmax) + (p ? ne : 0)) * (long long)R;
-  const int nkq = (R + tcl::kK - 1) / tcl::kK, nkl = (M + tcl::kK - 1) / tcl::kK;
-  float *tile = out + (off[2 * m + p] + (long long)t.z * (by_ring ? nkl : nkq) + t.w) * (tcl::kTile / 4);
+  const int nkq = (R + KK - 1) / KK, nkl = (M + KK - 1) / KK;
+  float *tile = out + (off[2 * m + p] + (long long)t.z * (by_ring ? nkl : nkq) + t.w) * (tcl::Geo<KK>::kTile / 4);
   if (!by_ring) {
-    const int l0 = t.z * tcl::kRows, q0 = t.w * tcl::kK;
-    pack_tile(tile, [&](int r, int k) {
+    const int l0 = t.z * tcl::kRows, q0 = t.w * KK;
+    pack_tile<KK>(tile, [&](int r, int k) {
       return (l0 + r < M && q0 + k < R) ? L[(long long)(l0 + r) * R + q0 + k] : 0.f;
     });
   } else {
-    const int qq = t.z * tcl::kRows, l0 = t.w * tcl::kK;
-    pack_tile(tile, [&](int r, int k) {
+    const int qq = t.z * tcl::kRows, l0 = t.w * KK;
+    pack_tile<KK>(tile, [&](int r, int k) {
       return (qq + r < R && l0 + k < M) ? L[(long long)(l0 + k) * R + qq + r] : 0.f;
     });
   }
@@ -807,24 +818,27 @@ __global__ void __launch_bounds__(tcl::kThreads) pack_eo_kernel(const float *__r
                                                                 const float *__restrict__ O, int R, int N2,
                                                                 float *__restrict__ out)
 {
-  const int nkq = (R + tcl::kK - 1) / tcl::kK, NT = N2 / tcl::kRows;
+  constexpr int KK = tcl::kKA;
+  const int nkq = (R + KK - 1) / KK, NT = N2 / tcl::kRows;
   const int kt = blockIdx.x % nkq, rest = blockIdx.x / nkq, ct = rest % NT, mp = rest / NT, m = mp >> 1, p = mp & 1;
   const float *src = (p ? O : E) + (long long)m * R * N2 + ct * tcl::kRows;
-  const int q0 = kt * tcl::kK;
-  float *tile = out + (long long)blockIdx.x * (tcl::kTile / 4);
-  pack_tile(tile, [&](int r, int k) { return q0 + k < R ? src[(long long)(q0 + k) * N2 + r] : 0.f; });
+  const int q0 = kt * KK;
+  float *tile = out + (long long)blockIdx.x * (tcl::Geo<KK>::kTile / 4);
+  pack_tile<KK>(tile, [&](int r, int k) { return q0 + k < R ? src[(long long)(q0 + k) * N2 + r] : 0.f; });
 }
 
-// the three MMAs of one K step (4 instructions of K = 8 each per 32-element tile)
+// the three MMAs of one K step (KK / 8 instructions of K = 8 each per tile)
+template <int KK>
 __device__ __forceinline__ void mma3(uint32_t acc0, uint32_t acc1, uint32_t a, uint32_t b, bool first)
 {
   constexpr uint32_t idesc = tc::idesc_tf32_f32(128, 128);
 #pragma unroll
-  for (int kk = 0; kk < 4; kk++) {
-    const uint64_t ah = tc::smem_desc(a + 256 * kk, tcl::kLBO, tcl::kSBO);
-    const uint64_t al = tc::smem_desc(a + tcl::kHalf + 256 * kk, tcl::kLBO, tcl::kSBO);
-    const uint64_t bh = tc::smem_desc(b + 256 * kk, tcl::kLBO, tcl::kSBO);
-    const uint64_t bl = tc::smem_desc(b + tcl::kHalf + 256 * kk, tcl::kLBO, tcl::kSBO);
+  constexpr uint32_t sbo = tcl::Geo<KK>::kSBO, half = tcl::Geo<KK>::kHalf;
+  for (int kk = 0; kk < KK / 8; kk++) {
+    const uint64_t ah = tc::smem_desc(a + 256 * kk, tcl::kLBO, sbo);
+    const uint64_t al = tc::smem_desc(a + half + 256 * kk, tcl::kLBO, sbo);
+    const uint64_t bh = tc::smem_desc(b + 256 * kk, tcl::kLBO, sbo);
+    const uint64_t bl = tc::smem_desc(b + half + 256 * kk, tcl::kLBO, sbo);
     const uint32_t acc = (first && kk == 0) ? 0u : 1u;
     tc::mma_tf32(acc0, ah, bh, idesc, acc);
     tc::mma_tf32(acc1, ah, bl, idesc, acc);
@@ -833,25 +847,25 @@ __device__ __forceinline__ void mma3(uint32_t acc0, uint32_t acc1, uint32_t a, u
 }
 
 // The K loop shared by both transforms: tiles kt = 0 .. nk-1, A and B of tile kt
-// (32 KB each, contiguous in global memory) at srcA(kt), srcB(kt); chain(kt)
-// selects the accumulator pair and first(kt) whether the tile starts it.  One
-// thread drives it: each stage is filled by two bulk copies completing on
-// full[s] and released by the commit of its MMAs to empty[s]; the stage of tile
-// kt - 1 is refilled once its MMAs are done, while those of tile kt are queued.
-// Every wait is bounded; on an expired wait the copies and MMAs in flight are
-// waited for (bounded again) and false is returned.
-template <class SrcA, class SrcB, class Chain>
+// (Geo<KK>::kTile bytes each, contiguous in global memory) at srcA(kt), srcB(kt);
+// chain(kt) selects the accumulator pair and first(kt) whether the tile starts it;
+// S stages.  One thread drives it: each stage is filled by two bulk copies
+// completing on full[s] and released by the commit of its MMAs to empty[s]; the
+// stage of tile kt - 1 is refilled once its MMAs are done, while those of tile kt
+// are queued.  Every wait is bounded; on an expired wait the copies and MMAs in
+// flight are waited for (bounded again) and false is returned.
+template <int S, int KK, class SrcA, class SrcB, class Chain>
 __device__ bool tc_k_loop(unsigned char *sm, uint64_t *full, uint64_t *empty, int nk, SrcA srcA, SrcB srcB,
                           Chain chain, int *fail)
 {
-  constexpr int S = tcl::kStages;
+  using G = tcl::Geo<KK>;
   if (threadIdx.x == 0) {
     auto load = [&](int kt) {
       const int s = kt % S;
-      unsigned char *dst = sm + s * tcl::kStageBytes;
-      tc::mbar_arrive_expect_tx(&full[s], tcl::kStageBytes);
-      tc::bulk_g2s(dst, srcA(kt), tcl::kTile, &full[s]);
-      tc::bulk_g2s(dst + tcl::kTile, srcB(kt), tcl::kTile, &full[s]);
+      unsigned char *dst = sm + s * G::kStage;
+      tc::mbar_arrive_expect_tx(&full[s], G::kStage);
+      tc::bulk_g2s(dst, srcA(kt), G::kTile, &full[s]);
+      tc::bulk_g2s(dst + G::kTile, srcB(kt), G::kTile, &full[s]);
     };
     int issued = 0, done = 0;  // tiles whose copies were issued / consumed by MMAs
     bool ok = true;
@@ -863,11 +877,11 @@ __device__ bool tc_k_loop(unsigned char *sm, uint64_t *full, uint64_t *empty, in
         break;
       }
       tc::fence_after_sync();
-      const uint32_t a = tc::smem_addr(sm + s * tcl::kStageBytes), b = a + tcl::kTile;
+      const uint32_t a = tc::smem_addr(sm + s * G::kStage), b = a + G::kTile;
       uint32_t acc0, acc1;
       bool first;
       chain(kt, acc0, acc1, first);
-      mma3(acc0, acc1, a, b, first);
+      mma3<KK>(acc0, acc1, a, b, first);
       tc::mma_commit(&empty[s]);
       done = kt + 1;
       if (kt >= 1 && issued < nk) {  // refill the stage of tile kt - 1 with tile kt - 1 + S
@@ -897,20 +911,22 @@ __device__ bool tc_k_loop(unsigned char *sm, uint64_t *full, uint64_t *empty, in
 // (tile (alm_off + l'/32) NT + ct).  The column tiles of one l' tile are consecutive
 // tasks, so that the CTAs streaming the same lambda tiles run together and share
 // them through L2.
-__global__ void __launch_bounds__(tcl::kThreads, 1)
+__global__ void __launch_bounds__(tcl::kThreads, 2)
     tc_legendre_analysis_kernel(const float *__restrict__ LA, const long long *__restrict__ la_off,
                                 const float *__restrict__ EOp, float *__restrict__ almp,
                                 const long long *__restrict__ alm_off, const int4 *__restrict__ tasks, int R, int lmax,
                                 int NT, float w, const float *__restrict__ sig2, int *err)
 {
   extern __shared__ __align__(1024) unsigned char sm[];
-  __shared__ uint64_t full[tcl::kStages], empty[tcl::kStages];
+  __shared__ uint64_t full[tcl::kStagesA], empty[tcl::kStagesA];
   __shared__ uint32_t tslot;
   __shared__ int fail;
   const int4 t = tasks[blockIdx.x];
   const int m = t.x, p = t.y, mt = t.z, ct = t.w;
   const int ne = (lmax - m) / 2 + 1, M = p ? (lmax - m + 1) / 2 : ne;
-  const int nkq = (R + tcl::kK - 1) / tcl::kK;
+  using GA = tcl::Geo<tcl::kKA>;
+  using GS = tcl::Geo<tcl::kKS>;
+  const int nkq = (R + tcl::kKA - 1) / tcl::kKA;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   __shared__ int skip;  // an earlier CTA's MMA wait expired: no new work (decided once for the CTA)
   if (tid == 0) skip = *(volatile int *)err;
@@ -918,7 +934,7 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
   if (skip) return;
   if (warp == 0) tc::tmem_alloc(&tslot, 256);
   if (tid == 0) {
-    for (int i = 0; i < tcl::kStages; i++) {
+    for (int i = 0; i < tcl::kStagesA; i++) {
       tc::mbar_init(&full[i], 1);
       tc::mbar_init(&empty[i], 1);
     }
@@ -928,12 +944,12 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tm = tslot;
-  const unsigned char *A0 = reinterpret_cast<const unsigned char *>(LA) + (la_off[2 * m + p] + (long long)mt * nkq) * tcl::kTile;
+  const unsigned char *A0 = reinterpret_cast<const unsigned char *>(LA) + (la_off[2 * m + p] + (long long)mt * nkq) * GA::kTile;
   const unsigned char *B0 =
-      reinterpret_cast<const unsigned char *>(EOp) + ((long long)(2 * m + p) * NT + ct) * nkq * tcl::kTile;
-  const bool ok = tc_k_loop(
-      sm, full, empty, nkq, [&](int kt) { return A0 + (long long)kt * tcl::kTile; },
-      [&](int kt) { return B0 + (long long)kt * tcl::kTile; },
+      reinterpret_cast<const unsigned char *>(EOp) + ((long long)(2 * m + p) * NT + ct) * nkq * GA::kTile;
+  const bool ok = tc_k_loop<tcl::kStagesA, tcl::kKA>(
+      sm, full, empty, nkq, [&](int kt) { return A0 + (long long)kt * GA::kTile; },
+      [&](int kt) { return B0 + (long long)kt * GA::kTile; },
       [&](int kt, uint32_t &a0, uint32_t &a1, bool &first) {
         a0 = tm;
         a1 = tm + 128;
@@ -944,7 +960,8 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
     const int lp = mt * tcl::kRows + 32 * warp + lane;  // this thread's TMEM lane = row l'
     const bool valid = lp < M;
     const float l = (float)(m + 2 * lp + p);
-    float *tile = almp + ((alm_off[2 * m + p] + (lp >> 5)) * NT + ct) * (tcl::kTile / 4);
+    // the a_lm in the synthesis' B geometry (rows = columns, K = l' in tiles of kKS)
+    float *tile = almp + ((alm_off[2 * m + p] + lp / tcl::kKS) * NT + ct) * (GS::kTile / 4);
     const uint32_t trow = tm + ((uint32_t)(32 * warp) << 16);
 #pragma unroll 1
     for (int cb = 0; cb < 128; cb += 32) {
@@ -959,9 +976,9 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
           if (sig2) sc *= expf(-0.5f * l * (l + 1.f) * sig2[(ct * tcl::kRows + col) >> 1]);
           float hi, lo;
           split_tf32((v0[j] + v1[j]) * sc, hi, lo);
-          const uint32_t o = tile_off(col, lp & 31) / 4;
+          const uint32_t o = tile_off<tcl::kKS>(col, lp & (tcl::kKS - 1)) / 4;
           tile[o] = hi;
-          tile[tcl::kHalf / 4 + o] = lo;
+          tile[GS::kHalf / 4 + o] = lo;
         }
       }
     }
@@ -982,13 +999,14 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
                                  float *__restrict__ Gs, int *err)
 {
   extern __shared__ __align__(1024) unsigned char sm[];
-  __shared__ uint64_t full[tcl::kStages], empty[tcl::kStages];
+  __shared__ uint64_t full[tcl::kStagesS], empty[tcl::kStagesS];
   __shared__ uint32_t tslot;
   __shared__ int fail;
   const int4 t = tasks[blockIdx.x];
   const int m = t.x, qt = t.z, ct = t.w, NT = N2 / tcl::kRows;
   const int ne = (lmax - m) / 2 + 1, no = (lmax - m + 1) / 2;
-  const int nke = (ne + tcl::kK - 1) / tcl::kK, nko = (no + tcl::kK - 1) / tcl::kK;
+  using GS = tcl::Geo<tcl::kKS>;
+  const int nke = (ne + tcl::kKS - 1) / tcl::kKS, nko = (no + tcl::kKS - 1) / tcl::kKS;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   __shared__ int skip;  // an earlier CTA's MMA wait expired: no new work (decided once for the CTA)
   if (tid == 0) skip = *(volatile int *)err;
@@ -996,7 +1014,7 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
   if (skip) return;
   if (warp == 0) tc::tmem_alloc(&tslot, 512);
   if (tid == 0) {
-    for (int i = 0; i < tcl::kStages; i++) {
+    for (int i = 0; i < tcl::kStagesS; i++) {
       tc::mbar_init(&full[i], 1);
       tc::mbar_init(&empty[i], 1);
     }
@@ -1008,15 +1026,15 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
   const uint32_t tm = tslot;
   const unsigned char *LSb = reinterpret_cast<const unsigned char *>(LS);
   const unsigned char *Ab = reinterpret_cast<const unsigned char *>(almp);
-  const bool ok = tc_k_loop(
+  const bool ok = tc_k_loop<tcl::kStagesS, tcl::kKS>(
       sm, full, empty, nke + nko,
       [&](int kt) {
         const int p = kt >= nke, k = p ? kt - nke : kt, nk = p ? nko : nke;
-        return LSb + (ls_off[2 * m + p] + (long long)qt * nk + k) * tcl::kTile;
+        return LSb + (ls_off[2 * m + p] + (long long)qt * nk + k) * GS::kTile;
       },
       [&](int kt) {
         const int p = kt >= nke, k = p ? kt - nke : kt;
-        return Ab + ((alm_off[2 * m + p] + k) * NT + ct) * tcl::kTile;
+        return Ab + ((alm_off[2 * m + p] + k) * NT + ct) * GS::kTile;
       },
       [&](int kt, uint32_t &a0, uint32_t &a1, bool &first) {
         const int p = kt >= nke;
@@ -1232,14 +1250,14 @@ void host_fft(std::vector<double> &re, std::vector<double> &im)
 int ensure_tc_tables(joint_ctx *c)
 {
   const int R = c->R, lmax = c->lmax, NT = c->N2 / tcl::kRows;
-  const int nkq = (R + tcl::kK - 1) / tcl::kK, nqt = (R + tcl::kRows - 1) / tcl::kRows;
+  const int nkq = (R + tcl::kKA - 1) / tcl::kKA, nqt = (R + tcl::kRows - 1) / tcl::kRows;
   std::vector<long long> la(2 * (lmax + 1)), ls(2 * (lmax + 1)), al(2 * (lmax + 1));
   std::vector<int4> pa, ps, ta, ts;
   long long na = 0, ns = 0, nl = 0;
   for (int m = 0; m <= lmax; m++) {
     for (int p = 0; p < 2; p++) {
       const int M = p ? (lmax - m + 1) / 2 : (lmax - m) / 2 + 1;
-      const int nmt = (M + tcl::kRows - 1) / tcl::kRows, nkl = (M + tcl::kK - 1) / tcl::kK;
+      const int nmt = (M + tcl::kRows - 1) / tcl::kRows, nkl = (M + tcl::kKS - 1) / tcl::kKS;
       la[2 * m + p] = na;
       ls[2 * m + p] = ns;
       al[2 * m + p] = nl;
@@ -1256,12 +1274,12 @@ int ensure_tc_tables(joint_ctx *c)
     for (int qt = 0; qt < nqt; qt++)
       for (int ct = 0; ct < NT; ct++) ts.push_back(make_int4(m, 0, qt, ct));
   }
-  const size_t tw4 = tcl::kTile / 4;
+  const size_t twa = tcl::Geo<tcl::kKA>::kTile / 4, tws = tcl::Geo<tcl::kKS>::kTile / 4;
   int rc;
   int4 *dpa = nullptr, *dps = nullptr;
-  if ((rc = jalloc(&c->LA, (size_t)na * tw4)) || (rc = jalloc(&c->LS, (size_t)ns * tw4)) ||
-      (rc = jalloc(&c->EOp, (size_t)2 * (lmax + 1) * NT * nkq * tw4)) ||
-      (rc = jalloc(&c->almp, (size_t)nl * NT * tw4)) ||
+  if ((rc = jalloc(&c->LA, (size_t)na * twa)) || (rc = jalloc(&c->LS, (size_t)ns * tws)) ||
+      (rc = jalloc(&c->EOp, (size_t)2 * (lmax + 1) * NT * nkq * twa)) ||
+      (rc = jalloc(&c->almp, (size_t)nl * NT * tws)) ||
       (rc = jalloc(&c->la_off, la.size())) || (rc = jalloc(&c->ls_off, ls.size())) ||
       (rc = jalloc(&c->alm_off, al.size())) || (rc = jalloc(&c->tasks_ta, ta.size())) ||
       (rc = jalloc(&c->tasks_ts, ts.size())) || (rc = jalloc(&c->tc_err, 1)) || (rc = jalloc(&dpa, pa.size())) ||
@@ -1284,14 +1302,16 @@ int ensure_tc_tables(joint_ctx *c)
   JCK(cudaMemcpyAsync(c->tasks_ts, ts.data(), sizeof(int4) * ts.size(), cudaMemcpyHostToDevice, c->stream));
   JCK(cudaMemcpyAsync(dpa, pa.data(), sizeof(int4) * pa.size(), cudaMemcpyHostToDevice, c->stream));
   JCK(cudaMemcpyAsync(dps, ps.data(), sizeof(int4) * ps.size(), cudaMemcpyHostToDevice, c->stream));
-  JCK(cudaMemsetAsync(c->almp, 0, sizeof(float) * nl * NT * tw4, c->stream));  // l' padding stays zero
+  JCK(cudaMemsetAsync(c->almp, 0, sizeof(float) * nl * NT * tws, c->stream));  // l' padding stays zero
   JCK(cudaMemsetAsync(c->tc_err, 0, sizeof(int), c->stream));
-  pack_lambda_kernel<<<(unsigned)pa.size(), tcl::kThreads, 0, c->stream>>>(c->lam, dpa, c->la_off, R, lmax, 0, c->LA);
+  pack_lambda_kernel<tcl::kKA><<<(unsigned)pa.size(), tcl::kThreads, 0, c->stream>>>(c->lam, dpa, c->la_off, R, lmax,
+                                                                                   0, c->LA);
   JCK(cudaGetLastError());
-  pack_lambda_kernel<<<(unsigned)ps.size(), tcl::kThreads, 0, c->stream>>>(c->lam, dps, c->ls_off, R, lmax, 1, c->LS);
+  pack_lambda_kernel<tcl::kKS><<<(unsigned)ps.size(), tcl::kThreads, 0, c->stream>>>(c->lam, dps, c->ls_off, R, lmax,
+                                                                                   1, c->LS);
   JCK(cudaGetLastError());
-  JCK(cudaFuncSetAttribute(tc_legendre_analysis_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcl::kSmem));
-  JCK(cudaFuncSetAttribute(tc_legendre_synthesis_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcl::kSmem));
+  JCK(cudaFuncSetAttribute(tc_legendre_analysis_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcl::kSmemA));
+  JCK(cudaFuncSetAttribute(tc_legendre_synthesis_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcl::kSmemS));
   JCK(cudaStreamSynchronize(c->stream));
   cudaFree(dpa);
   cudaFree(dps);
@@ -1534,13 +1554,13 @@ int sht_analysis(joint_ctx *c, const float *dmaps, int nch, const float *sig2, b
   {
     KSpan k(c, 1);  // the pack's own span (class 4) nests inside: class 1 = pack + GEMM
     if (tc) {
-      const int nkq = (c->R + tcl::kK - 1) / tcl::kK;
+      const int nkq = (c->R + tcl::kKA - 1) / tcl::kKA;
       {
         KSpan kp(c, 4);
         pack_eo_kernel<<<2 * (c->lmax + 1) * (c->N2 / tcl::kRows) * nkq, tcl::kThreads, 0, c->stream>>>(
             c->E, c->O, c->R, c->N2, c->EOp);
       }
-      tc_legendre_analysis_kernel<<<c->ntasks_ta, tcl::kThreads, tcl::kSmem, c->stream>>>(
+      tc_legendre_analysis_kernel<<<c->ntasks_ta, tcl::kThreads, tcl::kSmemA, c->stream>>>(
           c->LA, c->la_off, c->EOp, c->almp, c->alm_off, c->tasks_ta, c->R, c->lmax, c->N2 / tcl::kRows, w, sig2,
           c->tc_err);
     } else {
@@ -1558,7 +1578,7 @@ int sht_synthesis(joint_ctx *c, float *dmaps, int nch, bool tc)
   {
     KSpan k(c, 2);
     if (tc)
-      tc_legendre_synthesis_kernel<<<c->ntasks_ts, tcl::kThreads, tcl::kSmem, c->stream>>>(
+      tc_legendre_synthesis_kernel<<<c->ntasks_ts, tcl::kThreads, tcl::kSmemS, c->stream>>>(
           c->LS, c->ls_off, c->almp, c->alm_off, c->tasks_ts, c->R, c->lmax, c->N2, c->E, c->O, c->tc_err);
     else
       legendre_synthesis_kernel<<<c->ntasks_s, kThreads, 0, c->stream>>>(c->lam, c->alm, c->E, c->O, c->tasks_s,
