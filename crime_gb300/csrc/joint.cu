@@ -731,10 +731,11 @@ __global__ __launch_bounds__(kThreads, 2) void legendre_synthesis_kernel(const f
 // error flag the host reads.
 // ---------------------------------------------------------------------------
 namespace tcl {
-// operand tiles: 128 rows x KK elements of K, hi then lo; the analysis operands
-// (lambda by l' rows, E/O) use KK = 16, the synthesis operands (lambda by ring
-// rows, the packed a_lm) KK = 32
-constexpr int kRows = 128, kKA = 16, kKS = 32;
+// operand tiles: 128 rows x KK elements of K, hi then lo; KK for the analysis
+// operands (lambda by l' rows, E/O) and for the synthesis operands (lambda by ring
+// rows, the packed a_lm).  Both 16: 32 KB stages, two CTAs per SM (32-element
+// tiles with one CTA per SM measured slower in both directions)
+constexpr int kRows = 128, kKA = 16, kKS = 16;
 template <int KK>
 struct Geo {
   static constexpr uint32_t kHalf = kRows * KK * 4;  // the hi or the lo tile
@@ -742,8 +743,7 @@ struct Geo {
   static constexpr uint32_t kStage = 2 * kTile;      // A and B of one K step
   static constexpr uint32_t kSBO = 8 * KK * 4;       // stride of the 8-row core-matrix groups
 };
-// stages in flight: the analysis (256 TMEM columns) runs two CTAs per SM with three
-// 32 KB stages each, the synthesis (all 512 columns) one CTA with three 64 KB stages
+// stages in flight per CTA (two CTAs of 256 TMEM columns per SM)
 constexpr int kStagesA = 3, kStagesS = 3;
 constexpr size_t kSmemA = kStagesA * Geo<kKA>::kStage, kSmemS = kStagesS * Geo<kKS>::kStage;
 constexpr uint32_t kLBO = 128;  // K-adjacent core matrices
@@ -841,7 +841,7 @@ __device__ __forceinline__ void mma3(uint32_t acc0, uint32_t acc1, uint32_t a, u
     const uint64_t bl = tc::smem_desc(b + half + 256 * kk, tcl::kLBO, sbo);
     const uint32_t acc = (first && kk == 0) ? 0u : 1u;
     tc::mma_tf32(acc0, ah, bh, idesc, acc);
-    tc::mma_tf32(acc1, ah, bl, idesc, acc);
+    tc::mma_tf32(acc1, ah, bl, idesc, acc1 == acc0 ? 1u : acc);  // one accumulator: add to hi*hi
     tc::mma_tf32(acc1, al, bh, idesc, 1u);
   }
 }
@@ -991,8 +991,10 @@ __global__ void __launch_bounds__(tcl::kThreads, 2)
 }
 
 // synthesis, one CTA per (m, 128 ring pairs, column tile ct): G_e and G_o over the
-// packed a_lm of both parities; north = G_e + G_o, south = G_e - G_o, FP32 [m][q][col]
-__global__ void __launch_bounds__(tcl::kThreads, 1)
+// packed a_lm of both parities, each in one TMEM accumulator (hi*hi and the hi*lo,
+// lo*hi corrections together: 256 columns, two CTAs per SM); north = G_e + G_o,
+// south = G_e - G_o, FP32 [m][q][col]
+__global__ void __launch_bounds__(tcl::kThreads, 2)
     tc_legendre_synthesis_kernel(const float *__restrict__ LS, const long long *__restrict__ ls_off,
                                  const float *__restrict__ almp, const long long *__restrict__ alm_off,
                                  const int4 *__restrict__ tasks, int R, int lmax, int N2, float *__restrict__ Gn,
@@ -1012,7 +1014,7 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
   if (tid == 0) skip = *(volatile int *)err;
   __syncthreads();
   if (skip) return;
-  if (warp == 0) tc::tmem_alloc(&tslot, 512);
+  if (warp == 0) tc::tmem_alloc(&tslot, 256);
   if (tid == 0) {
     for (int i = 0; i < tcl::kStagesS; i++) {
       tc::mbar_init(&full[i], 1);
@@ -1038,8 +1040,8 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
       },
       [&](int kt, uint32_t &a0, uint32_t &a1, bool &first) {
         const int p = kt >= nke;
-        a0 = tm + 256 * p;
-        a1 = a0 + 128;
+        a0 = tm + 128 * p;  // hi*hi and the corrections in one accumulator per parity
+        a1 = a0;
         first = kt == 0 || kt == nke;
       },
       &fail);
@@ -1049,11 +1051,9 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
     float *gn = Gn + ((long long)m * R + q) * N2 + ct * tcl::kRows, *gs = Gs + ((long long)m * R + q) * N2 + ct * tcl::kRows;
 #pragma unroll 1
     for (int cb = 0; cb < 128; cb += 32) {
-      float e0[32], e1[32], o0[32], o1[32];
+      float e0[32], o0[32];
       tc::tmem_ld32(trow + cb, e0);
-      tc::tmem_ld32(trow + 128 + cb, e1);
-      tc::tmem_ld32(trow + 256 + cb, o0);
-      tc::tmem_ld32(trow + 384 + cb, o1);
+      tc::tmem_ld32(trow + 128 + cb, o0);
       if (q < R) {
 #pragma unroll
         for (int j = 0; j < 32; j += 4) {
@@ -1061,8 +1061,8 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
           float ev[4], ov[4];
 #pragma unroll
           for (int i = 0; i < 4; i++) {
-            ev[i] = e0[j + i] + e1[j + i];
-            ov[i] = nko ? o0[j + i] + o1[j + i] : 0.f;
+            ev[i] = e0[j + i];
+            ov[i] = nko ? o0[j + i] : 0.f;
           }
           vn = make_float4(ev[0] + ov[0], ev[1] + ov[1], ev[2] + ov[2], ev[3] + ov[3]);
           vs = make_float4(ev[0] - ov[0], ev[1] - ov[1], ev[2] - ov[2], ev[3] - ov[3]);
@@ -1076,7 +1076,7 @@ __global__ void __launch_bounds__(tcl::kThreads, 1)
   }
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tm, 512);
+  if (warp == 0) tc::tmem_dealloc(tm, 256);
 }
 
 // internal a_lm [m][parity][l'][2c] <-> HEALPix order [c][l + m lmax - m(m-1)/2] (complex)
