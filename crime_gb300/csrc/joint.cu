@@ -338,29 +338,6 @@ __device__ __forceinline__ void fold_pair(const float *__restrict__ Gn, const fl
   }
 }
 
-// The Hermitian-packed synthesis input of frequency k of pair q, channel c:
-// H_k = Q_k / 2 and H_{n-k} = conj Q_k / 2 (0 < k < n/2), H_0 = Re Q_0,
-// H_{n/2} = Re Q_{n/2}; returns H_north,k + i H_south,k (south zero on the equator)
-__device__ __forceinline__ float2 packed_value(const float *__restrict__ Gn, const float *__restrict__ Gs,
-                                              const RingPair &rp, const float2 *__restrict__ phtab, int q, bool eq,
-                                              int k, int lmax, int R, int N2, int c)
-{
-  const int n = rp.nph, half = n / 2, kk = k <= half ? k : n - k;
-  const long long mstride = (long long)R * N2, off = (long long)q * N2 + 2 * c;
-  const float2 ph = rp.shifted ? __ldg(phtab + rp.first_n + kk) : make_float2(1.f, 0.f);
-  float2 hn, hs;
-  fold_pair(Gn + off, Gs + off, mstride, kk, n, lmax, rp.shifted, ph, hn, hs);
-  if (eq) hs = make_float2(0.f, 0.f);
-  if (k == 0 || k == half) {
-    hn.y = 0.f;
-    hs.y = 0.f;
-  } else {
-    hn = make_float2(0.5f * hn.x, 0.5f * (k < half ? hn.y : -hn.y));
-    hs = make_float2(0.5f * hs.x, 0.5f * (k < half ? hs.y : -hs.y));
-  }
-  return make_float2(hn.x - hs.y, hn.y + hs.x);
-}
-
 // E and O of pair q for m = 0 .. lmax from the DFTs Z of z_j = north_j + i south_j
 // of S channels (z[b * PL + spad(k)], k < n): D_north,k = (Z_k + conj Z_{n-k}) / 2,
 // D_south,k = (Z_k - conj Z_{n-k}) / 2i, F_m = e^{-i m phi0} D_{m mod n} with
@@ -494,15 +471,32 @@ __global__ __launch_bounds__(kRingThreads, 2) void ring_synthesis_kernel(
   const bool blue = rp.bm > 0, eq = (q == R - 1);
   const SeqLayout sl = seq_layout(blue ? rp.bm : n, S);
   const float2 *ch = chirps + rp.tw_off, *Bt = btab + rp.b_off;
-  {  // one item per (k, channel), channels fastest (S = 2^lS divides the block)
-    const int b = threadIdx.x & (S - 1), c = c0 + b;
-    for (int k = threadIdx.x >> tk.w; k < sl.n; k += blockDim.x >> tk.w) {
-      float2 h = make_float2(0.f, 0.f);
-      if (k < n && c < nch) {
-        h = packed_value(Gn, Gs, rp, phtab, q, eq, k, lmax, R, N2, c);
-        if (blue) h = cmul(make_float2(h.x, -h.y), __ldg(ch + k));  // conjugated, times the chirp
+  {  // one item per (kk <= n/2, channel), channels fastest (S = 2^lS divides the block):
+     // the fold Q_kk serves both H_kk and H_{n-kk}; Bluestein's padding n .. M-1 is zero
+    const int b = threadIdx.x & (S - 1), c = c0 + b, kstep = blockDim.x >> tk.w, half = n / 2;
+    float2 *zb = z + b * sl.PL;
+    for (int k = n + (threadIdx.x >> tk.w); k < sl.n; k += kstep) zb[spad(k)] = make_float2(0.f, 0.f);
+    const long long mstride = (long long)R * N2, off = (long long)q * N2 + 2 * c;
+    for (int kk = threadIdx.x >> tk.w; kk <= half; kk += kstep) {
+      float2 hn = make_float2(0.f, 0.f), hs = hn;
+      if (c < nch) {
+        const float2 ph = rp.shifted ? __ldg(phtab + rp.first_n + kk) : make_float2(1.f, 0.f);
+        fold_pair(Gn + off, Gs + off, mstride, kk, n, lmax, rp.shifted, ph, hn, hs);
+        if (eq) hs = make_float2(0.f, 0.f);
       }
-      z[b * sl.PL + spad(k)] = h;
+      // H_k = Q_k / 2, H_{n-k} = conj Q_k / 2 (0 < k < n/2); H_0, H_{n/2} = Re Q; value north + i south
+      const bool edge = kk == 0 || kk == half;
+      const float f = edge ? 1.f : 0.5f;
+      const float2 a = make_float2(f * (hn.x - hs.y), f * (hn.y + hs.x));   // H at kk
+      const float2 a2 = make_float2(f * (hn.x + hs.y), f * (hs.x - hn.y));  // H at n - kk
+      float2 v = edge ? make_float2(hn.x, hs.x) : a;
+      if (blue) v = cmul(make_float2(v.x, -v.y), __ldg(ch + kk));  // conjugated, times the chirp
+      zb[spad(kk)] = v;
+      if (!edge) {
+        float2 v2 = a2;
+        if (blue) v2 = cmul(make_float2(v2.x, -v2.y), __ldg(ch + (n - kk)));
+        zb[spad(n - kk)] = v2;
+      }
     }
   }
   __syncthreads();
@@ -832,8 +826,8 @@ template <int KK>
 __device__ __forceinline__ void mma3(uint32_t acc0, uint32_t acc1, uint32_t a, uint32_t b, bool first)
 {
   constexpr uint32_t idesc = tc::idesc_tf32_f32(128, 128);
-#pragma unroll
   constexpr uint32_t sbo = tcl::Geo<KK>::kSBO, half = tcl::Geo<KK>::kHalf;
+#pragma unroll
   for (int kk = 0; kk < KK / 8; kk++) {
     const uint64_t ah = tc::smem_desc(a + 256 * kk, tcl::kLBO, sbo);
     const uint64_t al = tc::smem_desc(a + half + 256 * kk, tcl::kLBO, sbo);
