@@ -807,9 +807,11 @@ __global__ void __launch_bounds__(tcl::kThreads) pack_lambda_kernel(const float 
 
 // E and O packed by channel columns (rows = 128 columns of column tile ct, K = ring
 // pairs); one CTA per (m, parity, column tile, K tile), tile index
-// ((2 m + parity) NT + ct) nkq + kt
+// ((2 m + parity) NT + ct) nkq + kt.  Rows of columns beyond the batch (n2 = 2 x
+// its channels) are left as they are: each MMA output column depends on its own B
+// row only, and those outputs are never read.
 __global__ void __launch_bounds__(tcl::kThreads) pack_eo_kernel(const float *__restrict__ E,
-                                                                const float *__restrict__ O, int R, int N2,
+                                                                const float *__restrict__ O, int R, int N2, int n2,
                                                                 float *__restrict__ out)
 {
   constexpr int KK = tcl::kKA;
@@ -817,6 +819,7 @@ __global__ void __launch_bounds__(tcl::kThreads) pack_eo_kernel(const float *__r
   const int kt = blockIdx.x % nkq, rest = blockIdx.x / nkq, ct = rest % NT, mp = rest / NT, m = mp >> 1, p = mp & 1;
   const float *src = (p ? O : E) + (long long)m * R * N2 + ct * tcl::kRows;
   const int q0 = kt * KK;
+  if (ct * tcl::kRows + (int)threadIdx.x >= n2) return;  // this thread's row: a column beyond the batch
   float *tile = out + (long long)blockIdx.x * (tcl::Geo<KK>::kTile / 4);
   pack_tile<KK>(tile, [&](int r, int k) { return q0 + k < R ? src[(long long)(q0 + k) * N2 + r] : 0.f; });
 }
@@ -1297,6 +1300,7 @@ int ensure_tc_tables(joint_ctx *c)
   JCK(cudaMemcpyAsync(dpa, pa.data(), sizeof(int4) * pa.size(), cudaMemcpyHostToDevice, c->stream));
   JCK(cudaMemcpyAsync(dps, ps.data(), sizeof(int4) * ps.size(), cudaMemcpyHostToDevice, c->stream));
   JCK(cudaMemsetAsync(c->almp, 0, sizeof(float) * nl * NT * tws, c->stream));  // l' padding stays zero
+  JCK(cudaMemsetAsync(c->EOp, 0, sizeof(float) * 2 * (lmax + 1) * NT * nkq * twa, c->stream));  // padded columns
   JCK(cudaMemsetAsync(c->tc_err, 0, sizeof(int), c->stream));
   pack_lambda_kernel<tcl::kKA><<<(unsigned)pa.size(), tcl::kThreads, 0, c->stream>>>(c->lam, dpa, c->la_off, R, lmax,
                                                                                    0, c->LA);
@@ -1552,7 +1556,7 @@ int sht_analysis(joint_ctx *c, const float *dmaps, int nch, const float *sig2, b
       {
         KSpan kp(c, 4);
         pack_eo_kernel<<<2 * (c->lmax + 1) * (c->N2 / tcl::kRows) * nkq, tcl::kThreads, 0, c->stream>>>(
-            c->E, c->O, c->R, c->N2, c->EOp);
+            c->E, c->O, c->R, c->N2, 2 * nch, c->EOp);
       }
       tc_legendre_analysis_kernel<<<c->ntasks_ta, tcl::kThreads, tcl::kSmemA, c->stream>>>(
           c->LA, c->la_off, c->EOp, c->almp, c->alm_off, c->tasks_ta, c->R, c->lmax, c->N2 / tcl::kRows, w, sig2,
