@@ -467,7 +467,7 @@ def bench_joint(args):
                 "traffic": packed,
                 "traffic_source": "bytes of the packed operands per launch (hi and lo TF32 tiles of the Legendre "
                                   "table read once and of E/O for every 64-channel column tile, padded to "
-                                  "128 x 32 tiles, plus the packed a_lm written)",
+                                  "128 x 16 tiles, plus the packed a_lm written)",
                 "batch_channels": batch,
                 "traffic_gbs": round(packed / (ms_tc / 1e3) / 1e9, 1),
                 "traffic_frac": round(packed / (ms_tc / 1e3) / 1e9 / peak_hbm, 3),
