@@ -505,8 +505,8 @@ def bench_joint(args):
         "e2e": {"value": whole_job_rate(units, args.steps, ws, e2e_ms), "unit": "pixels/s",
                 "h2d_bytes_per_step": int(4 * units * len(comp)), "d2h_bytes_per_step": int(4 * units)},
         # per step: one sum of the device components, per batch the ring analysis and synthesis and
-        # the two Legendre kernels (+ the E/O pack on the tensor-core path), noise, mask
-        "gpu_launches": args.steps * (1 + (5 if j.uses_tensor_cores else 4) * chunks + 2),
+        # the two Legendre kernels (+ the E/O pack on the tensor-core path), noise and mask in one pass
+        "gpu_launches": args.steps * (1 + (5 if j.uses_tensor_cores else 4) * chunks + 1),
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:

@@ -193,18 +193,32 @@ __device__ __forceinline__ float noise_of(uint32_t w1, uint32_t w2, float s2)
   const float u1 = (float)(w1 >> 8) * (1.f / 16777216.f), u2 = (float)(w2 >> 8) * (1.f / 16777216.f);
   return sqrtf(-s2 * log1pf(-u2)) * cospif(2.f * u1);
 }
+// MASK: the mask applied in the same pass (noise, then mask, as the reference's
+// stages: masked pixels end at 0 whatever their noise; the draws are counter-based,
+// so skipping those of masked pixels changes no other pixel)
+template <bool MASK>
 __global__ void noise_philox_kernel(float *__restrict__ maps, const float *__restrict__ s2, long long npix,
-                                    uint32_t seed)
+                                    uint32_t seed, const int *__restrict__ mask)
 {
   const long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;  // pixel pair
   if (j >= npix / 2) return;
   const int c = blockIdx.y;
+  float2 *m = reinterpret_cast<float2 *>(maps + (long long)c * npix) + j;
+  int2 mk = make_int2(1, 1);
+  if (MASK) {
+    mk = reinterpret_cast<const int2 *>(mask)[j];
+    if (!mk.x && !mk.y) {
+      *m = make_float2(0.f, 0.f);
+      return;
+    }
+  }
   const uint4 r = philox4x32_10(make_uint4((uint32_t)j, (uint32_t)(j >> 32), (uint32_t)c, 0u), make_uint2(seed, 0x4A4F494Eu));
   const float sc = s2[c];
-  float2 *m = reinterpret_cast<float2 *>(maps + (long long)c * npix) + j;
   float2 v = *m;
   v.x = __fadd_rn(v.x, noise_of(r.x, r.y, sc));
   v.y = __fadd_rn(v.y, noise_of(r.z, r.w, sc));
+  if (!mk.x) v.x = 0.f;
+  if (!mk.y) v.y = 0.f;
   *m = v;
 }
 
@@ -1868,8 +1882,8 @@ extern "C" int joint_gpu_add_noise(joint_ctx *c)
   }
   const long long npix = c->npix;
   if (c->p.rng == JOINT_RNG_PHILOX) {
-    noise_philox_kernel<<<dim3((unsigned)((npix / 2 + kThreads - 1) / kThreads), c->p.n_nu), kThreads, 0,
-                          c->stream>>>(c->maps, c->s2, npix, c->p.seed);
+    noise_philox_kernel<false><<<dim3((unsigned)((npix / 2 + kThreads - 1) / kThreads), c->p.n_nu), kThreads, 0,
+                                 c->stream>>>(c->maps, c->s2, npix, c->p.seed, nullptr);
     JCK(cudaGetLastError());
     return GETHI_OK;
   }
@@ -1961,9 +1975,18 @@ extern "C" int joint_gpu_run(joint_ctx *c, float *maps_out)
   record(c, 1);
   if (c->p.dish_diameter > 0 && (rc = joint_gpu_apply_beam(c))) return rc;
   record(c, 2);
-  if (c->p.tsys > 0 && (rc = joint_gpu_add_noise(c))) return rc;
-  record(c, 3);
-  if ((rc = joint_gpu_apply_mask(c))) return rc;
+  const bool fuse = c->p.tsys > 0 && c->p.rng == JOINT_RNG_PHILOX && c->dmask;
+  if (fuse) {  // noise and mask in one pass (its time is the noise stage's; the mask stage reads 0)
+    if ((rc = need_maps(c))) return rc;
+    noise_philox_kernel<true><<<dim3((unsigned)((c->npix / 2 + kThreads - 1) / kThreads), c->p.n_nu), kThreads, 0,
+                                c->stream>>>(c->maps, c->s2, c->npix, c->p.seed, c->dmask);
+    JCK(cudaGetLastError());
+    record(c, 3);
+  } else {
+    if (c->p.tsys > 0 && (rc = joint_gpu_add_noise(c))) return rc;
+    record(c, 3);
+    if ((rc = joint_gpu_apply_mask(c))) return rc;
+  }
   record(c, 4);
   if (maps_out) {
     if ((rc = joint_gpu_get_maps(c, maps_out))) return rc;

@@ -98,7 +98,8 @@ int joint_gpu_alm2map(joint_ctx *c, const float *alms, int n_maps, float *maps);
 
 /* 1 when the context's Legendre sums run on the tensor cores (known after the first transform) */
 int joint_gpu_uses_tensor_cores(const joint_ctx *c);
-/* device time of the last joint_gpu_run per stage (ms): merge, beam, noise, mask */
+/* device time of the last joint_gpu_run per stage (ms): merge, beam, noise, mask (with device noise
+ * and a mask the two run as one pass, timed as noise) */
 int joint_gpu_stage_times(const joint_ctx *c, float *ms4);
 /* Per-kernel-class device times of the beam, accumulated while profiling is on
  * (events around each class; off by default): ring analysis (FFT + Bluestein),

@@ -140,6 +140,29 @@ def test_philox_noise_statistics(jt):
     assert not np.array_equal(jt.JoinT(nside, nu0, nuf, **dict(kw, seed=43)).run(), out)
 
 
+def test_run_fuses_noise_and_mask_exactly(jt):
+    """run() applies the Philox noise and the mask in one pass; the maps equal those of
+    the stages called one by one (merge, add_noise, apply_mask), bit for bit"""
+    nside = 64
+    rng = np.random.default_rng(7)
+    nu0 = np.array([700.0, 800.0, 900.0])
+    nuf = nu0 + 2.0
+    npix = 12 * nside * nside
+    mask = (rng.random(npix) > 0.3).astype(np.int32)
+    maps = rng.standard_normal((3, npix)).astype(np.float32)
+    kw = dict(tsys=20000.0, time_tot=100.0, n_dish=10, seed=9, mask=mask)
+    j = jt.JoinT(nside, nu0, nuf, **kw)
+    j.add_maps(maps, nside)
+    fused = j.run()
+    j2 = jt.JoinT(nside, nu0, nuf, **kw)
+    j2.add_maps(maps, nside)
+    j2.merge_maps()
+    j2.add_noise()
+    j2.apply_mask()
+    np.testing.assert_array_equal(j2.maps(), fused)
+    assert np.all(fused[:, mask == 0] == 0) and np.all(fused[:, mask == 1] != maps[:, mask == 1])
+
+
 def test_gethi_maps_handed_over_on_the_device(jt):
     import crime_gb300 as cg
     p = cg.make_params(n_grid=32, n_side=16, pk_filename="EH", frequencies_filename="", nu_min=700.0, nu_max=800.0,
