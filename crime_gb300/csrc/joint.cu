@@ -840,9 +840,8 @@ __global__ void __launch_bounds__(tcl::kThreads) pack_eo_kernel(const float *__r
 
 // the three MMAs of one K step (KK / 8 instructions of K = 8 each per tile)
 template <int KK>
-__device__ __forceinline__ void mma3(uint32_t acc0, uint32_t acc1, uint32_t a, uint32_t b, bool first)
+__device__ __forceinline__ void mma3(uint32_t acc0, uint32_t acc1, uint32_t a, uint32_t b, bool first, uint32_t idesc)
 {
-  constexpr uint32_t idesc = tc::idesc_tf32_f32(128, 128);
   constexpr uint32_t sbo = tcl::Geo<KK>::kSBO, half = tcl::Geo<KK>::kHalf;
 #pragma unroll
   for (int kk = 0; kk < KK / 8; kk++) {
@@ -860,23 +859,28 @@ __device__ __forceinline__ void mma3(uint32_t acc0, uint32_t acc1, uint32_t a, u
 // The K loop shared by both transforms: tiles kt = 0 .. nk-1, A and B of tile kt
 // (Geo<KK>::kTile bytes each, contiguous in global memory) at srcA(kt), srcB(kt);
 // chain(kt) selects the accumulator pair and first(kt) whether the tile starts it;
-// S stages.  One thread drives it: each stage is filled by two bulk copies
+// S stages.  Only the first nb rows of B (a multiple of 16: the batch's columns
+// in this column tile) are copied and multiplied (MMA N = nb).  One thread drives it: each stage is filled by two bulk copies
 // completing on full[s] and released by the commit of its MMAs to empty[s]; the
 // stage of tile kt - 1 is refilled once its MMAs are done, while those of tile kt
 // are queued.  Every wait is bounded; on an expired wait the copies and MMAs in
 // flight are waited for (bounded again) and false is returned.
 template <int S, int KK, class SrcA, class SrcB, class Chain>
-__device__ bool tc_k_loop(unsigned char *sm, uint64_t *full, uint64_t *empty, int nk, SrcA srcA, SrcB srcB,
+__device__ bool tc_k_loop(unsigned char *sm, uint64_t *full, uint64_t *empty, int nk, int nb, SrcA srcA, SrcB srcB,
                           Chain chain, int *fail)
 {
   using G = tcl::Geo<KK>;
+  const uint32_t bpart = (uint32_t)(nb / 8) * G::kSBO;  // rows 0 .. nb-1 of one half of a B tile
+  const uint32_t idesc = tc::idesc_tf32_f32(128, nb);
   if (threadIdx.x == 0) {
     auto load = [&](int kt) {
       const int s = kt % S;
       unsigned char *dst = sm + s * G::kStage;
-      tc::mbar_arrive_expect_tx(&full[s], G::kStage);
+      const unsigned char *b = srcB(kt);
+      tc::mbar_arrive_expect_tx(&full[s], G::kTile + 2 * bpart);
       tc::bulk_g2s(dst, srcA(kt), G::kTile, &full[s]);
-      tc::bulk_g2s(dst + G::kTile, srcB(kt), G::kTile, &full[s]);
+      tc::bulk_g2s(dst + G::kTile, b, bpart, &full[s]);
+      tc::bulk_g2s(dst + G::kTile + G::kHalf, b + G::kHalf, bpart, &full[s]);
     };
     int issued = 0, done = 0;  // tiles whose copies were issued / consumed by MMAs
     bool ok = true;
@@ -892,7 +896,7 @@ __device__ bool tc_k_loop(unsigned char *sm, uint64_t *full, uint64_t *empty, in
       uint32_t acc0, acc1;
       bool first;
       chain(kt, acc0, acc1, first);
-      mma3<KK>(acc0, acc1, a, b, first);
+      mma3<KK>(acc0, acc1, a, b, first, idesc);
       tc::mma_commit(&empty[s]);
       done = kt + 1;
       if (kt >= 1 && issued < nk) {  // refill the stage of tile kt - 1 with tile kt - 1 + S
@@ -926,7 +930,7 @@ __global__ void __launch_bounds__(tcl::kThreads, 2)
     tc_legendre_analysis_kernel(const float *__restrict__ LA, const long long *__restrict__ la_off,
                                 const float *__restrict__ EOp, float *__restrict__ almp,
                                 const long long *__restrict__ alm_off, const int4 *__restrict__ tasks, int R, int lmax,
-                                int NT, float w, const float *__restrict__ sig2, int *err)
+                                int NT, int n2, float w, const float *__restrict__ sig2, int *err)
 {
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ uint64_t full[tcl::kStagesA], empty[tcl::kStagesA];
@@ -942,7 +946,8 @@ __global__ void __launch_bounds__(tcl::kThreads, 2)
   __shared__ int skip;  // an earlier CTA's MMA wait expired: no new work (decided once for the CTA)
   if (tid == 0) skip = *(volatile int *)err;
   __syncthreads();
-  if (skip) return;
+  const int neff = min(tcl::kRows, ((n2 - ct * tcl::kRows) + 15) & ~15);  // MMA N: this tile's batch columns
+  if (skip || neff <= 0) return;
   if (warp == 0) tc::tmem_alloc(&tslot, 256);
   if (tid == 0) {
     for (int i = 0; i < tcl::kStagesA; i++) {
@@ -959,7 +964,7 @@ __global__ void __launch_bounds__(tcl::kThreads, 2)
   const unsigned char *B0 =
       reinterpret_cast<const unsigned char *>(EOp) + ((long long)(2 * m + p) * NT + ct) * nkq * GA::kTile;
   const bool ok = tc_k_loop<tcl::kStagesA, tcl::kKA>(
-      sm, full, empty, nkq, [&](int kt) { return A0 + (long long)kt * GA::kTile; },
+      sm, full, empty, nkq, neff, [&](int kt) { return A0 + (long long)kt * GA::kTile; },
       [&](int kt) { return B0 + (long long)kt * GA::kTile; },
       [&](int kt, uint32_t &a0, uint32_t &a1, bool &first) {
         a0 = tm;
@@ -975,7 +980,7 @@ __global__ void __launch_bounds__(tcl::kThreads, 2)
     float *tile = almp + ((alm_off[2 * m + p] + lp / tcl::kKS) * NT + ct) * (GS::kTile / 4);
     const uint32_t trow = tm + ((uint32_t)(32 * warp) << 16);
 #pragma unroll 1
-    for (int cb = 0; cb < 128; cb += 32) {
+    for (int cb = 0; cb < neff; cb += 32) {
       float v0[32], v1[32];
       tc::tmem_ld32(trow + cb, v0);
       tc::tmem_ld32(trow + 128 + cb, v1);
@@ -1008,7 +1013,7 @@ __global__ void __launch_bounds__(tcl::kThreads, 2)
 __global__ void __launch_bounds__(tcl::kThreads, 2)
     tc_legendre_synthesis_kernel(const float *__restrict__ LS, const long long *__restrict__ ls_off,
                                  const float *__restrict__ almp, const long long *__restrict__ alm_off,
-                                 const int4 *__restrict__ tasks, int R, int lmax, int N2, float *__restrict__ Gn,
+                                 const int4 *__restrict__ tasks, int R, int lmax, int N2, int n2, float *__restrict__ Gn,
                                  float *__restrict__ Gs, int *err)
 {
   extern __shared__ __align__(1024) unsigned char sm[];
@@ -1024,7 +1029,8 @@ __global__ void __launch_bounds__(tcl::kThreads, 2)
   __shared__ int skip;  // an earlier CTA's MMA wait expired: no new work (decided once for the CTA)
   if (tid == 0) skip = *(volatile int *)err;
   __syncthreads();
-  if (skip) return;
+  const int neff = min(tcl::kRows, ((n2 - ct * tcl::kRows) + 15) & ~15);  // MMA N: this tile's batch columns
+  if (skip || neff <= 0) return;
   if (warp == 0) tc::tmem_alloc(&tslot, 256);
   if (tid == 0) {
     for (int i = 0; i < tcl::kStagesS; i++) {
@@ -1040,7 +1046,7 @@ __global__ void __launch_bounds__(tcl::kThreads, 2)
   const unsigned char *LSb = reinterpret_cast<const unsigned char *>(LS);
   const unsigned char *Ab = reinterpret_cast<const unsigned char *>(almp);
   const bool ok = tc_k_loop<tcl::kStagesS, tcl::kKS>(
-      sm, full, empty, nke + nko,
+      sm, full, empty, nke + nko, neff,
       [&](int kt) {
         const int p = kt >= nke, k = p ? kt - nke : kt, nk = p ? nko : nke;
         return LSb + (ls_off[2 * m + p] + (long long)qt * nk + k) * GS::kTile;
@@ -1061,7 +1067,7 @@ __global__ void __launch_bounds__(tcl::kThreads, 2)
     const uint32_t trow = tm + ((uint32_t)(32 * warp) << 16);
     float *gn = Gn + ((long long)m * R + q) * N2 + ct * tcl::kRows, *gs = Gs + ((long long)m * R + q) * N2 + ct * tcl::kRows;
 #pragma unroll 1
-    for (int cb = 0; cb < 128; cb += 32) {
+    for (int cb = 0; cb < neff; cb += 32) {
       float e0[32], o0[32];
       tc::tmem_ld32(trow + cb, e0);
       tc::tmem_ld32(trow + 128 + cb, o0);
@@ -1573,8 +1579,8 @@ int sht_analysis(joint_ctx *c, const float *dmaps, int nch, const float *sig2, b
             c->E, c->O, c->R, c->N2, 2 * nch, c->EOp);
       }
       tc_legendre_analysis_kernel<<<c->ntasks_ta, tcl::kThreads, tcl::kSmemA, c->stream>>>(
-          c->LA, c->la_off, c->EOp, c->almp, c->alm_off, c->tasks_ta, c->R, c->lmax, c->N2 / tcl::kRows, w, sig2,
-          c->tc_err);
+          c->LA, c->la_off, c->EOp, c->almp, c->alm_off, c->tasks_ta, c->R, c->lmax, c->N2 / tcl::kRows, 2 * nch, w,
+          sig2, c->tc_err);
     } else {
       legendre_analysis_kernel<<<c->ntasks_a, kThreads, 0, c->stream>>>(c->lam, c->E, c->O, c->alm, c->tasks_a,
                                                                         c->R, c->lmax, c->N2, w, sig2);
@@ -1591,7 +1597,7 @@ int sht_synthesis(joint_ctx *c, float *dmaps, int nch, bool tc)
     KSpan k(c, 2);
     if (tc)
       tc_legendre_synthesis_kernel<<<c->ntasks_ts, tcl::kThreads, tcl::kSmemS, c->stream>>>(
-          c->LS, c->ls_off, c->almp, c->alm_off, c->tasks_ts, c->R, c->lmax, c->N2, c->E, c->O, c->tc_err);
+          c->LS, c->ls_off, c->almp, c->alm_off, c->tasks_ts, c->R, c->lmax, c->N2, 2 * nch, c->E, c->O, c->tc_err);
     else
       legendre_synthesis_kernel<<<c->ntasks_s, kThreads, 0, c->stream>>>(c->lam, c->alm, c->E, c->O, c->tasks_s,
                                                                          c->R, c->lmax, c->N2);
