@@ -16,14 +16,16 @@
 //           batch; the same buffers then hold the synthesised north and south
 //           ring sums
 //   alm     per m, [parity][l'][2 c] float
-// A transform is, per batch of channels: ring DFTs (one CTA per ring pair and a
-// few channels: the 2 nside + 1 equatorial rings, 4 nside pixels each, by a
-// register-resident radix-16 Stockham FFT of north + i south; the polar rings,
-// 4 i pixels, by Bluestein's DFT over the same FFTs), the
-// Legendre sums as FP32 GEMMs per (m, parity) on the CUDA cores (the beam
-// factor exp(-l(l+1) sigma_c^2 / 2) and the quadrature weight 4 pi / npix
-// applied in the epilogue), the transposed GEMMs back, and the inverse ring
-// sums.
+//   LA, LS, EOp, almp: the same tables and sums packed for the tensor cores
+//           (128-row tiles of TF32 hi and lo parts), per 64-channel column tile
+// A transform is, per batch of channels: ring DFTs (one launch over a task list
+// of (ring pair, channels): the 2 nside + 1 equatorial rings, 4 nside pixels
+// each, by a register-resident radix-16 Stockham FFT of north + i south; the
+// polar rings, 4 i pixels, by Bluestein's DFT over the same FFTs), the Legendre
+// sums per (m, parity) as 3xTF32 tcgen05 GEMMs (nside <= 512) or FP32 GEMMs on
+// the CUDA cores (the beam factor exp(-l(l+1) sigma_c^2 / 2) and the quadrature
+// weight 4 pi / npix applied in the epilogue), the transposed GEMMs back, and
+// the inverse ring transforms.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -1165,7 +1167,7 @@ struct joint_ctx {
   // spherical harmonic transform
   RingPair *rings = nullptr;
   float2 *tw2 = nullptr;   // e^{2 pi i t/M} at [M + t] for every power of two M
-  float2 *btab = nullptr;  // polar rings: spectra of the conjugate Bluestein chirps (bit-reversed)
+  float2 *btab = nullptr;  // polar rings: spectra of the conjugate Bluestein chirps (natural order)
   float2 *chirps = nullptr;  // polar rings: the chirps e^{-i pi j^2/n}, at 2 i (i - 1) for n = 4 i
   float *lam = nullptr;
   int chunk = 0, N2 = 0;
@@ -1174,7 +1176,7 @@ struct joint_ctx {
   int4 *tasks_a = nullptr, *tasks_s = nullptr;
   int ntasks_a = 0, ntasks_s = 0;
   double *noise_h = nullptr, *noise_d = nullptr;  // mt_validation staging (pinned host, device)
-  // tensor-core Legendre sums: packed tables, offsets (in 32 KB tiles per (m, parity)), task lists
+  // tensor-core Legendre sums: packed tables, offsets (in operand tiles per (m, parity)), task lists
   bool use_tc = false;
   float *LA = nullptr, *LS = nullptr, *EOp = nullptr, *almp = nullptr;
   long long *la_off = nullptr, *ls_off = nullptr, *alm_off = nullptr;
