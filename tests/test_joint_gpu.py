@@ -88,8 +88,10 @@ def test_beam_matches_oracle(jt, nside, dish, precision):
     assert rel_l2(out, maps) > 0.05  # the beam did smooth
 
 
-@pytest.mark.parametrize("nside", [4, 16, 32])
+@pytest.mark.parametrize("nside", [4, 16, 32, 128])
 def test_map2alm_alm2map_match_oracle(jt, nside):
+    """against the oracle's FP64 transform; Nside 128 takes the compile-time ring-FFT
+    plans (512-point equatorial rings, 1024-point Bluestein convolutions)"""
     rng = np.random.default_rng(7 + nside)
     lmax = 3 * nside - 1
     maps = rng.standard_normal((2, 12 * nside * nside)).astype(np.float32)
