@@ -40,7 +40,9 @@ typedef struct {
   const int *mask;           /* fname_mask= as 0/1 per pixel [12 nside^2], or NULL (all 1); copied */
   int rng;                   /* JOINT_RNG_* */
   int omp_threads_for_noise; /* JOINT_RNG_MT_VALIDATION: OpenMP threads of the emulated reference run */
-  int sht_chunk;             /* channels per spherical-harmonic batch; 0: automatic */
+  int sht_chunk;             /* channels per spherical-harmonic batch; 0: automatic (every channel, up to
+                                256, on the tensor cores; 64 on the CUDA cores); the tensor cores need a
+                                multiple of 64 */
   int sht_precision;         /* Legendre sums: 0 = tensor cores (3xTF32) where their tables fit (nside <= 512),
                                 else FP32 CUDA cores; 1 = FP32 CUDA cores */
 } joint_params;
