@@ -452,12 +452,14 @@ def bench_joint(args):
     if j.uses_tensor_cores:
         # the analysis GEMM alone (class "legendre_analysis" includes the E/O pack)
         ms_tc = (kt["legendre_analysis"][0] - kt["legendre_pack"][0]) / kt["legendre_analysis"][1]
-        nkq, nt = -(-R // 32), batch // 64
+        nkq = -(-R // 32)
         tiles = sum(-(-((lmax - m) // 2 + 1 if p == 0 else (lmax - m + 1) // 2) // 128) * nkq
                     for m in range(lmax + 1) for p in (0, 1))
-        # lambda tiles read once (their column tiles share them through L2), the E/O tiles
-        # of every column tile read, the packed a_lm written
-        packed = 32768.0 * (tiles + 2 * (lmax + 1) * nkq * nt) + 8.0 * nalm * 128 * nt
+        # columns used per 64-channel column tile (the last one cut to a multiple of 16)
+        used = sum(min(128, -(-(N2 - 128 * ct) // 16) * 16) for ct in range(-(-N2 // 128)))
+        # lambda tiles read once (their column tiles share them through L2), the used rows
+        # of the E/O tiles read, the packed a_lm written
+        packed = 32768.0 * (tiles + 2 * (lmax + 1) * nkq * used / 128) + 8.0 * nalm * used
         with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
             bf16 = float(json.load(f)["bf16_tflops"])
         achieved = gemm_bytes / (ms_tc / 1e3) / 1e9
@@ -466,8 +468,8 @@ def bench_joint(args):
                 "algorithmic_bytes_per_launch": gemm_bytes, "avg_launch_ms": round(ms_tc, 3),
                 "traffic": packed,
                 "traffic_source": "bytes of the packed operands per launch (hi and lo TF32 tiles of the Legendre "
-                                  "table read once and of E/O for every 64-channel column tile, padded to "
-                                  "128 x 16 tiles, plus the packed a_lm written)",
+                                  "table read once and of the used E/O rows of every 64-channel column tile, "
+                                  "padded to 128 x 16 tiles, plus the packed a_lm written)",
                 "batch_channels": batch,
                 "traffic_gbs": round(packed / (ms_tc / 1e3) / 1e9, 1),
                 "traffic_frac": round(packed / (ms_tc / 1e3) / 1e9 / peak_hbm, 3),
