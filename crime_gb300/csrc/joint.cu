@@ -361,14 +361,34 @@ __device__ __forceinline__ void fold_pair(const float *__restrict__ Gn, const fl
 // (m, channel), channels fastest: consecutive threads store consecutive channels.
 // S = 2^lS divides the block; a thread keeps its channel and steps m, with
 // (j, k) = divmod(m, n) kept up to date without divisions.
+// E + i O contributions of one channel row (b) at folded frequency k: (E, O) of m
+__device__ __forceinline__ void eo_of(const float2 *z, int PL, int b, int k, int n, bool eq, bool cj, float2 ph,
+                                      float2 &e, float2 &o)
+{
+  const float2 zk = z[b * PL + spad(k)], zm = z[b * PL + spad(k ? n - k : 0)];
+  float2 dn = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+  float2 ds = eq ? make_float2(0.f, 0.f) : make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
+  if (cj) {
+    dn.y = -dn.y;
+    ds.y = -ds.y;
+  }
+  e = cmul(make_float2(dn.x + ds.x, dn.y + ds.y), ph);
+  o = cmul(make_float2(dn.x - ds.x, dn.y - ds.y), ph);
+}
+
 __device__ __forceinline__ void write_eo(const float2 *z, int PL, const RingPair &rp, const float2 *__restrict__ phtab,
                                          int q, bool eq, int lmax, int R, int N2, int nch, int c0, int lS,
                                          float *__restrict__ E, float *__restrict__ O)
 {
-  const int n = rp.nph, half = n / 2, b = threadIdx.x & ((1 << lS) - 1), c = c0 + b;
+  // items of two adjacent channels when the block holds two or more and the rows keep
+  // 16-byte alignment (N2 a multiple of 4; c0 and b even): one 16-byte store each to E, O
+  const bool pairs = lS > 0 && (N2 & 3) == 0;
+  const int lP = pairs ? lS - 1 : lS, w = pairs ? 2 : 1;
+  const int n = rp.nph, half = n / 2, b = (threadIdx.x & ((1 << lP) - 1)) * w, c = c0 + b;
   if (c >= nch) return;
-  const int mstep = blockDim.x >> lS, jstep = mstep / n, kstep = mstep - jstep * n;
-  int m = threadIdx.x >> lS, j = m / n, kj = m - j * n;
+  const bool pair = pairs && c + 1 < nch;
+  const int mstep = blockDim.x >> lP, jstep = mstep / n, kstep = mstep - jstep * n;
+  int m = threadIdx.x >> lP, j = m / n, kj = m - j * n;
   for (; m <= lmax; m += mstep, kj += kstep, j += jstep) {
     if (kj >= n) {
       kj -= n;
@@ -382,16 +402,18 @@ __device__ __forceinline__ void write_eo(const float2 *z, int PL, const RingPair
     }
     const bool cj = k > half;
     if (cj) k = n - k;
-    const float2 zk = z[b * PL + spad(k)], zm = z[b * PL + spad(k ? n - k : 0)];
-    float2 dn = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
-    float2 ds = eq ? make_float2(0.f, 0.f) : make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
-    if (cj) {
-      dn.y = -dn.y;
-      ds.y = -ds.y;
-    }
     const long long base = ((long long)m * R + q) * N2 + 2 * c;
-    *reinterpret_cast<float2 *>(E + base) = cmul(make_float2(dn.x + ds.x, dn.y + ds.y), ph);
-    *reinterpret_cast<float2 *>(O + base) = cmul(make_float2(dn.x - ds.x, dn.y - ds.y), ph);
+    float2 e0, o0;
+    eo_of(z, PL, b, k, n, eq, cj, ph, e0, o0);
+    if (pair) {
+      float2 e1, o1;
+      eo_of(z, PL, b + 1, k, n, eq, cj, ph, e1, o1);
+      *reinterpret_cast<float4 *>(E + base) = make_float4(e0.x, e0.y, e1.x, e1.y);
+      *reinterpret_cast<float4 *>(O + base) = make_float4(o0.x, o0.y, o1.x, o1.y);
+    } else {
+      *reinterpret_cast<float2 *>(E + base) = e0;
+      *reinterpret_cast<float2 *>(O + base) = o0;
+    }
   }
 }
 
