@@ -166,6 +166,24 @@ def test_run_fuses_noise_and_mask_exactly(jt):
     assert np.all(fused[:, mask == 0] == 0) and np.all(fused[:, mask == 1] != maps[:, mask == 1])
 
 
+def test_beam_independent_of_the_channel_batching(jt):
+    """the beam of 7 channels in batches of 3 (odd column counts: single-channel E/O
+    stores, blocks with channels beyond the batch) equals the one-batch beam bit for
+    bit on the FP32 path, where every output column depends on its own channel only"""
+    nside = 16
+    rng = np.random.default_rng(21)
+    nu0 = np.linspace(600.0, 900.0, 7)
+    maps = rng.standard_normal((7, 12 * nside * nside)).astype(np.float32)
+    outs = []
+    for chunk in (0, 3):
+        j = jt.JoinT(nside, nu0, nu0 + 4.0, dish_diameter=2.0, sht_precision="fp32", sht_chunk=chunk)
+        j.add_maps(maps, nside)
+        outs.append(j.run())
+        j.close()
+    np.testing.assert_array_equal(outs[0], outs[1])
+    assert rel_l2(outs[0], maps) > 0.05
+
+
 def test_run_with_device_components_equals_the_stages(jt):
     """run() with device components (summed in one pass at the merge) equals merge,
     apply_beam, add_noise and apply_mask called one by one, bit for bit, also on a
