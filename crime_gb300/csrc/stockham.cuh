@@ -20,7 +20,9 @@ namespace stockham {
 // radices are 16 but for one pass of 2^(log2 n mod 4): the first pass of the
 // forward plan, the last of the reversed plan.  Between passes the points go
 // through shared memory at index i + i/16 (one float2 of padding per 16 points),
-// which keeps the 8-byte accesses of every pass free of bank conflicts.
+// which keeps the 8-byte accesses of every pass free of bank conflicts.  The
+// twiddles come from tw2, which holds e^{+2 pi i x/L} at tw2[L + x] (x < L) for
+// every power of two L up to n; the inverse sign conjugates them.
 
 using gethi::cadd;
 using gethi::cmul;
