@@ -354,6 +354,62 @@ __device__ __forceinline__ void fold_pair(const float *__restrict__ Gn, const fl
   }
 }
 
+// fold_pair for two adjacent channels (16-byte loads: G 16-byte aligned at the pair)
+__device__ __forceinline__ void fold_pair2(const float *__restrict__ Gn, const float *__restrict__ Gs,
+                                           long long mstride, int k, int n, int lmax, bool shifted, float2 ph,
+                                           float2 (&qn)[2], float2 (&qs)[2])
+{
+  const float flip = shifted ? -1.f : 1.f;
+  float4 An = make_float4(0.f, 0.f, 0.f, 0.f), As = An, Bn = An, Bs = An;
+  float sg = k ? 2.f : 1.f;  // c_0 = 1
+  for (int m = k; m <= lmax; m += n) {
+    const float4 gn = *reinterpret_cast<const float4 *>(Gn + m * mstride);
+    const float4 gs = *reinterpret_cast<const float4 *>(Gs + m * mstride);
+    An.x += sg * gn.x; An.y += sg * gn.y; An.z += sg * gn.z; An.w += sg * gn.w;
+    As.x += sg * gs.x; As.y += sg * gs.y; As.z += sg * gs.z; As.w += sg * gs.w;
+    sg = (m ? sg : 2.f) * flip;
+  }
+  if (k != 0 && 2 * k != n) {
+    sg = 2.f;
+    for (int m = n - k; m <= lmax; m += n) {
+      const float4 gn = *reinterpret_cast<const float4 *>(Gn + m * mstride);
+      const float4 gs = *reinterpret_cast<const float4 *>(Gs + m * mstride);
+      Bn.x += sg * gn.x; Bn.y += sg * gn.y; Bn.z += sg * gn.z; Bn.w += sg * gn.w;
+      Bs.x += sg * gs.x; Bs.y += sg * gs.y; Bs.z += sg * gs.z; Bs.w += sg * gs.w;
+      sg *= flip;
+    }
+  }
+  if (shifted) {  // ph (A - conj B)
+    qn[0] = cmul(ph, make_float2(An.x - Bn.x, An.y + Bn.y));
+    qn[1] = cmul(ph, make_float2(An.z - Bn.z, An.w + Bn.w));
+    qs[0] = cmul(ph, make_float2(As.x - Bs.x, As.y + Bs.y));
+    qs[1] = cmul(ph, make_float2(As.z - Bs.z, As.w + Bs.w));
+  } else {        // A + conj B
+    qn[0] = make_float2(An.x + Bn.x, An.y - Bn.y);
+    qn[1] = make_float2(An.z + Bn.z, An.w - Bn.w);
+    qs[0] = make_float2(As.x + Bs.x, As.y - Bs.y);
+    qs[1] = make_float2(As.z + Bs.z, As.w - Bs.w);
+  }
+}
+
+// the Hermitian-packed values of frequencies kk and n - kk of one channel row from its
+// folded sums: H_k = Q_k / 2, H_{n-k} = conj Q_k / 2 (0 < k < n/2), H_0, H_{n/2} = Re Q;
+// value north + i south (Bluestein: conjugated, times the chirp)
+__device__ __forceinline__ void put_spectrum(float2 *zb, int kk, int n, float2 hn, float2 hs, bool blue,
+                                             const float2 *__restrict__ ch)
+{
+  const bool edge = kk == 0 || 2 * kk == n;
+  const float f = edge ? 1.f : 0.5f;
+  float2 v = edge ? make_float2(hn.x, hs.x) : make_float2(f * (hn.x - hs.y), f * (hn.y + hs.x));
+  if (blue) v = cmul(make_float2(v.x, -v.y), __ldg(ch + kk));
+  zb[spad(kk)] = v;
+  if (!edge) {
+    float2 v2 = make_float2(f * (hn.x + hs.y), f * (hs.x - hn.y));
+    if (blue) v2 = cmul(make_float2(v2.x, -v2.y), __ldg(ch + (n - kk)));
+    zb[spad(n - kk)] = v2;
+  }
+}
+
 // E and O of pair q for m = 0 .. lmax from the DFTs Z of z_j = north_j + i south_j
 // of S channels (z[b * PL + spad(k)], k < n): D_north,k = (Z_k + conj Z_{n-k}) / 2,
 // D_south,k = (Z_k - conj Z_{n-k}) / 2i, F_m = e^{-i m phi0} D_{m mod n} with
@@ -509,31 +565,36 @@ __global__ __launch_bounds__(kRingThreads, 2) void ring_synthesis_kernel(
   const bool blue = rp.bm > 0, eq = (q == R - 1);
   const SeqLayout sl = seq_layout(blue ? rp.bm : n, S);
   const float2 *ch = chirps + rp.tw_off, *Bt = btab + rp.b_off;
-  {  // one item per (kk <= n/2, channel), channels fastest (S = 2^lS divides the block):
-     // the fold Q_kk serves both H_kk and H_{n-kk}; Bluestein's padding n .. M-1 is zero
-    const int b = threadIdx.x & (S - 1), c = c0 + b, kstep = blockDim.x >> tk.w, half = n / 2;
+  {  // one item per (kk <= n/2, channel or pair of adjacent channels), channels fastest
+     // (S = 2^lS divides the block): the fold Q_kk serves both H_kk and H_{n-kk};
+     // Bluestein's padding n .. M-1 is zero.  Pairs (16-byte loads) where the rows keep
+     // 16-byte alignment (N2 a multiple of 4; c0 and b even)
+    const bool pairs = tk.w > 0 && (N2 & 3) == 0;
+    const int lP = pairs ? tk.w - 1 : tk.w, w = pairs ? 2 : 1;
+    const int b = (threadIdx.x & ((1 << lP) - 1)) * w, c = c0 + b, kstep = blockDim.x >> lP, half = n / 2;
     float2 *zb = z + b * sl.PL;
-    for (int k = n + (threadIdx.x >> tk.w); k < sl.n; k += kstep) zb[spad(k)] = make_float2(0.f, 0.f);
+    for (int k = n + (threadIdx.x >> lP); k < sl.n; k += kstep) {
+      zb[spad(k)] = make_float2(0.f, 0.f);
+      if (pairs) zb[sl.PL + spad(k)] = make_float2(0.f, 0.f);
+    }
     const long long mstride = (long long)R * N2, off = (long long)q * N2 + 2 * c;
-    for (int kk = threadIdx.x >> tk.w; kk <= half; kk += kstep) {
-      float2 hn = make_float2(0.f, 0.f), hs = hn;
-      if (c < nch) {
-        const float2 ph = rp.shifted ? __ldg(phtab + rp.first_n + kk) : make_float2(1.f, 0.f);
-        fold_pair(Gn + off, Gs + off, mstride, kk, n, lmax, rp.shifted, ph, hn, hs);
-        if (eq) hs = make_float2(0.f, 0.f);
-      }
-      // H_k = Q_k / 2, H_{n-k} = conj Q_k / 2 (0 < k < n/2); H_0, H_{n/2} = Re Q; value north + i south
-      const bool edge = kk == 0 || kk == half;
-      const float f = edge ? 1.f : 0.5f;
-      const float2 a = make_float2(f * (hn.x - hs.y), f * (hn.y + hs.x));   // H at kk
-      const float2 a2 = make_float2(f * (hn.x + hs.y), f * (hs.x - hn.y));  // H at n - kk
-      float2 v = edge ? make_float2(hn.x, hs.x) : a;
-      if (blue) v = cmul(make_float2(v.x, -v.y), __ldg(ch + kk));  // conjugated, times the chirp
-      zb[spad(kk)] = v;
-      if (!edge) {
-        float2 v2 = a2;
-        if (blue) v2 = cmul(make_float2(v2.x, -v2.y), __ldg(ch + (n - kk)));
-        zb[spad(n - kk)] = v2;
+    for (int kk = threadIdx.x >> lP; kk <= half; kk += kstep) {
+      const float2 ph = rp.shifted ? __ldg(phtab + rp.first_n + kk) : make_float2(1.f, 0.f);
+      if (pairs) {
+        float2 hn[2] = {}, hs[2] = {};
+        if (c < nch) {  // the second channel may lie beyond the batch (its spectrum is not used)
+          fold_pair2(Gn + off, Gs + off, mstride, kk, n, lmax, rp.shifted, ph, hn, hs);
+          if (eq) hs[0] = hs[1] = make_float2(0.f, 0.f);
+        }
+        put_spectrum(zb, kk, n, hn[0], hs[0], blue, ch);
+        put_spectrum(zb + sl.PL, kk, n, hn[1], hs[1], blue, ch);
+      } else {
+        float2 hn = make_float2(0.f, 0.f), hs = hn;
+        if (c < nch) {
+          fold_pair(Gn + off, Gs + off, mstride, kk, n, lmax, rp.shifted, ph, hn, hs);
+          if (eq) hs = make_float2(0.f, 0.f);
+        }
+        put_spectrum(zb, kk, n, hn, hs, blue, ch);
       }
     }
   }
