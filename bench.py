@@ -139,11 +139,14 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def algorithmic_bytes(cls, n, npix, n_nu):
-    """Minimum HBM bytes of one launch of a kernel class (FP32 data)."""
+def algorithmic_bytes(cls, n, npix, n_nu, zfields=3, gaussianised=True):
+    """Minimum HBM bytes of one launch of a kernel class (FP32 data; a mode is one
+    complex of the N^3/2-mode half spectrum, a cell one of N^3)."""
     n3 = float(n) ** 3
     return {
-        "zpass": 8 * n3,            # write the raw modes and the transformed column: 2 x 8 B/mode
+        # the drawing Z pass writes zfields transformed fields (delta; + phi; + i kz phi for the
+        # spectral velocity) at 8 B/mode each and reads P_G (4 B/mode) when the spectrum is Gaussianised
+        "zpass": 4 * zfields * n3 + (2 * n3 if gaussianised else 0),
         "zpass_raw": 8 * n3,        # read the raw modes, write the transformed column
         "ypass": 8 * n3,            # read + write 8 B/mode
         "xpass": 8 * n3,            # read 8 B/mode, write 4 B/cell
@@ -611,7 +614,9 @@ def bench_ours(args):
               key=lambda kv: kv[1][0])
     cls, (tot_ms, cnt) = dom
     per_launch_ms = tot_ms / cnt
-    abytes = algorithmic_bytes(cls, n, npix, n_nu)
+    zf = (3 if cfg.get("velocity_mode") == "spectral" else 2) if cfg["do_rsd"] else 1
+    gz = bool(cfg.get("gaussianise"))
+    abytes = algorithmic_bytes(cls, n, npix, n_nu, zf, gz)
     achieved = abytes / (per_launch_ms / 1e3) / 1e9
     traffic = None
     tf = os.path.join(REPO, "profiles", "traffic.json")
@@ -626,7 +631,7 @@ def bench_ours(args):
     kernels = {k: {"ms_per_step": round(v[0] / args.steps, 4), "launches_per_step": v[1] / args.steps}
                for k, v in ktimes.items() if v[1] > 0}
     for k in kernels:
-        b = algorithmic_bytes(k, n, npix, n_nu)
+        b = algorithmic_bytes(k, n, npix, n_nu, zf, gz)
         if b:
             kernels[k]["GBps"] = round(b / (ktimes[k][0] / ktimes[k][1] / 1e3) / 1e9, 1)
 

@@ -1,6 +1,6 @@
 """Build the GB300 GetHI library in-tree: crime_gb300/lib/libgethi_gpu.so (+ the
-GetHI_gpu and JoinT_gpu command-line drivers and the colpass_bench column-transform benchmark).  sm_103a only; translation units compile in
-parallel.  Usage: python -m crime_gb300.build [--force]"""
+GetHI_gpu and JoinT_gpu command-line drivers).  sm_103a only; translation
+units compile in parallel.  Usage: python -m crime_gb300.build [--force]"""
 import concurrent.futures as cf
 import os
 import subprocess
@@ -57,11 +57,6 @@ def build(force=False, verbose=False):
     objs = [os.path.join(OBJ, f + ".o") for f in CU + CXX]
     if force or jobs or _newer(LIB, objs):
         _run([NVCC, *ARCH, "-shared", "-cudart", "static", *objs, "-o", LIB])
-    cb = os.path.join(CSRC, "colpass_bench.cu")
-    cbx = os.path.join(LIBDIR, "colpass_bench")
-    if os.path.exists(cb) and (force or _newer(cbx, [cb, LIB] + hdrs)):
-        _run([NVCC, *ARCH, "-std=c++17", "-O2", "--expt-relaxed-constexpr", cb, "-I" + CSRC, "-L" + LIBDIR,
-              "-lgethi_gpu", "-Xlinker", "-rpath,$ORIGIN", "-o", cbx])
     drv = os.path.join(CSRC, "gethi_main.c")
     if os.path.exists(drv) and (force or _newer(EXE, [drv, LIB])):
         _run(["gcc", "-O2", "-Wall", drv, "-I" + os.path.join(os.path.dirname(PKG), "include"), "-L" + LIBDIR,

@@ -115,7 +115,7 @@ void fill_cfg(gethi_ctx *c)
   g.n = s.p.n_grid;
   g.m = s.p.n_grid / 2;
   g.l_box = s.d.l_box;
-  g.dx = s.d.l_box / s.p.n_grid;  // src/pixelize.c:328
+  g.dx = s.d.l_box / s.p.n_grid;  // src/pixelize.c:175
   g.pos_obs = s.d.pos_obs;
   g.dxf = (float)g.dx;
   g.pos_obsf = (float)g.pos_obs;
@@ -151,7 +151,7 @@ void fill_cfg(gethi_ctx *c)
   g.npix = 12 * s.p.n_side * s.p.n_side;
   g.nu_min = s.p.nu_min;
   g.nu_max = s.p.nu_max;
-  g.inv_dnu = s.p.n_nu / (s.p.nu_max - s.p.nu_min);  // src/pixelize.c:330
+  g.inv_dnu = s.p.n_nu / (s.p.nu_max - s.p.nu_min);  // src/pixelize.c:177
   g.nu_edges = c->edges_d;
   g.nu_edges_f = c->edges_f;
   g.prefac = c->prefac;

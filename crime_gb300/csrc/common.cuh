@@ -271,7 +271,7 @@ struct DevCfg {
   const double *nu_edges;  // n_nu + 1 edges
   const float *nu_edges_f; // FP32 copy for the fast path
   const float *prefac;     // n_nu
-  // sub-samples (src/pixelize.c:306-317)
+  // sub-samples (src/pixelize.c:157-164)
   double xs[kNSUB], ys[kNSUB], zs[kNSUB];
   // model switches
   int bias_const, do_rsd;

@@ -515,7 +515,7 @@ int setup_build(const gethi_params &p, Setup &s, std::string &err)
   s.d.pk_norm = p.sigma_8 * p.sigma_8 / s2;
   for (auto &v : s.pk) v *= s.d.pk_norm;
 
-  // sub-sample offsets (src/pixelize.c:310-317)
+  // sub-sample offsets (src/pixelize.c:157-164)
   {
     MT19937 rng(p.seed);
     double lcell = s.d.l_box / p.n_grid;
@@ -526,7 +526,7 @@ int setup_build(const gethi_params &p, Setup &s, std::string &err)
     }
   }
 
-  // channel factors (src/pixelize.c:308, 399-414)
+  // channel factors (src/pixelize.c:155, 246-261)
   double M2T = 90.057156 * p.omega_B * p.h * (12.0 * p.n_side * p.n_side) / (4 * M_PI);
   s.prefac.resize(s.p.n_nu);
   for (int inu = 0; inu < s.p.n_nu; inu++) {

@@ -25,9 +25,9 @@ struct Setup {
   std::vector<double> logk, pk;
   // frequency shells: bin edges nu0[i] <= nu < nuf[i] (src/io_gh.c:29-57)
   std::vector<double> nu0, nuf;
-  // sub-sample offsets (src/pixelize.c:306-317)
+  // sub-sample offsets (src/pixelize.c:157-164)
   double xs[NSUB], ys[NSUB], zs[NSUB];
-  // per-channel temperature factor M2T/(r^2 dnu) (src/pixelize.c:399-414)
+  // per-channel temperature factor M2T/(r^2 dnu) (src/pixelize.c:246-261)
   std::vector<double> prefac;
   double n_scal;
   // point sources (do_psources=1): n(z) and rejection bounds (src/psources.c:98-124),

@@ -10,6 +10,7 @@
 // and shell edges the kernels read -- lives in the file-scope device arrays
 // below, which every GPU that loads the library keeps until the process exits.
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "../../include/gethi_gpu.h"
@@ -42,6 +43,7 @@ struct Scratch {
   float *tab_f = nullptr, *edges_f = nullptr, *prefac = nullptr;
 };
 Scratch g_scratch[kMaxDevices];
+std::mutex g_scratch_mutex;  // first calls from several host threads look the addresses up once
 
 int fail(const std::string &m, int code)
 {
@@ -54,6 +56,7 @@ int fail(const std::string &m, int code)
 int scratch_for(int dev, Scratch **out)
 {
   if (dev < 0 || dev >= kMaxDevices) return fail("device index out of range", GETHI_E_ARG);
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
   Scratch &s = g_scratch[dev];
   if (!s.ready) {
     cudaError_t e = cudaSuccess;
@@ -105,43 +108,53 @@ extern "C" int gethi_project_noalloc(const gethi_params *p, const gethi_derived 
   cudaStream_t st = (cudaStream_t)stream;
 
   // host setup values into the device arrays: stream-ordered copies from
-  // pageable host memory (each returns once its source has been staged, so the
-  // small stack buffers below can be reused), no allocation
-  NA_CK(cudaMemcpyAsync(sc->tab_d, tables + 2 * NZ, sizeof(double) * NZ, cudaMemcpyHostToDevice, st));  // z_r2z
-  NA_CK(cudaMemcpyAsync(sc->tab_d + NZ, tables + 3 * NZ, sizeof(double) * NZ, cudaMemcpyHostToDevice, st));
-  NA_CK(cudaMemcpyAsync(sc->tab_d + 2 * NZ, tables + 4 * NZ, sizeof(double) * 2 * NZ, cudaMemcpyHostToDevice, st));
-  float tf[3 * 64];
-  for (int base = 0; base < NZ; base += 64) {  // FP32 copies, staged through a small stack buffer
-    const int cnt = NZ - base < 64 ? NZ - base : 64;
-    for (int k = 0; k < 3; k++)
-      for (int i = 0; i < cnt; i++) tf[k * 64 + i] = (float)tables[(k == 0 ? 2 : 3 + k) * NZ + base + i];
-    for (int k = 0; k < 3; k++)
-      NA_CK(cudaMemcpyAsync(sc->tab_f + k * NZ + base, tf + k * 64, sizeof(float) * cnt, cudaMemcpyHostToDevice, st));
-  }
-  float buf[256];
-  for (int base = 0; base <= n_nu; base += 256) {
-    const int cnt = n_nu + 1 - base < 256 ? n_nu + 1 - base : 256;
-    double eb[256];
-    for (int i = 0; i < cnt; i++) {
-      const int k = base + i;
-      eb[i] = d->regular_nu ? p->nu_min + (p->nu_max - p->nu_min) * (double)k / n_nu : nu_edges[k];
-      buf[i] = (float)eb[i];
+  // pageable stack buffers (each cudaMemcpyAsync returns once its source has
+  // been staged, so the buffers can be refilled and the caller's arrays may
+  // change as soon as the call returns), up to 8 KB per copy, no allocation
+  constexpr int kChunk = 1024;
+  double db[kChunk];
+  float fb[kChunk];
+  // FP64 copy of src[0..cnt); src may be db itself (one chunk)
+  auto put_d = [&](double *dst, const double *src, int cnt) -> cudaError_t {
+    for (int base = 0; base < cnt; base += kChunk) {
+      const int k = cnt - base < kChunk ? cnt - base : kChunk;
+      if (src != db) std::memcpy(db, src + base, sizeof(double) * k);
+      cudaError_t e = cudaMemcpyAsync(dst + base, db, sizeof(double) * k, cudaMemcpyHostToDevice, st);
+      if (e != cudaSuccess) return e;
     }
-    NA_CK(cudaMemcpyAsync(sc->edges_d + base, eb, sizeof(double) * cnt, cudaMemcpyHostToDevice, st));
-    NA_CK(cudaMemcpyAsync(sc->edges_f + base, buf, sizeof(float) * cnt, cudaMemcpyHostToDevice, st));
+    return cudaSuccess;
+  };
+  // FP32 copy of src[0..cnt)
+  auto put_f = [&](float *dst, const double *src, int cnt) -> cudaError_t {
+    for (int base = 0; base < cnt; base += kChunk) {
+      const int k = cnt - base < kChunk ? cnt - base : kChunk;
+      for (int i = 0; i < k; i++) fb[i] = (float)src[base + i];
+      cudaError_t e = cudaMemcpyAsync(dst + base, fb, sizeof(float) * k, cudaMemcpyHostToDevice, st);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  };
+  NA_CK(put_d(sc->tab_d, tables + 2 * NZ, NZ));               // z(r)
+  NA_CK(put_d(sc->tab_d + NZ, tables + 3 * NZ, NZ));          // r
+  NA_CK(put_d(sc->tab_d + 2 * NZ, tables + 4 * NZ, 2 * NZ));  // growth of density and velocity
+  NA_CK(put_f(sc->tab_f, tables + 2 * NZ, NZ));
+  NA_CK(put_f(sc->tab_f + NZ, tables + 4 * NZ, NZ));
+  NA_CK(put_f(sc->tab_f + 2 * NZ, tables + 5 * NZ, NZ));
+  for (int base = 0; base <= n_nu; base += kChunk) {  // shell edges, FP64 and FP32
+    const int k = n_nu + 1 - base < kChunk ? n_nu + 1 - base : kChunk;
+    for (int i = 0; i < k; i++)
+      db[i] = d->regular_nu ? p->nu_min + (p->nu_max - p->nu_min) * (double)(base + i) / n_nu : nu_edges[base + i];
+    NA_CK(put_f(sc->edges_f + base, db, k));
+    NA_CK(put_d(sc->edges_d + base, db, k));
   }
-  for (int base = 0; base < n_nu; base += 256) {
-    const int cnt = n_nu - base < 256 ? n_nu - base : 256;
-    for (int i = 0; i < cnt; i++) buf[i] = (float)prefac[base + i];
-    NA_CK(cudaMemcpyAsync(sc->prefac + base, buf, sizeof(float) * cnt, cudaMemcpyHostToDevice, st));
-  }
+  NA_CK(put_f(sc->prefac, prefac, n_nu));
 
   DevCfg g;
   std::memset(&g, 0, sizeof(g));
   g.n = n;
   g.m = n / 2;
   g.l_box = d->l_box;
-  g.dx = d->l_box / n;  // src/pixelize.c:328
+  g.dx = d->l_box / n;  // src/pixelize.c:175
   g.pos_obs = d->pos_obs;
   g.dxf = (float)g.dx;
   g.pos_obsf = (float)g.pos_obs;
@@ -162,7 +175,7 @@ extern "C" int gethi_project_noalloc(const gethi_params *p, const gethi_derived 
   g.npix = 12 * p->n_side * p->n_side;
   g.nu_min = d->regular_nu ? p->nu_min : nu_edges[0];
   g.nu_max = d->regular_nu ? p->nu_max : nu_edges[n_nu];
-  g.inv_dnu = n_nu / (g.nu_max - g.nu_min);  // src/pixelize.c:330
+  g.inv_dnu = n_nu / (g.nu_max - g.nu_min);  // src/pixelize.c:177
   g.nu_edges = sc->edges_d;
   g.nu_edges_f = sc->edges_f;
   g.prefac = sc->prefac;

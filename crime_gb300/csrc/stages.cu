@@ -85,7 +85,7 @@ __global__ void get_hi_kernel(DevCfg c, const double *__restrict__ stats, float 
 
 // ---------------------------------------------------------------------------
 // exact (FP64) sample key: the reference's operation sequence
-// (src/pixelize.c:346-379, src/cosmo.c:52-62) with every rounding explicit, so
+// (src/pixelize.c:206-222, src/cosmo.c:52-62) with every rounding explicit, so
 // no multiply-add is contracted; vec2pix_ring is the RING scheme of Gorski et
 // al. (2005) in the same form as the oracle.
 // ---------------------------------------------------------------------------
@@ -102,7 +102,7 @@ __device__ __forceinline__ double z_of_r_exact(const DevCfg &c, double r)
 
 __device__ __forceinline__ int bin_exact(const DevCfg &c, double nu)
 {
-  if (c.regular_nu) return (int)__dmul_rn(c.inv_dnu, __dsub_rn(nu, c.nu_min));  // src/pixelize.c:369
+  if (c.regular_nu) return (int)__dmul_rn(c.inv_dnu, __dsub_rn(nu, c.nu_min));  // src/pixelize.c:216
   // src/pixelize.c:28-56: the walk ends in the unique bin nu0 <= nu < nuf of the contiguous table
   const double *e = c.nu_edges;
   if (!(nu >= __ldg(&e[0]))) return -1;
@@ -198,7 +198,7 @@ __device__ __noinline__ uint32_t key_refine(const DevCfg &c, int ix, int iy, int
   constexpr df kNu21 = df_const(1420.40575177);
   const df nu = df_div(kNu21, df_add(df_f(1.f), red));
   int inu;
-  if (c.regular_nu) {  // (int) truncation, src/pixelize.c:369
+  if (c.regular_nu) {  // (int) truncation, src/pixelize.c:216
     const df t = df_mul(df_of(c.inv_dnu_df), df_sub(nu, df_of(c.nu_min_df)));
     const float m = kM * (fabsf(t.hi) + fabsf(c.inv_dnu_df.x * nu.hi) + 1.f);
     const int f = df_floor(t, m, unc);
@@ -350,7 +350,7 @@ __device__ __forceinline__ uint32_t key_fast(const DevCfg &c, const FastConst &f
   if (c.regular_nu) {
     const float t = (nu - f.nu_min) * f.inv_dnu;
     unc = near_int(t, (mnu + 1.2e-7f * nu) * f.inv_dnu + 4e-7f * fabsf(t) + 1e-6f);
-    inu = (int)t;  // truncation, src/pixelize.c:369
+    inu = (int)t;  // truncation, src/pixelize.c:216
   } else {
     // edges ef[0..nn]: branch-free search for the last edge <= nu (inu = -1 below ef[0], nn at/above ef[nn])
     const int nn = c.n_nu;
@@ -428,7 +428,7 @@ __device__ __forceinline__ uint32_t pixel_fast(const DevCfg &c, float X, float Y
 
 // ---------------------------------------------------------------------------
 // projection: 10 sub-samples per cell -> maps[bin][pix] += mass/10
-// (src/pixelize.c:343-384).  One block per 8x8x8 tile of cells.  Each thread
+// (src/pixelize.c:190-231).  One block per 8x8x8 tile of cells.  Each thread
 // merges runs of equal keys among its cell's sub-samples; the tile's
 // (key, mass) pairs are then accumulated per distinct key in a shared-memory
 // table, and each distinct key of the tile is added to the map once.  Samples
@@ -526,7 +526,7 @@ __global__ void __launch_bounds__(kProjThreads) project_kernel(DevCfg c, FastCon
       mass = ak;
       dz = bk;
     }
-    const float msub = mass / 10.f;  // src/pixelize.c:356
+    const float msub = mass / 10.f;  // src/pixelize.c:203
     const float Xc = (float)ix - f.half_n, Yc = (float)iy - f.half_n, Zc = (float)iz - f.half_n;
     uint32_t cur = 0xFFFFFFFFu;
     float acc = 0.f;
@@ -606,7 +606,7 @@ __global__ void fixup_kernel(DevCfg c, const FallbackEntry *__restrict__ fq, con
   }
 }
 
-// maps *= M2T / (r(nu_c)^2 dnu) per channel, src/pixelize.c:399-414
+// maps *= M2T / (r(nu_c)^2 dnu) per channel, src/pixelize.c:246-261
 // blockIdx.y = channel; VEC: four pixels per thread (npix = 12 nside^2 is a multiple
 // of 4; maps 16-byte aligned), else one
 template <bool VEC>

@@ -5,7 +5,7 @@ The reference drives one realisation as (src/main_gh.c:34-74)
     par = read_run_params(fname)      # src/io_gh.c:188
     create_d_and_vr_fields(par)       # src/fourier.c:375
     get_HI(par)                       # src/grid_tools.c:103
-    mk_T_maps(par)                    # src/pixelize.c:303
+    mk_T_maps(par)                    # src/pixelize.c:150
     write_maps(par)                   # src/io_gh.c:109
     param_gethi_free(par)             # src/io_gh.c:298
 

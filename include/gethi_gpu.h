@@ -79,7 +79,7 @@ int gethi_read_params(const char *ini_path, gethi_params *p);
  * read_run_params/cosmo_set (src/io_gh.c:255-266, src/cosmo.c:341-413).
  * Optional outputs: tables[6*GETHI_NZ] = z_z2r, r_z2r, z_r2z, r_r2z, growth_d,
  * growth_v; logk[numk], pk[numk] (normalised); offsets[30] = the sub-sample
- * offsets x0,y0,z0,x1,... (src/pixelize.c:310-317); prefac[n_nu]. */
+ * offsets x0,y0,z0,x1,... (src/pixelize.c:159-163); prefac[n_nu]. */
 int gethi_host_setup(const gethi_params *p, gethi_derived *d, double *tables, double *logk, double *pk,
                      double *offsets, double *prefac);
 /* Host draw of the reference's modes (src/fourier.c:234-305) as `nthreads`
@@ -108,7 +108,7 @@ const char *gethi_last_error(void);
 int gethi_gpu_make_fields(gethi_ctx *ctx, const float *modes_k);
 /* get_HI (src/grid_tools.c:103-153): lognormal HI mass and dz_rsd, in place. */
 int gethi_gpu_get_hi(gethi_ctx *ctx);
-/* mk_T_maps (src/pixelize.c:303-417): maps[n_nu][12 n_side^2] in mK.
+/* mk_T_maps (src/pixelize.c:150-286): maps[n_nu][12 n_side^2] in mK.
  * maps_out may be NULL (maps stay on the device). */
 int gethi_gpu_make_maps(gethi_ctx *ctx, float *maps_out);
 /* Device pointers of the maps the last make_maps / run left on the context's
@@ -196,7 +196,7 @@ int gethi_gpu_download_modes(gethi_ctx *ctx, float *modes_k);
 int gethi_gpu_stage_times(const gethi_ctx *ctx, float *ms, int n);
 
 /* ---- projection without device allocation ----
- * No counterpart in the reference.  mk_T_maps (src/pixelize.c:303-417) for
+ * No counterpart in the reference.  mk_T_maps (src/pixelize.c:150-286) for
  * callers that cannot let a library call cudaMalloc: they own all device
  * memory through their own allocator or arena, or may not allocate once a run
  * has started.  mass and dz are the caller's device grids (N^3 floats,
@@ -204,7 +204,9 @@ int gethi_gpu_stage_times(const gethi_ctx *ctx, float *ms, int n);
  * output [n_nu][12 n_side^2] (overwritten).  d, tables, offsets and prefac are
  * the outputs of gethi_host_setup for the same parameters; nu_edges holds the
  * n_nu+1 shell edges of a frequency file (NULL for a regular table).  stream is
- * a cudaStream_t (NULL: default stream); the work is enqueued on it.
+ * a cudaStream_t (NULL: default stream); the work is enqueued on it.  The host
+ * arrays are copied through the call's own stack buffers before it returns,
+ * so the caller may change or free them once it has returned.
  * The call allocates nothing: its scratch (a 16 MiB queue of samples whose
  * FP32 key needs the FP64 check, counters, distance tables and shell edges,
  * about 16.4 MiB in all) is a set of file-scope device arrays that every GPU

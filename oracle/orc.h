@@ -44,7 +44,7 @@ typedef struct {
   int n_grid;
   int n_nu;
   unsigned int seed;
-  int regular_nu;         /* 1: (int)(inv_dnu (nu-nu_min)) binning (pixelize.c:369) */
+  int regular_nu;         /* 1: (int)(inv_dnu (nu-nu_min)) binning (pixelize.c:216) */
   int bias_const;         /* 0: bias_HI(z) of src/user_defined.c:32-35 */
   int do_rsd;             /* 0: dz_rsd forced to 0 */
   int pad_;

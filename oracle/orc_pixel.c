@@ -1,7 +1,7 @@
 /*
  * Oracle (test infrastructure only): projection of the HI mass grid onto
  * HEALPix maps, one per frequency shell.  Restates src/pixelize.c:28-56
- * (get_inu) and :303-417 (mk_T_maps).
+ * (get_inu) and :150-286 (mk_T_maps).
  *
  * vec2pix_ring/pix2ang_ring are restated from the RING-scheme formulas of
  * Gorski et al. 2005 (ApJ 622:759, section 4), not from chealpix, which is
@@ -98,7 +98,7 @@ int orc_get_inu(const double *nu0, const double *nuf, int n_nu, double nu, int i
   }
 }
 
-/* src/pixelize.c:306-317: 10 offsets from one MT19937(seed) stream, x,y,z per sub-sample */
+/* src/pixelize.c:157-164: 10 offsets from one MT19937(seed) stream, x,y,z per sub-sample */
 void orc_subsample_offsets(unsigned int seed, double lcell, double *xs, double *ys, double *zs)
 {
   orc_mt rng;
@@ -110,7 +110,7 @@ void orc_subsample_offsets(unsigned int seed, double lcell, double *xs, double *
   }
 }
 
-/* src/pixelize.c:399-414 */
+/* src/pixelize.c:246-261 */
 void orc_channel_prefactors(const orc_config *c, const orc_derived *d, const double *nu0,
                             const double *nuf, double *prefac)
 {
