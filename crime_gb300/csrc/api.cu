@@ -489,15 +489,19 @@ extern "C" int gethi_gpu_init(const gethi_params *p, int device, gethi_ctx **out
       gethi_gpu_free(c);
       return GETHI_E_ARG;
     }
-    if ((rc = dalloc(&c->tc_bmat, tc_table_bytes() / sizeof(uint4))) || (rc = dalloc(&c->tc_tw, tw.size())) ||
-        (rc = dalloc(&c->tc_err, 1))) {
+    if ((rc = dalloc(&c->tc_bmat, tc_table_bytes() / sizeof(uint4))) || (rc = dalloc(&c->tc_tw, tw.size()))) {
       gethi_gpu_free(c);
       return rc;
     }
     cudaMemcpy(c->tc_bmat, bm.data(), tc_table_bytes(), cudaMemcpyHostToDevice);
     cudaMemcpy(c->tc_tw, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice);
-    cudaMemset(c->tc_err, 0, sizeof(int));
   }
+  // error flag of the bounded device-side waits (tensor-core passes, wait self-test)
+  if ((rc = dalloc(&c->tc_err, 1))) {
+    gethi_gpu_free(c);
+    return rc;
+  }
+  cudaMemset(c->tc_err, 0, sizeof(int));
   // tables
   std::vector<float2> t;
   twiddles(t, (int)n);
@@ -674,17 +678,29 @@ static int ensure_fq(gethi_ctx *c)
   return GETHI_OK;
 }
 
-// the tensor-core passes record an expired wait in tc_err (after a synchronize)
+// the tensor-core passes record an expired wait in tc_err (read after a
+// synchronize); the flag is reported once, by the call whose work expired, and
+// cleared, so the context serves the next call
 static int check_tc(const gethi_ctx *c)
 {
   if (!c->tc_err) return GETHI_OK;
   int flag = 0;
   CK(cudaMemcpy(&flag, c->tc_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (flag) {
-    set_error("tensor-core FFT: an MMA completion wait expired");
+    CK(cudaMemset(c->tc_err, 0, sizeof(int)));
+    set_error("a bounded device wait expired (tensor-core MMA completion or wait self-test)");
     return GETHI_E_CUDA;
   }
   return GETHI_OK;
+}
+
+extern "C" int gethi_gpu_wait_selftest(gethi_ctx *c, long limit_us)
+{
+  if (!c || limit_us < 1 || limit_us > 10000000) return GETHI_E_ARG;
+  CK(cudaSetDevice(c->device));
+  CK(wait_selftest(c->tc_err, (uint64_t)limit_us * 1000ull, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return check_tc(c);
 }
 
 static int maps_common(gethi_ctx *c, float *maps_out, int fused)

@@ -46,6 +46,8 @@ cudaError_t tc_col_pass(const DevCfg &c, const ColGeom &g, int mode, int nout, c
                         float2 *out2, cudaStream_t st);
 bool tc_tables(int n, std::vector<uint16_t> &bmat, std::vector<float2> &tw);
 size_t tc_table_bytes();
+// a bounded wait on an mbarrier nothing arrives on: sets *err after limit_ns
+cudaError_t wait_selftest(int *err, uint64_t limit_ns, cudaStream_t st);
 
 // point sources (stages.cu)
 constexpr int kPsNZ = 256;                  // src/common_gh.h:35 (NZ_PSOURCES)

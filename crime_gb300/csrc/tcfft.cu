@@ -313,6 +313,25 @@ cudaError_t launch(const DevCfg &c, const ColGeom &g, int nout, const float2 *sr
 
 }  // namespace
 
+// Failure detection of the bounded waits: one warp waits on an mbarrier that
+// nothing ever arrives on (no asynchronous copy or MMA is issued), through the
+// same bounded wait the tensor-core passes use, and raises the context's error
+// flag when the wait expires, as an expired MMA-completion wait does.
+__global__ void wait_selftest_kernel(int *err, uint64_t limit_ns)
+{
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) tc::mbar_init(&bar, 1);
+  __syncthreads();
+  if (threadIdx.x == 0 && !tc::mbar_wait(&bar, 0, limit_ns)) atomicExch(err, 1);
+  __syncthreads();
+}
+
+cudaError_t wait_selftest(int *err, uint64_t limit_ns, cudaStream_t st)
+{
+  wait_selftest_kernel<<<1, 32, 0, st>>>(err, limit_ns);
+  return cudaGetLastError();
+}
+
 bool tc_col_supported(const DevCfg &c, const ColGeom &g, int nyq)
 {
   return c.tc_bmat && !nyq && c.n == kL && g.cstride == 1 && g.ncols % kTX == 0 && g.cpp % kTX == 0;

@@ -92,6 +92,7 @@ def lib():
         L.gethi_gpu_upload_inputs.restype = C.c_long
         L.gethi_gpu_kernel_times.argtypes = [vp, vp, vp, vp]
         L.gethi_gpu_fallback_count.argtypes = [vp, vp]
+        L.gethi_gpu_wait_selftest.argtypes = [vp, C.c_long]
         L.gethi_gpu_run_batch.argtypes = [vp, C.c_int, vp, vp, C.c_int, vp, C.c_int, vp]
         L.gethi_gpu_autotune.argtypes = [vp, vp, vp]
         L.gethi_gpu_run_async.argtypes = [vp, vp]
@@ -299,6 +300,10 @@ class GetHI:
         launches = np.zeros(1, np.int64)
         lib().gethi_gpu_kernel_times(self._ctx, _ptr(ms), _ptr(cnt), _ptr(launches))
         return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.KERNEL_CLASSES)}, int(launches[0])
+
+    def wait_selftest(self, limit_us=20000):
+        """Run the bounded-wait expiry path once (gethi_gpu_wait_selftest); returns its status code."""
+        return lib().gethi_gpu_wait_selftest(self._ctx, int(limit_us))
 
     def fallback_count(self):
         v = np.zeros(1, np.int64)

@@ -243,6 +243,15 @@ int gethi_gpu_profile(gethi_ctx *ctx, int on);
 int gethi_gpu_kernel_times(const gethi_ctx *ctx, double *ms, long *count, long *launches);
 /* samples of the last projection that needed the FP64 key */
 int gethi_gpu_fallback_count(const gethi_ctx *ctx, long *n);
+/* Failure detection (the reference has none on this path: every error calls
+ * exit(), src/common_gh.c:104-120).  Every device-side wait of this library
+ * (mbarrier waits of the tensor-core passes) is bounded by time; on expiry the
+ * kernel raises the context's error flag and returns, and the next synchronizing
+ * call reports GETHI_E_CUDA once and clears it.  This call runs that path on
+ * purpose: one warp waits limit_us (1 us .. 10 s) on an mbarrier nothing arrives
+ * on, with no copy or MMA in flight.  Returns GETHI_E_CUDA when the wait
+ * expired (always, unless the GPU misbehaves); the context stays usable. */
+int gethi_gpu_wait_selftest(gethi_ctx *ctx, long limit_us);
 
 #ifdef __cplusplus
 }

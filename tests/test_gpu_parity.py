@@ -239,3 +239,56 @@ def test_projection_many_keys_per_tile(gh):
     ref = o.mk_T_maps(pad, padz)
     assert np.count_nonzero(ref) > 10000
     np.testing.assert_allclose(maps, ref, rtol=1e-5, atol=1e-6 * np.abs(ref).max())
+
+
+def test_fast_keys_certified_nside1024(gh):
+    """The 2048^3 workload's geometry (box 6000 Mpc/h, 256 shells over z 0.2-2.5,
+    Nside 1024) at 128^3: certified FP32 keys == FP64 keys on 21M samples."""
+    nu21 = 1420.40575177
+    n = 128
+    ctx = gh.GetHI(synthetic_params(gh, n_grid=n, n_side=1024, l_box=6000.0, nu_min=nu21 / 3.5, nu_max=nu21 / 1.2,
+                                    n_nu=256))
+    rng = np.random.default_rng(6)
+    mass = rng.lognormal(0, 1, (n, n, n)).astype(np.float32)
+    dz = rng.normal(0, 3e-3, (n, n, n)).astype(np.float32)
+    ctx.upload_grids(mass, dz, stage=2)
+    exact = ctx.sample_keys(exact=True)
+    fast = ctx.sample_keys(exact=False)
+    ctx.free()
+    assert np.count_nonzero(exact != 0xFFFFFFFF) > 0.5 * exact.size
+    np.testing.assert_array_equal(fast, exact)
+
+
+def test_c1_shaped_run_vs_oracle(gh):
+    """The 512^3 workload's shells at 128^3 (box 2500 Mpc/h, 150 shells over z
+    0.3-2.0, Nside 256, spectral RSD, Gaussianised P(k), Philox modes): the fused
+    run() against the oracle on the same modes, with the tolerances of
+    test_production_run_vs_oracle; then the validation path, the oracle's own
+    mass and dz uploaded: FP32 keys == FP64 keys, maps element-wise within 1e-5."""
+    from oracle import orc
+    nu21 = 1420.40575177
+    n, nside = 128, 256
+    p = synthetic_params(gh, n_grid=n, n_side=nside, l_box=2500.0, nu_min=nu21 / 3.0, nu_max=nu21 / 1.3, n_nu=150,
+                         velocity_mode="spectral", gaussianise=1, seed=2001)
+    ctx = gh.GetHI(p)
+    maps = ctx.run()
+    modes = ctx.device_modes()
+    k, pk = orc.load_pk(os.path.join(GOLDEN, "pk_eh_nowiggle.txt"))
+    o = orc.Oracle(dict(OmegaM=0.315, OmegaL=0.685, OmegaB=0.049, hhub=0.67, weos=-1.0, n_scal=0.96, sig8=0.83,
+                        n_grid=n, n_side=nside, seed=2001, regular_nu=1, nu_min=p.nu_min, nu_max=p.nu_max,
+                        n_nu=150, l_box_override=2500.0), k, pk)
+    dens = o.normalize(o.c2r(modes))
+    rv = o.radial_velocity_spectral(modes)
+    _, s2 = o.sigma(dens)
+    mass, dz = o.get_hi(dens, rv, s2)
+    ref = o.mk_T_maps(mass, dz)
+    assert np.count_nonzero(ref) > 100000
+    assert rel_l2(maps, ref) < 1e-4
+    close = np.isclose(maps, ref, rtol=1e-5, atol=1e-6 * np.abs(ref).max())
+    assert close.mean() > 0.995
+    # validation path on the oracle's grids
+    ctx.upload_grids(np.ascontiguousarray(cells(mass, n)), np.ascontiguousarray(cells(dz, n)), stage=2)
+    np.testing.assert_array_equal(ctx.sample_keys(exact=False), ctx.sample_keys(exact=True))
+    vmaps = ctx.mk_T_maps()
+    ctx.free()
+    np.testing.assert_allclose(vmaps, ref, rtol=1e-5, atol=1e-6 * np.abs(ref).max())
