@@ -329,8 +329,52 @@ constexpr uint32_t kKeyUncertain = 0xFFFFFFFEu;  // FP32 cannot decide: use key_
 
 __device__ __forceinline__ uint32_t pixel_fast(const DevCfg &c, float X, float Y, float Z, float rho2, float iR);
 
-__device__ __forceinline__ uint32_t key_fast(const DevCfg &c, const FastConst &f, const float *ef, int log2nn, float X,
-                                             float Y, float Z, float dz)
+// frequency-file edges ef[0..nn] (FP32, increasing): the last index lo in -1..nn
+// with ef[lo] <= nu, branch-free over the steps 2^log2nn .. 1
+__device__ __forceinline__ int edge_search(const float *ef, int nn, int log2nn, float nu)
+{
+  int lo = -1;
+#pragma unroll 1
+  for (int step = 1 << log2nn; step > 0; step >>= 1) {
+    const int cand = lo + step;
+    lo = (cand <= nn && nu >= ef[min(cand, nn)]) ? cand : lo;
+  }
+  return lo;
+}
+
+// The bins of a frequency file around a cell centre: bin lo of the centre's
+// frequency and the edges ef[lo-1] .. ef[lo+2] (-inf / +inf beyond 0..nn).  A
+// sub-sample within one bin of the centre's is then binned with four compares;
+// the search is left to samples two or more bins away.  (Regular tables bin by
+// one truncation and need none of this.)
+struct EdgeBracket {
+  int lo;
+  float e0, e1, e2, e3;
+};
+
+__device__ __forceinline__ EdgeBracket edge_bracket(const DevCfg &c, const FastConst &f, const float *ef, int log2nn,
+                                                    float Xc, float Yc, float Zc, float dz)
+{
+  EdgeBracket b{0, 0.f, 0.f, 0.f, 0.f};
+  if (c.regular_nu) return b;
+  // frequency of the cell centre (no certification needed: lo only picks the bracket)
+  const float X = Xc + 0.5f, Y = Yc + 0.5f, Z = Zc + 0.5f;
+  const float tr = fminf(sqrtf(fmaf(Z, Z, fmaf(Y, Y, X * X))) * f.idr_cell, (float)(kNZ - 2));
+  const int ir = (int)tr;
+  const float z0 = __ldg(&c.z_r2z_f[ir]), z1 = __ldg(&c.z_r2z_f[ir + 1]);
+  const float nu = __fdividef(1420.40575177f, 1.f + (fmaf(z1 - z0, tr - (float)ir, z0) + dz));
+  const int nn = c.n_nu;
+  const float inf = __int_as_float(0x7f800000);
+  b.lo = edge_search(ef, nn, log2nn, nu);
+  b.e0 = b.lo - 1 >= 0 ? ef[b.lo - 1] : -inf;
+  b.e1 = b.lo >= 0 ? ef[b.lo] : -inf;
+  b.e2 = b.lo + 1 <= nn ? ef[b.lo + 1] : inf;
+  b.e3 = b.lo + 2 <= nn ? ef[min(b.lo + 2, nn)] : inf;
+  return b;
+}
+
+__device__ __forceinline__ uint32_t key_fast(const DevCfg &c, const FastConst &f, const float *ef, int log2nn,
+                                             const EdgeBracket &br, float X, float Y, float Z, float dz)
 {
   const float rho2 = fmaf(Y, Y, X * X);
   const float R2 = fmaf(Z, Z, rho2);
@@ -352,18 +396,17 @@ __device__ __forceinline__ uint32_t key_fast(const DevCfg &c, const FastConst &f
     unc = near_int(t, (mnu + 1.2e-7f * nu) * f.inv_dnu + 4e-7f * fabsf(t) + 1e-6f);
     inu = (int)t;  // truncation, src/pixelize.c:216
   } else {
-    // edges ef[0..nn]: branch-free search for the last edge <= nu (inu = -1 below ef[0], nn at/above ef[nn])
-    const int nn = c.n_nu;
-    int lo = -1;
-#pragma unroll 1
-    for (int step = 1 << log2nn; step > 0; step >>= 1) {
-      const int cand = lo + step;
-      lo = (cand <= nn && nu >= ef[cand]) ? cand : lo;
+    // bin inu: ef[inu] <= nu < ef[inu + 1] (-1 below ef[0], nn at or above ef[nn])
+    inu = br.lo + (nu >= br.e2 ? 1 : 0) - (nu < br.e1 ? 1 : 0);
+    unc = fabsf(nu - br.e0) < mnu || fabsf(nu - br.e1) < mnu || fabsf(nu - br.e2) < mnu || fabsf(nu - br.e3) < mnu;
+    if (nu < br.e0 || nu >= br.e3) {  // two or more bins from the cell centre's (rare)
+      const int nn = c.n_nu;
+      const int lo = edge_search(ef, nn, log2nn, nu);
+      inu = lo;
+      const float below = lo >= 0 ? nu - ef[max(lo, 0)] : 1e30f;
+      const float above = lo < nn ? ef[min(lo + 1, nn)] - nu : 1e30f;
+      unc = below < mnu || above < mnu;
     }
-    inu = lo;
-    const float below = lo >= 0 ? nu - ef[lo] : 1e30f;
-    const float above = lo < nn ? ef[lo + 1] - nu : 1e30f;
-    unc = below < mnu || above < mnu;
   }
   if (bad || unc) return kKeyUncertain;
   if (inu < 0 || inu >= c.n_nu) return kKeyInvalid;
@@ -462,7 +505,7 @@ struct FallbackEntry {
 };
 
 template <bool FUSED>
-__global__ void __launch_bounds__(kProjThreads) project_kernel(DevCfg c, FastConst f, const double *__restrict__ stats,
+__global__ void __launch_bounds__(kProjThreads, 4) project_kernel(DevCfg c, FastConst f, const double *__restrict__ stats,
                                                                const float *__restrict__ a, const float *__restrict__ b,
                                                                float *__restrict__ maps, int *__restrict__ counters,
                                                                FallbackEntry *__restrict__ fq, long fq_cap)
@@ -510,11 +553,12 @@ __global__ void __launch_bounds__(kProjThreads) project_kernel(DevCfg c, FastCon
     }
     const float msub = mass / 10.f;  // src/pixelize.c:203
     const float Xc = (float)ix - f.half_n, Yc = (float)iy - f.half_n, Zc = (float)iz - f.half_n;
+    const EdgeBracket br = edge_bracket(c, f, ef, log2nn, Xc, Yc, Zc, dz);
     uint32_t cur = 0xFFFFFFFFu, umask = 0;
     float acc = 0.f;
 #pragma unroll kProjUnroll
     for (int j = 0; j < kNSUB; j++) {
-      const uint32_t key = key_fast(c, f, ef, log2nn, Xc + f.txsp[j], Yc + f.tysp[j], Zc + f.tzsp[j], dz);
+      const uint32_t key = key_fast(c, f, ef, log2nn, br, Xc + f.txsp[j], Yc + f.tysp[j], Zc + f.tzsp[j], dz);
       umask |= (key == kKeyUncertain ? 1u : 0u) << j;
       if (key < kKeyUncertain) {  // a key inside the shells; the run of cur ends at a new key
         if (key != cur && cur != 0xFFFFFFFFu) map_add(maps, cur, acc);
@@ -624,9 +668,11 @@ __global__ void sample_keys_kernel(DevCfg c, FastConst f, const float *__restric
     const int iy = (int)(rest % n), iz = (int)(rest / n);
     const float dz = dzg[i];
     const float Xc = (float)ix - f.half_n, Yc = (float)iy - f.half_n, Zc = (float)iz - f.half_n;
+    const EdgeBracket br = edge_bracket(c, f, c.nu_edges_f, log2nn, Xc, Yc, Zc, dz);
     for (int is = 0; is < kNSUB; is++) {
       uint32_t key = kKeyUncertain;
-      if (!exact) key = key_fast(c, f, c.nu_edges_f, log2nn, Xc + f.xsp[is], Yc + f.ysp[is], Zc + f.zsp[is], dz);
+      if (!exact)
+        key = key_fast(c, f, c.nu_edges_f, log2nn, br, Xc + f.xsp[is], Yc + f.ysp[is], Zc + f.zsp[is], dz);
       if (key == kKeyUncertain) {
         key = exact ? key_exact(c, ix, iy, iz, is, dz) : key_resolve(c, ix, iy, iz, is, dz);
         nfall++;
