@@ -162,17 +162,38 @@ __device__ __forceinline__ void row_c2r_smem(float2 *v, float2 *srow, float2 xm,
   stockham_run<M, P, true>(v, srow, 1, t, twM, Rad{});
 }
 
+// asynchronous copy of one float2 from global to shared memory (cp.async, no
+// register staging); completed by cp_async_wait_all
+__device__ __forceinline__ void cp_async8(float2 *dst, const float2 *src)
+{
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all()
+{
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
+// one row of M complex points into shared memory (skewed slots), asynchronously
+template <int M, int P>
+__device__ __forceinline__ void row_load_async(float2 *srow, const float2 *__restrict__ grow, bool active, int t)
+{
+  constexpr int T = M / P;
+#pragma unroll
+  for (int j = 0; j < P; j++) {
+    float2 *d = &srow[sm_slot<true>(t + T * j, 1)];
+    if (active) cp_async8(d, grow + t + T * j);
+    else *d = make_float2(0.f, 0.f);
+  }
+}
+
 template <int M, int P, int RW, class Rad>
 __device__ __forceinline__ void row_c2r(float2 *v, float2 *srow, const float2 *__restrict__ grow, float2 xm,
                                         bool active, int t, const float2 *__restrict__ twN,
                                         const float2 *__restrict__ twM)
 {
-  constexpr int T = M / P;
-  float2 ld[P];
-#pragma unroll
-  for (int j = 0; j < P; j++) ld[j] = active ? grow[t + T * j] : make_float2(0.f, 0.f);
-#pragma unroll
-  for (int j = 0; j < P; j++) srow[sm_slot<true>(t + T * j, 1)] = ld[j];
+  row_load_async<M, P>(srow, grow, active, t);
+  cp_async_wait_all();
   __syncthreads();
   row_c2r_smem<M, P, Rad>(v, srow, xm, t, twN, twM);
 }
@@ -199,14 +220,10 @@ __global__ void __launch_bounds__(RW *(M / P), EPI == 2 ? 512 / (RW * (M / P)) :
 #pragma unroll
     for (int comp = 0; comp < 3; comp++) {
       sr[comp] = smem + (comp * RW + rl) * sm_len<M, true>();
-      const float2 *grow = in.main[comp] + row * (long)M;
-      float2 ld[P];
-#pragma unroll
-      for (int j = 0; j < P; j++) ld[j] = active ? grow[t + T * j] : make_float2(0.f, 0.f);
-#pragma unroll
-      for (int j = 0; j < P; j++) sr[comp][sm_slot<true>(t + T * j, 1)] = ld[j];
+      row_load_async<M, P>(sr[comp], in.main[comp] + row * (long)M, active, t);
       xm[comp] = active ? in.nyq[comp][row] : make_float2(0.f, 0.f);
     }
+    cp_async_wait_all();
     __syncthreads();
     float2 acc[P];
     const int iy = (int)(row % c.n), iz = (int)(row / c.n);
