@@ -1036,6 +1036,14 @@ extern "C" int gethi_gpu_autotune(gethi_ctx *c, int *choice, float *ms_out)
   return check_tc(c);
 }
 
+extern "C" int gethi_gpu_set_launch(gethi_ctx *c, int proj_zsteps, int col_variant)
+{
+  if (!c || proj_zsteps < 0 || proj_zsteps > 4 || col_variant < 0 || col_variant > 2) return GETHI_E_ARG;
+  c->cfg.proj_zsteps = proj_zsteps;
+  c->cfg.col_variant = col_variant;
+  return GETHI_OK;
+}
+
 extern "C" int gethi_gpu_write_maps(const gethi_ctx *c, const float *maps)
 {
   if (!c || !maps) return GETHI_E_ARG;

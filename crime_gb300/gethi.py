@@ -95,6 +95,7 @@ def lib():
         L.gethi_gpu_wait_selftest.argtypes = [vp, C.c_long]
         L.gethi_gpu_run_batch.argtypes = [vp, C.c_int, vp, vp, C.c_int, vp, C.c_int, vp]
         L.gethi_gpu_autotune.argtypes = [vp, vp, vp]
+        L.gethi_gpu_set_launch.argtypes = [vp, C.c_int, C.c_int]
         L.gethi_gpu_run_async.argtypes = [vp, vp]
         L.gethi_gpu_wait.argtypes = [vp]
         L.gethi_gpu_psources_maps.argtypes = [vp, vp, vp]
@@ -309,6 +310,10 @@ class GetHI:
         v = np.zeros(1, np.int64)
         _check(lib().gethi_gpu_fallback_count(self._ctx, _ptr(v)))
         return int(v[0])
+
+    def set_launch(self, proj_zsteps=0, col_variant=0):
+        """Launch shapes by hand (gethi_gpu_set_launch)."""
+        _check(lib().gethi_gpu_set_launch(self._ctx, int(proj_zsteps), int(col_variant)))
 
     def autotune(self):
         """Pick the fastest projection tile depth / column tile width for this

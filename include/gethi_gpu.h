@@ -184,6 +184,13 @@ int gethi_gpu_run_batch(gethi_ctx *const *ctx, int nctx, const int *job_ctx, con
  * choice (may be NULL) = {tile depth / 4, column variant}; ms = best time per
  * realisation. */
 int gethi_gpu_autotune(gethi_ctx *ctx, int *choice, float *ms);
+/* Launch shapes by hand (no counterpart in the reference; gethi_gpu_autotune
+ * picks them by timing): proj_zsteps = projection tile depth / 4 cells (1..4,
+ * 0 = built-in), col_variant = FP32 column passes: 0 = built-in (Y passes of
+ * 512- and 1024-point columns from TMA-staged tiles), 1 = half-width tiles
+ * (128/256/384 points), 2 = tiles loaded through registers.  All choices give
+ * the same fields to FP32 rounding. */
+int gethi_gpu_set_launch(gethi_ctx *ctx, int proj_zsteps, int col_variant);
 
 /* ---- validation / inspection (compact [z][y][x] float grids, N^3) ---- */
 int gethi_gpu_download_grids(const gethi_ctx *ctx, float *dens, float *rvel);
