@@ -241,7 +241,10 @@ __global__ void __launch_bounds__(TX *(L / P), MINB)
 // c2r of one row held in shared memory (srow, skewed slots): Z[k] at the
 // first-stage positions, then the M-point inverse FFT; srow is reused as the
 // exchange buffer
-template <int M, int P, class Rad>
+// SKEWIN: the input row sits in the skewed slots (loaded point by point); false:
+// in natural order (a bulk copy), which the reads of k and M - k by consecutive
+// threads take without bank conflicts as well
+template <int M, int P, class Rad, bool SKEWIN = true>
 __device__ __forceinline__ void row_c2r_smem(float2 *v, float2 *srow, float2 xm, int t, const float2 *__restrict__ twN,
                                              const float2 *__restrict__ twM)
 {
@@ -252,7 +255,7 @@ __device__ __forceinline__ void row_c2r_smem(float2 *v, float2 *srow, float2 xm,
 #pragma unroll
     for (int r = 0; r < R0; r++) {
       const int k = t + T * j + (M / R0) * r;
-      float2 a = srow[sm_slot<true>(k, 1)], b = k == 0 ? xm : srow[sm_slot<true>(M - k, 1)];
+      float2 a = srow[sm_slot<SKEWIN>(k, 1)], b = k == 0 ? xm : srow[sm_slot<SKEWIN>(M - k, 1)];
       if (k == 0) {
         a.y = 0.f;
         b.y = 0.f;
@@ -300,6 +303,47 @@ __device__ __forceinline__ void row_c2r(float2 *v, float2 *srow, const float2 *_
   row_c2r_smem<M, P, Rad>(v, srow, xm, t, twN, twM);
 }
 
+// v_r of one row: v . (x - x_obs) accumulated over the components (x in the
+// two cells 2e, 2e + 1 of point e), then divided by |x - x_obs| once
+template <int M, int P, int RL>
+__device__ __forceinline__ void vr_accumulate(const DevCfg &c, int comp, const float2 *v, float2 *acc, int t, float y,
+                                              float z)
+{
+  constexpr int T = M / P;
+#pragma unroll
+  for (int j = 0; j < P / RL; j++)
+#pragma unroll
+    for (int r = 0; r < RL; r++) {
+      const int e = t + T * j + (M / RL) * r;
+      const float2 x = v[j * RL + r];
+      if (comp == 0) {
+        const float x0 = c.dxf * (2 * e + 0.5f) - c.pos_obsf, x1 = c.dxf * (2 * e + 1.5f) - c.pos_obsf;
+        acc[j * RL + r] = make_float2(x.x * x0, x.y * x1);
+      } else {
+        const float w = comp == 1 ? y : z;
+        acc[j * RL + r] = make_float2(fmaf(x.x, w, acc[j * RL + r].x), fmaf(x.y, w, acc[j * RL + r].y));
+      }
+    }
+}
+
+template <int M, int P, int RL>
+__device__ __forceinline__ void vr_store(const DevCfg &c, const float2 *acc, float *vrow_f, int t, float y, float z,
+                                         float scale)
+{
+  constexpr int T = M / P;
+  float2 *vrow = reinterpret_cast<float2 *>(vrow_f);
+  const float yz = y * y + z * z;
+#pragma unroll
+  for (int j = 0; j < P / RL; j++)
+#pragma unroll
+    for (int r = 0; r < RL; r++) {
+      const int e = t + T * j + (M / RL) * r;
+      const float x0 = c.dxf * (2 * e + 0.5f) - c.pos_obsf, x1 = c.dxf * (2 * e + 1.5f) - c.pos_obsf;
+      const float s0 = scale * rsqrtf(fmaf(x0, x0, yz)), s1 = scale * rsqrtf(fmaf(x1, x1, yz));
+      vrow[e] = make_float2(acc[j * RL + r].x * s0, acc[j * RL + r].y * s1);
+    }
+}
+
 template <int M, int P, int RW, class Rad, int EPI>
 __global__ void __launch_bounds__(RW *(M / P), EPI == 2 ? 512 / (RW * (M / P)) : 3) row_pass_kernel(DevCfg c, RowIn in, long nrows,
                                                                const float2 *__restrict__ twN,
@@ -334,34 +378,9 @@ __global__ void __launch_bounds__(RW *(M / P), EPI == 2 ? 512 / (RW * (M / P)) :
 #pragma unroll 1
     for (int comp = 0; comp < 3; comp++) {
       row_c2r_smem<M, P, Rad>(v, sr[comp], xm[comp], t, twN, twM);
-#pragma unroll
-      for (int j = 0; j < P / RL; j++)
-#pragma unroll
-        for (int r = 0; r < RL; r++) {
-          const int e = t + T * j + (M / RL) * r;
-          const float2 x = v[j * RL + r];
-          if (comp == 0) {
-            const float x0 = c.dxf * (2 * e + 0.5f) - c.pos_obsf, x1 = c.dxf * (2 * e + 1.5f) - c.pos_obsf;
-            acc[j * RL + r] = make_float2(x.x * x0, x.y * x1);
-          } else {
-            const float w = comp == 1 ? y : z;
-            acc[j * RL + r] = make_float2(fmaf(x.x, w, acc[j * RL + r].x), fmaf(x.y, w, acc[j * RL + r].y));
-          }
-        }
+      vr_accumulate<M, P, RL>(c, comp, v, acc, t, y, z);
     }
-    if (active) {
-      float2 *vrow = reinterpret_cast<float2 *>(vr + row * (long)c.n);
-      const float yz = y * y + z * z;
-#pragma unroll
-      for (int j = 0; j < P / RL; j++)
-#pragma unroll
-        for (int r = 0; r < RL; r++) {
-          const int e = t + T * j + (M / RL) * r;
-          const float x0 = c.dxf * (2 * e + 0.5f) - c.pos_obsf, x1 = c.dxf * (2 * e + 1.5f) - c.pos_obsf;
-          const float s0 = scale * rsqrtf(fmaf(x0, x0, yz)), s1 = scale * rsqrtf(fmaf(x1, x1, yz));
-          vrow[e] = make_float2(acc[j * RL + r].x * s0, acc[j * RL + r].y * s1);
-        }
-    }
+    if (active) vr_store<M, P, RL>(c, acc, vr + row * (long)c.n, t, y, z, scale);
   } else {
     float2 *grow = in.main[0] + row * (long)M;
     row_c2r<M, P, RW, Rad>(v, srow, grow, active ? in.nyq[0][row] : make_float2(0.f, 0.f), active, t, twN, twM);
@@ -420,6 +439,74 @@ __global__ void __launch_bounds__(RW *(M / P), EPI == 2 ? 512 / (RW * (M / P)) :
       }
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Fused v_r X pass, persistent, rows staged by bulk copies: a CTA walks groups
+// of RW rows; one thread copies the group's three component rows (RW x 3 copies
+// of N/2 complex, cp.async.bulk completing on one mbarrier) into natural-order
+// slots of the skewed row buffers, which the c2r's Stockham exchanges then use.
+// Once a group is stored the buffers are refilled with the CTA's next group;
+// the other CTAs on the SM cover that wait.  Waits are bounded by 1 s of the
+// global timer (on expiry: *err raised, copies in flight awaited, stop).
+// ---------------------------------------------------------------------------
+template <int M, int P, int RW, int MINB, class Rad>
+__global__ void __launch_bounds__(RW *(M / P), MINB)
+    row_vel_bulk_kernel(DevCfg c, RowIn in, long ngroups, const float2 *__restrict__ twN,
+                        const float2 *__restrict__ twM, float scale, float *vr, int *err)
+{
+  constexpr int T = M / P, RL = radix_last(Rad{}), SL = sm_len<M, true>();
+  constexpr uint32_t kRowBytes = M * sizeof(float2);
+  extern __shared__ float2 smem_raw[];  // [comp][row of the group][SL], from a 128-byte boundary
+  float2 *smem = smem_raw + ((128u - (tc::smem_addr(smem_raw) & 127u)) & 127u) / sizeof(float2);
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int stop;
+  const int tid = threadIdx.x, rl = tid / T, t = tid % T;
+  auto issue = [&](long g) {
+    tc::mbar_arrive_expect_tx(&bar, 3 * RW * kRowBytes);
+#pragma unroll
+    for (int comp = 0; comp < 3; comp++)
+#pragma unroll
+      for (int r = 0; r < RW; r++)
+        tc::bulk_g2s(smem + (comp * RW + r) * SL, in.main[comp] + (g * RW + r) * (long)M, kRowBytes, &bar);
+  };
+  if (tid == 0) {
+    tc::mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    stop = 0;
+    if ((long)blockIdx.x < ngroups) issue(blockIdx.x);
+  }
+  __syncthreads();
+  uint32_t phase = 0;
+  float2 *sr[3];
+#pragma unroll
+  for (int comp = 0; comp < 3; comp++) sr[comp] = smem + (comp * RW + rl) * SL;
+  for (long g = blockIdx.x; g < ngroups; g += gridDim.x) {
+    const long row = g * RW + rl;
+    float2 xm[3];
+#pragma unroll
+    for (int comp = 0; comp < 3; comp++) xm[comp] = in.nyq[comp][row];
+    if (tid == 0 && !tc::mbar_wait(&bar, phase, kTmaWaitNs)) {
+      if (err) atomicExch(err, 1);
+      stop = 1;
+    }
+    __syncthreads();
+    if (stop) break;
+    phase ^= 1u;
+    float2 v[P], acc[P];
+    const int iy = (int)(row % c.n), iz = (int)(row / c.n);
+    const float y = c.dxf * (iy + 0.5f) - c.pos_obsf, z = c.dxf * (iz + 0.5f) - c.pos_obsf;
+#pragma unroll 1
+    for (int comp = 0; comp < 3; comp++) {
+      row_c2r_smem<M, P, Rad, false>(v, sr[comp], xm[comp], t, twN, twM);
+      vr_accumulate<M, P, RL>(c, comp, v, acc, t, y, z);
+    }
+    vr_store<M, P, RL>(c, acc, vr + row * (long)c.n, t, y, z, scale);
+    tc::fence_proxy_async();  // this group's accesses before the copies that refill the buffers
+    __syncthreads();
+    if (tid == 0 && g + (long)gridDim.x < ngroups) issue(g + gridDim.x);
+  }
+  if (stop && tid == 0) tc::mbar_wait(&bar, phase, kTmaWaitNs);
 }
 
 // Kahan-compensated FP64 sum of the per-block partials -> stats = (mean, sigma^2)
@@ -698,6 +785,46 @@ static cudaError_t launch_row(const DevCfg &c, const RowIn &in, const float2 *tw
   return cudaGetLastError();
 }
 
+// persistent bulk-copy v_r X pass: plans per row length (N/2 complex points)
+template <int M> struct VelBulkPlan { static constexpr bool ok = false; };
+template <> struct VelBulkPlan<512> { static constexpr bool ok = true; static constexpr int P = 16, RW = 4, MINB = 4; using R = Radices<16, 16, 2>; };
+template <> struct VelBulkPlan<1024> { static constexpr bool ok = true; static constexpr int P = 16, RW = 2, MINB = 4; using R = Radices<16, 16, 4>; };
+
+template <int M>
+static bool row_vel_bulk(const DevCfg &c, const RowIn &in, const float2 *twN, const float2 *twM, float scale,
+                         float *vr, cudaStream_t st, cudaError_t &e)
+{
+  if constexpr (!VelBulkPlan<M>::ok) {
+    return false;
+  } else {
+    using PL = VelBulkPlan<M>;
+    if (c.col_variant != 0) return false;
+    for (int k = 0; k < 3; k++)
+      if (reinterpret_cast<uintptr_t>(in.main[k]) & 15) return false;
+    constexpr int threads = PL::RW * (M / PL::P);
+    const size_t sm = sizeof(float2) * 3 * PL::RW * sm_len<M, true>() + 128;
+    auto kern = row_vel_bulk_kernel<M, PL::P, PL::RW, PL::MINB, typename PL::R>;
+    static int bps = 0;
+    if (!bps) {
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, threads, sm);
+      if (e != cudaSuccess) return true;
+      if (bps < 1) {
+        e = cudaErrorInvalidConfiguration;
+        return true;
+      }
+    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long ngroups = (long)c.n * c.n / PL::RW;
+    const long grid = ngroups < (long)sms * bps ? ngroups : (long)sms * bps;
+    kern<<<(unsigned)grid, threads, sm, st>>>(c, in, ngroups, twN, twM, scale, vr, c.tc_err);
+    e = cudaGetLastError();
+    return true;
+  }
+}
+
 long row_pass_blocks(int n)
 {
   long nrows = (long)n * n;
@@ -766,6 +893,9 @@ cudaError_t col_pass(const DevCfg &c, const ColGeom &g, int nyq, int mode, int n
 cudaError_t row_pass(const DevCfg &c, const RowIn &in, const float2 *twN, const float2 *twM, float scale, int epi,
                      float *vr, double2 *partials, cudaStream_t st)
 {
+  cudaError_t be = cudaSuccess;
+  if (epi == 2 && c.m == 512 && row_vel_bulk<512>(c, in, twN, twM, scale, vr, st, be)) return be;
+  if (epi == 2 && c.m == 1024 && row_vel_bulk<1024>(c, in, twN, twM, scale, vr, st, be)) return be;
   switch (epi) {
     case 0: GETHI_ROW_DISPATCH(0, RowPlan)
     case 2: GETHI_ROW_DISPATCH(2, RowPlanV)
