@@ -509,6 +509,106 @@ __global__ void __launch_bounds__(RW *(M / P), MINB)
   if (stop && tid == 0) tc::mbar_wait(&bar, phase, kTmaWaitNs);
 }
 
+// ---------------------------------------------------------------------------
+// Density X pass, persistent, rows staged by bulk copies (as the v_r pass): the
+// real row is written back in place, and each thread's FP32 sums of delta and
+// delta^2 (Neumaier-compensated, src/fourier.c:43-54) run over all its groups.
+// Block b writes partials[b] and zeroes partials[b + k gridDim.x] < npartials,
+// the entries of the launch shape that had one block per row group.
+// ---------------------------------------------------------------------------
+template <int M, int P, int RW, int MINB, class Rad>
+__global__ void __launch_bounds__(RW *(M / P), MINB)
+    row_den_bulk_kernel(DevCfg c, float2 *main, const float2 *__restrict__ nyq, long ngroups,
+                        const float2 *__restrict__ twN, const float2 *__restrict__ twM, float scale,
+                        double2 *partials, long npartials, int *err)
+{
+  constexpr int T = M / P, RL = radix_last(Rad{}), SL = sm_len<M, true>();
+  constexpr uint32_t kRowBytes = M * sizeof(float2);
+  extern __shared__ float2 smem_raw[];  // [row of the group][SL], from a 128-byte boundary
+  float2 *smem = smem_raw + ((128u - (tc::smem_addr(smem_raw) & 127u)) & 127u) / sizeof(float2);
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int stop;
+  __shared__ float red[4][32];
+  const int tid = threadIdx.x, rl = tid / T, t = tid % T;
+  auto issue = [&](long g) {
+    tc::mbar_arrive_expect_tx(&bar, RW * kRowBytes);
+#pragma unroll
+    for (int r = 0; r < RW; r++) tc::bulk_g2s(smem + r * SL, main + (g * RW + r) * (long)M, kRowBytes, &bar);
+  };
+  if (tid == 0) {
+    tc::mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    stop = 0;
+    if ((long)blockIdx.x < ngroups) issue(blockIdx.x);
+  }
+  __syncthreads();
+  uint32_t phase = 0;
+  float2 *srow = smem + rl * SL;
+  float a1 = 0.f, c1 = 0.f, a2 = 0.f, c2 = 0.f;
+  auto nsum = [](float &acc, float &comp, float val) {
+    float s = acc + val;
+    comp += fabsf(acc) >= fabsf(val) ? (acc - s) + val : (val - s) + acc;
+    acc = s;
+  };
+  for (long g = blockIdx.x; g < ngroups; g += gridDim.x) {
+    const long row = g * RW + rl;
+    const float2 xm = nyq[row];
+    if (tid == 0 && !tc::mbar_wait(&bar, phase, kTmaWaitNs)) {
+      if (err) atomicExch(err, 1);
+      stop = 1;
+    }
+    __syncthreads();
+    if (stop) break;
+    phase ^= 1u;
+    float2 v[P];
+    row_c2r_smem<M, P, Rad, false>(v, srow, xm, t, twN, twM);
+    float2 *grow = main + row * (long)M;
+#pragma unroll
+    for (int j = 0; j < P / RL; j++)
+#pragma unroll
+      for (int r = 0; r < RL; r++) {
+        const int e = t + T * j + (M / RL) * r;
+        const float2 x = cscale(v[j * RL + r], scale);
+        grow[e] = x;
+        nsum(a1, c1, x.x);
+        nsum(a1, c1, x.y);
+        nsum(a2, c2, x.x * x.x);  // float squares, src/fourier.c:51
+        nsum(a2, c2, x.y * x.y);
+      }
+    tc::fence_proxy_async();  // this group's accesses before the copies that refill the buffers
+    __syncthreads();
+    if (tid == 0 && g + (long)gridDim.x < ngroups) issue(g + gridDim.x);
+  }
+  if (stop && tid == 0) tc::mbar_wait(&bar, phase, kTmaWaitNs);
+  // warp reduction in double-float, FP64 for the block's sum
+  df s1 = two_sum(a1, c1), s2 = two_sum(a2, c2);
+  for (int o = 16; o > 0; o >>= 1) {
+    const df t1 = {__shfl_xor_sync(0xffffffffu, s1.hi, o), __shfl_xor_sync(0xffffffffu, s1.lo, o)};
+    const df t2 = {__shfl_xor_sync(0xffffffffu, s2.hi, o), __shfl_xor_sync(0xffffffffu, s2.lo, o)};
+    s1 = df_add(s1, t1);
+    s2 = df_add(s2, t2);
+  }
+  const int w = tid >> 5, lane = tid & 31, nw = (RW * T + 31) >> 5;
+  __syncthreads();
+  if (lane == 0) {
+    red[0][w] = s1.hi;
+    red[1][w] = s1.lo;
+    red[2][w] = s2.hi;
+    red[3][w] = s2.lo;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double a = 0, b = 0;
+    for (int i = 0; i < nw; i++) {
+      a += (double)red[0][i] + (double)red[1][i];
+      b += (double)red[2][i] + (double)red[3][i];
+    }
+    partials[blockIdx.x] = make_double2(a, b);
+  }
+  for (long i = blockIdx.x + (long)gridDim.x * (1 + tid); i < npartials; i += (long)gridDim.x * blockDim.x)
+    partials[i] = make_double2(0.0, 0.0);
+}
+
 // Kahan-compensated FP64 sum of the per-block partials -> stats = (mean, sigma^2)
 __global__ void finish_sigma_kernel(const double2 *__restrict__ partials, int np, double ncells, double *stats)
 {
@@ -825,6 +925,46 @@ static bool row_vel_bulk(const DevCfg &c, const RowIn &in, const float2 *twN, co
   }
 }
 
+// persistent bulk-copy density X pass
+template <int M> struct DenBulkPlan { static constexpr bool ok = false; };
+template <> struct DenBulkPlan<512> { static constexpr bool ok = true; static constexpr int P = 16, RW = 4, MINB = 8; using R = Radices<16, 16, 2>; };
+template <> struct DenBulkPlan<1024> { static constexpr bool ok = true; static constexpr int P = 16, RW = 2, MINB = 8; using R = Radices<16, 16, 4>; };
+
+template <int M>
+static bool row_den_bulk(const DevCfg &c, const RowIn &in, const float2 *twN, const float2 *twM, float scale,
+                         double2 *partials, long npartials, cudaStream_t st, cudaError_t &e)
+{
+  if constexpr (!DenBulkPlan<M>::ok) {
+    return false;
+  } else {
+    using PL = DenBulkPlan<M>;
+    if (c.col_variant != 0 || !partials || (reinterpret_cast<uintptr_t>(in.main[0]) & 15)) return false;
+    constexpr int threads = PL::RW * (M / PL::P);
+    const size_t sm = sizeof(float2) * PL::RW * sm_len<M, true>() + 128;
+    auto kern = row_den_bulk_kernel<M, PL::P, PL::RW, PL::MINB, typename PL::R>;
+    static int bps = 0;
+    if (!bps) {
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, threads, sm);
+      if (e != cudaSuccess) return true;
+      if (bps < 1) {
+        e = cudaErrorInvalidConfiguration;
+        return true;
+      }
+    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long ngroups = (long)c.n * c.n / PL::RW;
+    long grid = ngroups < (long)sms * bps ? ngroups : (long)sms * bps;
+    grid = grid < npartials ? grid : npartials;
+    kern<<<(unsigned)grid, threads, sm, st>>>(c, in.main[0], in.nyq[0], ngroups, twN, twM, scale, partials,
+                                              npartials, c.tc_err);
+    e = cudaGetLastError();
+    return true;
+  }
+}
+
 long row_pass_blocks(int n)
 {
   long nrows = (long)n * n;
@@ -894,6 +1034,9 @@ cudaError_t row_pass(const DevCfg &c, const RowIn &in, const float2 *twN, const 
                      float *vr, double2 *partials, cudaStream_t st)
 {
   cudaError_t be = cudaSuccess;
+  const long np = row_pass_blocks(c.n);
+  if (epi == 0 && c.m == 512 && row_den_bulk<512>(c, in, twN, twM, scale, partials, np, st, be)) return be;
+  if (epi == 0 && c.m == 1024 && row_den_bulk<1024>(c, in, twN, twM, scale, partials, np, st, be)) return be;
   if (epi == 2 && c.m == 512 && row_vel_bulk<512>(c, in, twN, twM, scale, vr, st, be)) return be;
   if (epi == 2 && c.m == 1024 && row_vel_bulk<1024>(c, in, twN, twM, scale, vr, st, be)) return be;
   switch (epi) {

@@ -294,22 +294,26 @@ def test_c1_shaped_run_vs_oracle(gh):
     np.testing.assert_allclose(vmaps, ref, rtol=1e-5, atol=1e-6 * np.abs(ref).max())
 
 
-def test_tma_column_passes_bit_identical(gh):
-    """The Y passes of 512-point columns run from TMA-staged tiles by default; the
-    same Philox realisation with the tiles loaded through registers
-    (gethi_gpu_set_launch col_variant=2) gives the same delta bit for bit and the
-    same v_r to FP32 rounding (the compiler fuses the velocity factors' products
-    into FMAs differently in the two kernels)."""
+def test_tma_and_bulk_passes_match_register_passes(gh):
+    """At 512^3 the Y passes run from TMA-staged tiles and the X passes from
+    bulk-copied rows by default; the same Philox realisation with every pass
+    loading through registers (gethi_gpu_set_launch col_variant=2) gives the same
+    delta, v_r and sigma^2 to FP32 rounding (the compiler fuses products into
+    FMAs differently in the kernels)."""
     nu21 = 1420.40575177
     n = 512
     ctx = gh.GetHI(synthetic_params(gh, n_grid=n, n_side=64, l_box=2500.0, nu_min=nu21 / 3.0, nu_max=nu21 / 1.3,
                                     n_nu=8, velocity_mode="spectral", seed=77))
     ctx.create_d_and_vr_fields()
     d_tma, v_tma = ctx.grids()
+    s_tma = ctx.derived().sigma2_gauss
     ctx.set_launch(0, 2)
     ctx.create_d_and_vr_fields()
     d_reg, v_reg = ctx.grids()
+    s_reg = ctx.derived().sigma2_gauss
     ctx.free()
     assert np.isfinite(d_tma).all() and np.abs(d_tma).max() > 0
-    np.testing.assert_array_equal(d_tma, d_reg)
-    assert rel_l2(v_tma, v_reg) < 1e-6  # each is ~2e-7 from FP64; the FFT bound against FP64 is 2e-6
+    # each path is ~2e-7 from FP64; the FFT bound against FP64 is 2e-6
+    assert rel_l2(d_tma, d_reg) < 1e-6
+    assert rel_l2(v_tma, v_reg) < 1e-6
+    assert abs(s_tma - s_reg) < 1e-6 * s_reg
