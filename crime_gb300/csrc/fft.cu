@@ -887,6 +887,7 @@ static cudaError_t launch_row(const DevCfg &c, const RowIn &in, const float2 *tw
 
 // persistent bulk-copy v_r X pass: plans per row length (N/2 complex points)
 template <int M> struct VelBulkPlan { static constexpr bool ok = false; };
+template <> struct VelBulkPlan<256> { static constexpr bool ok = true; static constexpr int P = 16, RW = 8, MINB = 4; using R = Radices<16, 16>; };
 template <> struct VelBulkPlan<512> { static constexpr bool ok = true; static constexpr int P = 16, RW = 4, MINB = 4; using R = Radices<16, 16, 2>; };
 template <> struct VelBulkPlan<1024> { static constexpr bool ok = true; static constexpr int P = 16, RW = 2, MINB = 4; using R = Radices<16, 16, 4>; };
 
@@ -927,6 +928,7 @@ static bool row_vel_bulk(const DevCfg &c, const RowIn &in, const float2 *twN, co
 
 // persistent bulk-copy density X pass
 template <int M> struct DenBulkPlan { static constexpr bool ok = false; };
+template <> struct DenBulkPlan<256> { static constexpr bool ok = true; static constexpr int P = 16, RW = 8, MINB = 8; using R = Radices<16, 16>; };
 template <> struct DenBulkPlan<512> { static constexpr bool ok = true; static constexpr int P = 16, RW = 4, MINB = 8; using R = Radices<16, 16, 2>; };
 template <> struct DenBulkPlan<1024> { static constexpr bool ok = true; static constexpr int P = 16, RW = 2, MINB = 8; using R = Radices<16, 16, 4>; };
 
@@ -1035,8 +1037,10 @@ cudaError_t row_pass(const DevCfg &c, const RowIn &in, const float2 *twN, const 
 {
   cudaError_t be = cudaSuccess;
   const long np = row_pass_blocks(c.n);
+  if (epi == 0 && c.m == 256 && row_den_bulk<256>(c, in, twN, twM, scale, partials, np, st, be)) return be;
   if (epi == 0 && c.m == 512 && row_den_bulk<512>(c, in, twN, twM, scale, partials, np, st, be)) return be;
   if (epi == 0 && c.m == 1024 && row_den_bulk<1024>(c, in, twN, twM, scale, partials, np, st, be)) return be;
+  if (epi == 2 && c.m == 256 && row_vel_bulk<256>(c, in, twN, twM, scale, vr, st, be)) return be;
   if (epi == 2 && c.m == 512 && row_vel_bulk<512>(c, in, twN, twM, scale, vr, st, be)) return be;
   if (epi == 2 && c.m == 1024 && row_vel_bulk<1024>(c, in, twN, twM, scale, vr, st, be)) return be;
   switch (epi) {
