@@ -446,9 +446,12 @@ __global__ void __launch_bounds__(RW *(M / P), EPI == 2 ? 512 / (RW * (M / P)) :
 // of RW rows; one thread copies the group's three component rows (RW x 3 copies
 // of N/2 complex, cp.async.bulk completing on one mbarrier) into natural-order
 // slots of the skewed row buffers, which the c2r's Stockham exchanges then use.
-// Once a group is stored the buffers are refilled with the CTA's next group;
-// the other CTAs on the SM cover that wait.  Waits are bounded by 1 s of the
-// global timer (on expiry: *err raised, copies in flight awaited, stop).
+// Along a row y and z are constant and the c2r is linear, so the y and z terms
+// of v . (x - x_obs) are combined in the spectrum, W = y V_y + z V_z, and a row
+// takes two transforms (V_x and W) instead of three.  Once a group is stored the
+// buffers are refilled with the CTA's next group; the other CTAs on the SM cover
+// that wait.  Waits are bounded by 1 s of the global timer (on expiry: *err
+// raised, copies in flight awaited, stop).
 // ---------------------------------------------------------------------------
 template <int M, int P, int RW, int MINB, class Rad>
 __global__ void __launch_bounds__(RW *(M / P), MINB)
@@ -496,11 +499,20 @@ __global__ void __launch_bounds__(RW *(M / P), MINB)
     float2 v[P], acc[P];
     const int iy = (int)(row % c.n), iz = (int)(row / c.n);
     const float y = c.dxf * (iy + 0.5f) - c.pos_obsf, z = c.dxf * (iz + 0.5f) - c.pos_obsf;
-#pragma unroll 1
-    for (int comp = 0; comp < 3; comp++) {
-      row_c2r_smem<M, P, Rad, false>(v, sr[comp], xm[comp], t, twN, twM);
-      vr_accumulate<M, P, RL>(c, comp, v, acc, t, y, z);
+    // W = y V_y + z V_z into the V_y buffer (natural order), Nyquist terms likewise
+#pragma unroll
+    for (int j = 0; j < P; j++) {
+      const int k = t + T * j;
+      const float2 a = sr[1][k], b = sr[2][k];
+      sr[1][k] = make_float2(fmaf(y, a.x, z * b.x), fmaf(y, a.y, z * b.y));
     }
+    const float2 xmw = make_float2(fmaf(y, xm[1].x, z * xm[2].x), fmaf(y, xm[1].y, z * xm[2].y));
+    __syncthreads();
+    row_c2r_smem<M, P, Rad, false>(v, sr[0], xm[0], t, twN, twM);
+    vr_accumulate<M, P, RL>(c, 0, v, acc, t, y, z);
+    row_c2r_smem<M, P, Rad, false>(v, sr[1], xmw, t, twN, twM);
+#pragma unroll
+    for (int i = 0; i < P; i++) acc[i] = make_float2(acc[i].x + v[i].x, acc[i].y + v[i].y);
     vr_store<M, P, RL>(c, acc, vr + row * (long)c.n, t, y, z, scale);
     tc::fence_proxy_async();  // this group's accesses before the copies that refill the buffers
     __syncthreads();
