@@ -803,6 +803,7 @@ template <int L> struct TmaPlan { static constexpr bool ok = false; };
 // the transform of a 64 KB tile outlasts its load, so the second CTA's
 // transform is what hides the first one's copies.
 template <> struct TmaPlan<1024> { static constexpr bool ok = true; static constexpr int P = 32, TX = 8, MINB = 2, NBUF = 1; using R = Radices<32, 32>; };
+template <> struct TmaPlan<256> { static constexpr bool ok = true; static constexpr int P = 16, TX = 8, MINB = 4, NBUF = 1; using R = Radices<16, 16>; };
 template <> struct TmaPlan<512> { static constexpr bool ok = true; static constexpr int P = 32, TX = 8, MINB = 4, NBUF = 1; using R = Radices<32, 16>; };
 
 static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
@@ -899,6 +900,7 @@ static cudaError_t launch_row(const DevCfg &c, const RowIn &in, const float2 *tw
 
 // persistent bulk-copy v_r X pass: plans per row length (N/2 complex points)
 template <int M> struct VelBulkPlan { static constexpr bool ok = false; };
+template <> struct VelBulkPlan<128> { static constexpr bool ok = true; static constexpr int P = 16, RW = 16, MINB = 4; using R = Radices<16, 8>; };
 template <> struct VelBulkPlan<256> { static constexpr bool ok = true; static constexpr int P = 16, RW = 8, MINB = 4; using R = Radices<16, 16>; };
 template <> struct VelBulkPlan<512> { static constexpr bool ok = true; static constexpr int P = 16, RW = 4, MINB = 4; using R = Radices<16, 16, 2>; };
 template <> struct VelBulkPlan<1024> { static constexpr bool ok = true; static constexpr int P = 16, RW = 2, MINB = 4; using R = Radices<16, 16, 4>; };
@@ -940,6 +942,7 @@ static bool row_vel_bulk(const DevCfg &c, const RowIn &in, const float2 *twN, co
 
 // persistent bulk-copy density X pass
 template <int M> struct DenBulkPlan { static constexpr bool ok = false; };
+template <> struct DenBulkPlan<128> { static constexpr bool ok = true; static constexpr int P = 16, RW = 16, MINB = 8; using R = Radices<16, 8>; };
 template <> struct DenBulkPlan<256> { static constexpr bool ok = true; static constexpr int P = 16, RW = 8, MINB = 8; using R = Radices<16, 16>; };
 template <> struct DenBulkPlan<512> { static constexpr bool ok = true; static constexpr int P = 16, RW = 4, MINB = 8; using R = Radices<16, 16, 2>; };
 template <> struct DenBulkPlan<1024> { static constexpr bool ok = true; static constexpr int P = 16, RW = 2, MINB = 8; using R = Radices<16, 16, 4>; };
@@ -1024,6 +1027,7 @@ cudaError_t col_pass(const DevCfg &c, const ColGeom &g, int nyq, int mode, int n
   cudaError_t te = cudaSuccess;
   if (c.n == 1024 && col_tma<1024>(c, g, nyq, mode, tw, out1, st, te)) return te;
   if (c.n == 512 && col_tma<512>(c, g, nyq, mode, tw, out1, st, te)) return te;
+  if (c.n == 256 && col_tma<256>(c, g, nyq, mode, tw, out1, st, te)) return te;
   switch (mode) {
     case 0: GETHI_COL_DISPATCH(0)
     case 1: GETHI_COL_DISPATCH(1)
@@ -1049,9 +1053,11 @@ cudaError_t row_pass(const DevCfg &c, const RowIn &in, const float2 *twN, const 
 {
   cudaError_t be = cudaSuccess;
   const long np = row_pass_blocks(c.n);
+  if (epi == 0 && c.m == 128 && row_den_bulk<128>(c, in, twN, twM, scale, partials, np, st, be)) return be;
   if (epi == 0 && c.m == 256 && row_den_bulk<256>(c, in, twN, twM, scale, partials, np, st, be)) return be;
   if (epi == 0 && c.m == 512 && row_den_bulk<512>(c, in, twN, twM, scale, partials, np, st, be)) return be;
   if (epi == 0 && c.m == 1024 && row_den_bulk<1024>(c, in, twN, twM, scale, partials, np, st, be)) return be;
+  if (epi == 2 && c.m == 128 && row_vel_bulk<128>(c, in, twN, twM, scale, vr, st, be)) return be;
   if (epi == 2 && c.m == 256 && row_vel_bulk<256>(c, in, twN, twM, scale, vr, st, be)) return be;
   if (epi == 2 && c.m == 512 && row_vel_bulk<512>(c, in, twN, twM, scale, vr, st, be)) return be;
   if (epi == 2 && c.m == 1024 && row_vel_bulk<1024>(c, in, twN, twM, scale, vr, st, be)) return be;
