@@ -902,7 +902,7 @@ static cudaError_t launch_row(const DevCfg &c, const RowIn &in, const float2 *tw
 template <int M> struct VelBulkPlan { static constexpr bool ok = false; };
 template <> struct VelBulkPlan<128> { static constexpr bool ok = true; static constexpr int P = 16, RW = 16, MINB = 4; using R = Radices<16, 8>; };
 template <> struct VelBulkPlan<256> { static constexpr bool ok = true; static constexpr int P = 16, RW = 8, MINB = 4; using R = Radices<16, 16>; };
-template <> struct VelBulkPlan<512> { static constexpr bool ok = true; static constexpr int P = 16, RW = 4, MINB = 4; using R = Radices<16, 16, 2>; };
+template <> struct VelBulkPlan<512> { static constexpr bool ok = true; static constexpr int P = 32, RW = 4, MINB = 4; using R = Radices<32, 16>; };
 template <> struct VelBulkPlan<1024> { static constexpr bool ok = true; static constexpr int P = 16, RW = 2, MINB = 4; using R = Radices<16, 16, 4>; };
 
 template <int M>
@@ -944,7 +944,7 @@ static bool row_vel_bulk(const DevCfg &c, const RowIn &in, const float2 *twN, co
 template <int M> struct DenBulkPlan { static constexpr bool ok = false; };
 template <> struct DenBulkPlan<128> { static constexpr bool ok = true; static constexpr int P = 16, RW = 16, MINB = 8; using R = Radices<16, 8>; };
 template <> struct DenBulkPlan<256> { static constexpr bool ok = true; static constexpr int P = 16, RW = 8, MINB = 8; using R = Radices<16, 16>; };
-template <> struct DenBulkPlan<512> { static constexpr bool ok = true; static constexpr int P = 16, RW = 4, MINB = 8; using R = Radices<16, 16, 2>; };
+template <> struct DenBulkPlan<512> { static constexpr bool ok = true; static constexpr int P = 32, RW = 4, MINB = 8; using R = Radices<32, 16>; };
 template <> struct DenBulkPlan<1024> { static constexpr bool ok = true; static constexpr int P = 16, RW = 2, MINB = 8; using R = Radices<16, 16, 4>; };
 
 template <int M>
