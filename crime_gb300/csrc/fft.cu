@@ -898,12 +898,15 @@ static cudaError_t launch_row(const DevCfg &c, const RowIn &in, const float2 *tw
   return cudaGetLastError();
 }
 
-// persistent bulk-copy v_r X pass: plans per row length (N/2 complex points)
+// persistent bulk-copy v_r X pass: plans per row length (N/2 complex points).
+// 32 points per thread won at 512- and 1024-point rows (1024^3: v_r 4.20 -> 3.60 ms,
+// density 1.86 -> 1.69 ms; 2048^3: 39.0 -> 32.9 and 17.4 -> 15.2 ms) and lost at
+// 256-point rows (512^3: 0.39 -> 0.51 and 0.20 -> 0.23 ms)
 template <int M> struct VelBulkPlan { static constexpr bool ok = false; };
 template <> struct VelBulkPlan<128> { static constexpr bool ok = true; static constexpr int P = 16, RW = 16, MINB = 4; using R = Radices<16, 8>; };
 template <> struct VelBulkPlan<256> { static constexpr bool ok = true; static constexpr int P = 16, RW = 8, MINB = 4; using R = Radices<16, 16>; };
 template <> struct VelBulkPlan<512> { static constexpr bool ok = true; static constexpr int P = 32, RW = 4, MINB = 4; using R = Radices<32, 16>; };
-template <> struct VelBulkPlan<1024> { static constexpr bool ok = true; static constexpr int P = 16, RW = 2, MINB = 4; using R = Radices<16, 16, 4>; };
+template <> struct VelBulkPlan<1024> { static constexpr bool ok = true; static constexpr int P = 32, RW = 2, MINB = 4; using R = Radices<32, 32>; };
 
 template <int M>
 static bool row_vel_bulk(const DevCfg &c, const RowIn &in, const float2 *twN, const float2 *twM, float scale,
@@ -945,7 +948,7 @@ template <int M> struct DenBulkPlan { static constexpr bool ok = false; };
 template <> struct DenBulkPlan<128> { static constexpr bool ok = true; static constexpr int P = 16, RW = 16, MINB = 8; using R = Radices<16, 8>; };
 template <> struct DenBulkPlan<256> { static constexpr bool ok = true; static constexpr int P = 16, RW = 8, MINB = 8; using R = Radices<16, 16>; };
 template <> struct DenBulkPlan<512> { static constexpr bool ok = true; static constexpr int P = 32, RW = 4, MINB = 8; using R = Radices<32, 16>; };
-template <> struct DenBulkPlan<1024> { static constexpr bool ok = true; static constexpr int P = 16, RW = 2, MINB = 8; using R = Radices<16, 16, 4>; };
+template <> struct DenBulkPlan<1024> { static constexpr bool ok = true; static constexpr int P = 32, RW = 2, MINB = 8; using R = Radices<32, 32>; };
 
 template <int M>
 static bool row_den_bulk(const DevCfg &c, const RowIn &in, const float2 *twN, const float2 *twM, float scale,
