@@ -806,20 +806,18 @@ template <> struct TmaPlan<1024> { static constexpr bool ok = true; static const
 template <> struct TmaPlan<256> { static constexpr bool ok = true; static constexpr int P = 16, TX = 8, MINB = 4, NBUF = 1; using R = Radices<16, 16>; };
 template <> struct TmaPlan<512> { static constexpr bool ok = true; static constexpr int P = 32, TX = 8, MINB = 4, NBUF = 1; using R = Radices<32, 16>; };
 
+// the driver's tensor-map encoder, looked up once (thread-safe static initialisation)
 static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
     cudaDriverEntryPointQueryResult q;
     void *p = nullptr;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    else
-      cudaGetLastError();
-  }
+      return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    cudaGetLastError();
+    return nullptr;
+  }();
   return fn;
 }
 
