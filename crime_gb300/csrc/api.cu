@@ -74,6 +74,20 @@ struct gethi_ctx {
 
 namespace {
 
+// FP32 tables, NZ entries each: z(r), density growth, velocity growth, and the
+// projection's line table (slope, deviation bound)
+constexpr int kTabF = 5;
+
+void line_table(const Setup &s, float *out)
+{
+  const double dx = s.d.l_box / s.p.n_grid, rho = subsample_radius(s.xs, s.ys, s.zs, dx);
+  for (int i = 0; i < NZ; i++) {
+    const float2 v = shell_line_entry(s.z_r2z.data(), s.d.glob_idr, dx, rho, i);
+    out[i] = v.x;
+    out[NZ + i] = v.y;
+  }
+}
+
 int cuda_fail(cudaError_t e, const char *what)
 {
   set_error(std::string(what) + ": " + cudaGetErrorString(e));
@@ -141,6 +155,8 @@ void fill_cfg(gethi_ctx *c)
   g.z_r2z_f = c->tab_f;
   g.gd_f = c->tab_f + NZ;
   g.gv_f = c->tab_f + 2 * NZ;
+  g.z_lin_g = c->tab_f + 3 * NZ;
+  g.z_lin_e = c->tab_f + 4 * NZ;
   g.glob_idr = s.d.glob_idr;
   g.glob_idr_f = (float)s.d.glob_idr;
   g.r_tab_max = s.r_r2z[NZ - 1];
@@ -436,7 +452,7 @@ extern "C" int gethi_gpu_init(const gethi_params *p, int device, gethi_ctx **out
       (rc = dalloc(&c->twN, (size_t)n)) || (rc = dalloc(&c->twM, (size_t)m)) ||
       (rc = dalloc(&c->partials, (size_t)c->npartials)) || (rc = dalloc(&c->stats, 4)) ||
       (rc = dalloc(&c->pk_f, (size_t)s.d.numk)) || (rc = dalloc(&c->logk_f, (size_t)s.d.numk)) ||
-      (rc = dalloc(&c->tab_f, (size_t)3 * NZ)) || (rc = dalloc(&c->tab_d, (size_t)4 * NZ)) ||
+      (rc = dalloc(&c->tab_f, (size_t)kTabF * NZ)) || (rc = dalloc(&c->tab_d, (size_t)4 * NZ)) ||
       (rc = dalloc(&c->prefac, (size_t)s.p.n_nu)) || (rc = dalloc(&c->edges_f, (size_t)s.p.n_nu + 1)) ||
       (rc = dalloc(&c->edges_d, (size_t)s.p.n_nu + 1)) || (rc = dalloc(&c->counters, 16))) {
     gethi_gpu_free(c);
@@ -514,7 +530,7 @@ extern "C" int gethi_gpu_init(const gethi_params *p, int device, gethi_ctx **out
   for (int i = 0; i < s.d.numk; i++) f[i] = (float)s.logk[i];
   cudaMemcpy(c->logk_f, f.data(), sizeof(float) * s.d.numk, cudaMemcpyHostToDevice);
   std::vector<double> td(4 * NZ);
-  std::vector<float> tf(3 * NZ);
+  std::vector<float> tf(kTabF * NZ);
   for (int i = 0; i < NZ; i++) {
     td[i] = s.z_r2z[i];
     td[NZ + i] = s.r_r2z[i];
@@ -524,8 +540,9 @@ extern "C" int gethi_gpu_init(const gethi_params *p, int device, gethi_ctx **out
     tf[NZ + i] = (float)s.gd[i];
     tf[2 * NZ + i] = (float)s.gv[i];
   }
+  line_table(s, tf.data() + 3 * NZ);
   cudaMemcpy(c->tab_d, td.data(), sizeof(double) * 4 * NZ, cudaMemcpyHostToDevice);
-  cudaMemcpy(c->tab_f, tf.data(), sizeof(float) * 3 * NZ, cudaMemcpyHostToDevice);
+  cudaMemcpy(c->tab_f, tf.data(), sizeof(float) * kTabF * NZ, cudaMemcpyHostToDevice);
   std::vector<double> ed(s.p.n_nu + 1);
   std::vector<float> ef(s.p.n_nu + 1), pf(s.p.n_nu);
   for (int i = 0; i < s.p.n_nu; i++) {
@@ -1247,7 +1264,7 @@ extern "C" long gethi_gpu_upload_inputs(gethi_ctx *c)
   if (!c) return GETHI_E_ARG;
   const Setup &s = c->s;
   const int nk = s.d.numk, nn = s.p.n_nu;
-  size_t bytes = sizeof(float) * (2 * nk + 3 * NZ + nn + nn + 1) + sizeof(double) * (4 * NZ + nn + 1);
+  size_t bytes = sizeof(float) * (2 * nk + kTabF * NZ + nn + nn + 1) + sizeof(double) * (4 * NZ + nn + 1);
   if (!c->staging) {
     if (cudaHostAlloc(&c->staging, bytes, cudaHostAllocDefault) != cudaSuccess) {
       c->staging = nullptr;
@@ -1274,7 +1291,8 @@ extern "C" long gethi_gpu_upload_inputs(gethi_ctx *c)
       tf[NZ + i] = (float)s.gd[i];
       tf[2 * NZ + i] = (float)s.gv[i];
     }
-    float *pf = tf + 3 * NZ;
+    line_table(s, tf + 3 * NZ);
+    float *pf = tf + kTabF * NZ;
     for (int i = 0; i < nn; i++) pf[i] = (float)s.prefac[i];
     float *ef = pf + nn;
     for (int i = 0; i <= nn; i++) ef[i] = (float)ed[i];
@@ -1282,12 +1300,12 @@ extern "C" long gethi_gpu_upload_inputs(gethi_ctx *c)
   cudaStream_t st = c->stream;
   char *p = (char *)c->staging;
   double *td = (double *)p, *ed = td + 4 * NZ;
-  float *f = (float *)(ed + nn + 1), *tf = f + 2 * nk, *pf = tf + 3 * NZ, *ef = pf + nn;
+  float *f = (float *)(ed + nn + 1), *tf = f + 2 * nk, *pf = tf + kTabF * NZ, *ef = pf + nn;
   CK(cudaMemcpyAsync(c->tab_d, td, sizeof(double) * 4 * NZ, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(c->edges_d, ed, sizeof(double) * (nn + 1), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(c->pk_f, f, sizeof(float) * nk, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(c->logk_f, f + nk, sizeof(float) * nk, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(c->tab_f, tf, sizeof(float) * 3 * NZ, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->tab_f, tf, sizeof(float) * kTabF * NZ, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(c->prefac, pf, sizeof(float) * nn, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(c->edges_f, ef, sizeof(float) * (nn + 1), cudaMemcpyHostToDevice, st));
   return (long)bytes;

@@ -264,6 +264,10 @@ struct DevCfg {
   const float *z_r2z_f, *gd_f, *gv_f;
   double glob_idr, r_tab_max;
   float glob_idr_f, r_tab_max_f;
+  // per table interval i (shell_line_entry): the slope dz/dR per cell and the
+  // largest distance of z(R) from that interval's line within a sub-sample
+  // radius of the interval
+  const float *z_lin_g, *z_lin_e;
   // shells and pixels
   int n_nu, regular_nu;
   long nside, npix;

@@ -79,6 +79,11 @@ cudaError_t project(const DevCfg &c, const double *stats, const float *a, const 
                     int *counters, void *fq, long fq_cap, cudaStream_t st);
 cudaError_t fixup(const DevCfg &c, const void *fq, const int *counters, long fq_cap, float *maps, cudaStream_t st);
 long fallback_queue_capacity(int n);
+// largest distance of a sub-sample from its cell centre, in cells
+double subsample_radius(const double *xs, const double *ys, const double *zs, double dx);
+// entry i of DevCfg::z_lin_g / z_lin_e for the FP64 redshift table z_r2z[kNZ],
+// cell size dx and sub-sample radius rho (cells)
+float2 shell_line_entry(const double *z_r2z, double glob_idr, double dx, double rho, int i);
 size_t fallback_entry_bytes();
 cudaError_t scale_maps(const DevCfg &c, float *maps, cudaStream_t st);
 cudaError_t sample_keys(const DevCfg &c, const float *dz, uint32_t *keys, int exact, int *counters,

@@ -30,7 +30,7 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_queue[kQueueEntries * 16];
 static __device__ __align__(256) int g_counters[16];
 static __device__ __align__(256) double g_tab_d[4 * kNZ];
-static __device__ __align__(256) float g_tab_f[3 * kNZ];
+static __device__ __align__(256) float g_tab_f[5 * kNZ];  // z, growth d, growth v, line slope, line bound
 static __device__ __align__(256) double g_edges_d[kMaxNu + 1];
 static __device__ __align__(256) float g_edges_f[kMaxNu + 1];
 static __device__ __align__(256) float g_prefac[kMaxNu];
@@ -140,6 +140,24 @@ extern "C" int gethi_project_noalloc(const gethi_params *p, const gethi_derived 
   NA_CK(put_f(sc->tab_f, tables + 2 * NZ, NZ));
   NA_CK(put_f(sc->tab_f + NZ, tables + 4 * NZ, NZ));
   NA_CK(put_f(sc->tab_f + 2 * NZ, tables + 5 * NZ, NZ));
+  {  // the projection's line table: slopes, then deviation bounds
+    double ox[NSUB], oy[NSUB], oz[NSUB];
+    for (int i = 0; i < NSUB; i++) {
+      ox[i] = offsets[3 * i];
+      oy[i] = offsets[3 * i + 1];
+      oz[i] = offsets[3 * i + 2];
+    }
+    const double dxl = d->l_box / n, rho = subsample_radius(ox, oy, oz, dxl);
+    for (int half = 0; half < 2; half++)
+      for (int base = 0; base < NZ; base += kChunk) {
+        const int k = NZ - base < kChunk ? NZ - base : kChunk;
+        for (int i = 0; i < k; i++) {
+          const float2 v = shell_line_entry(tables + 2 * NZ, d->glob_idr, dxl, rho, base + i);
+          fb[i] = half ? v.y : v.x;
+        }
+        NA_CK(cudaMemcpyAsync(sc->tab_f + (3 + half) * NZ + base, fb, sizeof(float) * k, cudaMemcpyHostToDevice, st));
+      }
+  }
   for (int base = 0; base <= n_nu; base += kChunk) {  // shell edges, FP64 and FP32
     const int k = n_nu + 1 - base < kChunk ? n_nu + 1 - base : kChunk;
     for (int i = 0; i < k; i++)
@@ -165,6 +183,8 @@ extern "C" int gethi_project_noalloc(const gethi_params *p, const gethi_derived 
   g.z_r2z_f = sc->tab_f;
   g.gd_f = sc->tab_f + NZ;
   g.gv_f = sc->tab_f + 2 * NZ;
+  g.z_lin_g = sc->tab_f + 3 * NZ;
+  g.z_lin_e = sc->tab_f + 4 * NZ;
   g.glob_idr = d->glob_idr;
   g.glob_idr_f = (float)d->glob_idr;
   g.r_tab_max = tables[3 * NZ + NZ - 1];

@@ -288,6 +288,7 @@ __device__ __forceinline__ uint32_t key_resolve(const DevCfg &c, int ix, int iy,
 struct FastConst {
   float xsp[kNSUB], ysp[kNSUB], zsp[kNSUB];  // 0.5 + offset/dx
   float idr_cell;                             // glob_idr * dx
+  float rho, rho_idr;                         // sub-sample distance bound from the cell centre (cells), * idr_cell
   float half_n;                               // n/2
   float nu_min, inv_dnu;                      // regular table
   // the projection visits the sub-samples along a short path through the cell
@@ -342,73 +343,118 @@ __device__ __forceinline__ int edge_search(const float *ef, int nn, int log2nn, 
   return lo;
 }
 
-// The bins of a frequency file around a cell centre: bin lo of the centre's
-// frequency and the edges ef[lo-1] .. ef[lo+2] (-inf / +inf beyond 0..nn).  A
-// sub-sample within one bin of the centre's is then binned with four compares;
-// the search is left to samples two or more bins away.  (Regular tables bin by
-// one truncation and need none of this.)
-struct EdgeBracket {
+// The shell coordinate of a cell's sub-samples, linear in their radius.
+//
+// Within one cell the redshift shift dz is fixed and the sub-samples lie within
+// rho cells of the centre, so the shell coordinate u (the channel coordinate
+// t = (nu - nu_min)/dnu of a regular table, the frequency nu itself for a
+// frequency file) is set once per cell as
+//     u(R) = u_c + s (R - Rc),   |u(R) - u_exact(R)| < m,
+// and each sub-sample spends one subtraction and one FMA on it.  u_exact is the
+// FP64 key's value: u of 1 + z(R) + dz, z the piecewise-linear FP64 table
+// (src/cosmo.c:52-62).  s = du/dz g, with g the slope of the table interval
+// the centre falls in; z(R) stays within e of that interval's line for every R
+// a sub-sample of the cell can have (z_lin_g / z_lin_e, from the FP64 table).
+// The bound m is the per-sample budget above taken at the centre (whose radius
+// is correctly rounded: 1.8e-7), plus (each term x 1.5):
+//   radius rounding of the sub-sample and the centre: |s| (3.7e-7 (Rc + rho) + 1.8e-7 Rc)
+//     (R - Rc is exact: both lie within a factor 2 of each other);
+//   the table: |du/dz| e;
+//   the FP32 slope and the products forming s: 2e-6 |s| rho;
+//   curvature of u in z: |d2u/dz2| dZ^2/2 <= A sc dZ^2 / (1 + z + dz - dZ)^3,
+//     dZ = |g| rho + e the largest change of z over the cell;
+//   rounding of the FMA: 1.2e-7 (|u_c| + |s| rho).
+// Cells closer than 2 rho + 2 cells to the observer, or reaching the last table
+// interval, get m = inf: their sub-samples all go to the exact path.
+//
+// A frequency file also keeps the bins around the centre: bin lo of u_c and
+// the edges ef[lo-1] .. ef[lo+2] (-inf / +inf beyond 0..nn).  A sub-sample
+// within one bin of the centre's is binned with four compares; the search is
+// left to samples two or more bins away.
+struct CellShell {
+  float u, s, Rc, m;
   int lo;
   float e0, e1, e2, e3;
 };
 
-__device__ __forceinline__ EdgeBracket edge_bracket(const DevCfg &c, const FastConst &f, const float *ef, int log2nn,
-                                                    float Xc, float Yc, float Zc, float dz)
+__device__ __forceinline__ CellShell cell_shell(const DevCfg &c, const FastConst &f, const float *ef, int log2nn,
+                                                float Xc, float Yc, float Zc, float dz)
 {
-  EdgeBracket b{0, 0.f, 0.f, 0.f, 0.f};
-  if (c.regular_nu) return b;
-  // frequency of the cell centre (no certification needed: lo only picks the bracket)
+  constexpr float A = 1420.40575177f;
+  CellShell o;
+  // the centre: quarter-integer squares, so R2 is exact below 2^22 and rounded
+  // once above; sqrtf is correctly rounded (1.8e-7 covers both)
   const float X = Xc + 0.5f, Y = Yc + 0.5f, Z = Zc + 0.5f;
-  const float tr = fminf(sqrtf(fmaf(Z, Z, fmaf(Y, Y, X * X))) * f.idr_cell, (float)(kNZ - 2));
-  const int ir = (int)tr;
+  const float R2 = fmaf(Z, Z, fmaf(Y, Y, X * X));
+  const float Rc = sqrtf(R2);
+  const float tr = Rc * f.idr_cell;
+  bool ok = tr + f.rho_idr < (float)(kNZ - 3) && Rc > 2.f * f.rho + 2.f;
+  const float trs = ok ? tr : 0.f;
+  const int ir = (int)trs;
   const float z0 = __ldg(&c.z_r2z_f[ir]), z1 = __ldg(&c.z_r2z_f[ir + 1]);
-  const float nu = __fdividef(1420.40575177f, 1.f + (fmaf(z1 - z0, tr - (float)ir, z0) + dz));
-  const int nn = c.n_nu;
-  const float inf = __int_as_float(0x7f800000);
-  b.lo = edge_search(ef, nn, log2nn, nu);
-  b.e0 = b.lo - 1 >= 0 ? ef[b.lo - 1] : -inf;
-  b.e1 = b.lo >= 0 ? ef[b.lo] : -inf;
-  b.e2 = b.lo + 1 <= nn ? ef[b.lo + 1] : inf;
-  b.e3 = b.lo + 2 <= nn ? ef[min(b.lo + 2, nn)] : inf;
-  return b;
+  const float g = __ldg(&c.z_lin_g[ir]), e = __ldg(&c.z_lin_e[ir]);  // slope per cell, line bound
+  const float dzt = z1 - z0;
+  const float zz = 1.f + (fmaf(dzt, trs - (float)ir, z0) + dz);
+  const float izz = __fdividef(1.f, zz);
+  const float nu = A * izz;
+  const float sc = c.regular_nu ? f.inv_dnu : 1.f;
+  const float u = c.regular_nu ? (nu - f.nu_min) * sc : nu;
+  const float mnu = 2.f * nu * (fabsf(dzt) * trs * 1.8e-7f * izz + 4.8e-7f + 2.7e-7f);
+  const float mc = c.regular_nu ? (mnu + 1.2e-7f * nu) * sc + 4e-7f * fabsf(u) + 1e-6f : mnu;
+  const float d1 = A * sc * izz * izz;  // |du/dz| at the centre
+  const float s = -d1 * g;
+  const float dZ = fabsf(g) * f.rho + e;  // largest |z(R) - z(Rc)| over the cell
+  const float zlo = zz - dZ;
+  ok = ok && zlo > 0.25f;
+  const float izlo = __fdividef(1.f, zlo);
+  const float lin = fabsf(s) * (3.7e-7f * (Rc + f.rho) + 1.8e-7f * Rc) + d1 * e + 2e-6f * fabsf(s) * f.rho +
+                    A * sc * dZ * dZ * izlo * izlo * izlo + 1.2e-7f * (fabsf(u) + fabsf(s) * f.rho);
+  o.u = ok ? u : 0.5f;
+  o.s = ok ? s : 0.f;
+  o.Rc = Rc;
+  o.m = ok ? mc + 1.5f * lin : __int_as_float(0x7f800000);
+  o.lo = 0;
+  o.e0 = o.e1 = o.e2 = o.e3 = 0.f;
+  if (!c.regular_nu) {
+    const int nn = c.n_nu;
+    const float inf = __int_as_float(0x7f800000);
+    o.lo = edge_search(ef, nn, log2nn, o.u);
+    o.e0 = o.lo - 1 >= 0 ? ef[o.lo - 1] : -inf;
+    o.e1 = o.lo >= 0 ? ef[o.lo] : -inf;
+    o.e2 = o.lo + 1 <= nn ? ef[o.lo + 1] : inf;
+    o.e3 = o.lo + 2 <= nn ? ef[min(o.lo + 2, nn)] : inf;
+  }
+  return o;
 }
 
-__device__ __forceinline__ uint32_t key_fast(const DevCfg &c, const FastConst &f, const float *ef, int log2nn,
-                                             const EdgeBracket &br, float X, float Y, float Z, float dz)
+__device__ __forceinline__ uint32_t key_fast(const DevCfg &c, const float *ef, int log2nn, const CellShell &cs,
+                                             float X, float Y, float Z)
 {
   const float rho2 = fmaf(Y, Y, X * X);
   const float R2 = fmaf(Z, Z, rho2);
   const float iR = rsqrtf(R2);
-  const float R = R2 * iR;
-  float tr = R * f.idr_cell;
-  const bool bad = !(tr < (float)(kNZ - 2)) || !(rho2 > 0.f);
-  tr = bad ? 0.f : tr;
-  const int ir = (int)tr;
-  const float fr = tr - (float)ir;
-  const float z0 = __ldg(&c.z_r2z_f[ir]), z1 = __ldg(&c.z_r2z_f[ir + 1]);
-  const float zz = 1.f + (fmaf(z1 - z0, fr, z0) + dz);
-  const float nu = __fdividef(1420.40575177f, zz);
-  const float mnu = 2.f * nu * (__fdividef(fabsf(z1 - z0) * tr * 3.7e-7f, zz) + 4.8e-7f + 2.7e-7f);
+  const float u = fmaf(cs.s, R2 * iR - cs.Rc, cs.u);
+  const float m = cs.m;
   int inu;
   bool unc;
   if (c.regular_nu) {
-    const float t = (nu - f.nu_min) * f.inv_dnu;
-    unc = near_int(t, (mnu + 1.2e-7f * nu) * f.inv_dnu + 4e-7f * fabsf(t) + 1e-6f);
-    inu = (int)t;  // truncation, src/pixelize.c:216
+    unc = near_int(u, m);
+    inu = (int)u;  // truncation, src/pixelize.c:216
   } else {
     // bin inu: ef[inu] <= nu < ef[inu + 1] (-1 below ef[0], nn at or above ef[nn])
-    inu = br.lo + (nu >= br.e2 ? 1 : 0) - (nu < br.e1 ? 1 : 0);
-    unc = fabsf(nu - br.e0) < mnu || fabsf(nu - br.e1) < mnu || fabsf(nu - br.e2) < mnu || fabsf(nu - br.e3) < mnu;
-    if (nu < br.e0 || nu >= br.e3) {  // two or more bins from the cell centre's (rare)
+    const float nu = u;
+    inu = cs.lo + (nu >= cs.e2 ? 1 : 0) - (nu < cs.e1 ? 1 : 0);
+    unc = fabsf(nu - cs.e0) < m || fabsf(nu - cs.e1) < m || fabsf(nu - cs.e2) < m || fabsf(nu - cs.e3) < m;
+    if (nu < cs.e0 || nu >= cs.e3) {  // two or more bins from the cell centre's (rare)
       const int nn = c.n_nu;
       const int lo = edge_search(ef, nn, log2nn, nu);
       inu = lo;
       const float below = lo >= 0 ? nu - ef[max(lo, 0)] : 1e30f;
       const float above = lo < nn ? ef[min(lo + 1, nn)] - nu : 1e30f;
-      unc = below < mnu || above < mnu;
+      unc = below < m || above < m;
     }
   }
-  if (bad || unc) return kKeyUncertain;
+  if (!(rho2 > 0.f) || unc) return kKeyUncertain;
   if (inu < 0 || inu >= c.n_nu) return kKeyInvalid;
   const uint32_t pix = pixel_fast(c, X, Y, Z, rho2, iR);
   return pix == kKeyUncertain ? kKeyUncertain : pix + (uint32_t)c.npix * (uint32_t)inu;
@@ -553,12 +599,12 @@ __global__ void __launch_bounds__(kProjThreads, 4) project_kernel(DevCfg c, Fast
     }
     const float msub = mass / 10.f;  // src/pixelize.c:203
     const float Xc = (float)ix - f.half_n, Yc = (float)iy - f.half_n, Zc = (float)iz - f.half_n;
-    const EdgeBracket br = edge_bracket(c, f, ef, log2nn, Xc, Yc, Zc, dz);
+    const CellShell cs = cell_shell(c, f, ef, log2nn, Xc, Yc, Zc, dz);
     uint32_t cur = 0xFFFFFFFFu, umask = 0;
     float acc = 0.f;
 #pragma unroll kProjUnroll
     for (int j = 0; j < kNSUB; j++) {
-      const uint32_t key = key_fast(c, f, ef, log2nn, br, Xc + f.txsp[j], Yc + f.tysp[j], Zc + f.tzsp[j], dz);
+      const uint32_t key = key_fast(c, ef, log2nn, cs, Xc + f.txsp[j], Yc + f.tysp[j], Zc + f.tzsp[j]);
       umask |= (key == kKeyUncertain ? 1u : 0u) << j;
       if (key < kKeyUncertain) {  // a key inside the shells; the run of cur ends at a new key
         if (key != cur && cur != 0xFFFFFFFFu) map_add(maps, cur, acc);
@@ -668,11 +714,11 @@ __global__ void sample_keys_kernel(DevCfg c, FastConst f, const float *__restric
     const int iy = (int)(rest % n), iz = (int)(rest / n);
     const float dz = dzg[i];
     const float Xc = (float)ix - f.half_n, Yc = (float)iy - f.half_n, Zc = (float)iz - f.half_n;
-    const EdgeBracket br = edge_bracket(c, f, c.nu_edges_f, log2nn, Xc, Yc, Zc, dz);
+    const CellShell cs = cell_shell(c, f, c.nu_edges_f, log2nn, Xc, Yc, Zc, dz);
     for (int is = 0; is < kNSUB; is++) {
       uint32_t key = kKeyUncertain;
       if (!exact)
-        key = key_fast(c, f, c.nu_edges_f, log2nn, br, Xc + f.xsp[is], Yc + f.ysp[is], Zc + f.zsp[is], dz);
+        key = key_fast(c, c.nu_edges_f, log2nn, cs, Xc + f.xsp[is], Yc + f.ysp[is], Zc + f.zsp[is]);
       if (key == kKeyUncertain) {
         key = exact ? key_exact(c, ix, iy, iz, is, dz) : key_resolve(c, ix, iy, iz, is, dz);
         nfall++;
@@ -704,6 +750,35 @@ cudaError_t get_hi(const DevCfg &c, const double *stats, float *dens, float *rve
   return cudaGetLastError();
 }
 
+double subsample_radius(const double *xs, const double *ys, const double *zs, double dx)
+{
+  double r = 0;
+  for (int i = 0; i < kNSUB; i++) r = std::fmax(r, std::sqrt(xs[i] * xs[i] + ys[i] * ys[i] + zs[i] * zs[i]) / dx);
+  return r;
+}
+
+// Interval i of the table spans R in [a, a + h) cells (h = 1/(glob_idr dx); the
+// nodes sit at r = k/glob_idr).  Its line is z_i + g (R - a).  A cell whose FP32
+// centre falls in interval i has its sub-samples within rho of the centre and
+// the centre within eps of the interval, so the deviation bound e is the
+// largest |z(R) - line| over R in [a - rho - eps, a + h + rho + eps]: z is
+// piecewise linear, so the largest value sits at a node or at an end.
+float2 shell_line_entry(const double *z, double glob_idr, double dx, double rho, int i)
+{
+  if (i < 0 || i + 1 >= kNZ) return make_float2(0.f, 0.f);
+  const double h = 1.0 / (glob_idr * dx), a = i * h, b = a + h, top = (kNZ - 1) * h;
+  const double g = (z[i + 1] - z[i]) * glob_idr * dx;
+  const double eps = 1e-3 + 1e-6 * b;  // FP32 centre radius and interval index
+  const double lo = std::fmax(0.0, a - rho - eps), hi = std::fmin(top, b + rho + eps);
+  auto line_dev = [&](double R) {
+    const int k = std::min((int)(R / h), kNZ - 2);
+    return std::fabs(z[k] + (z[k + 1] - z[k]) * (R / h - k) - z[i] - g * (R - a));
+  };
+  double e = std::fmax(line_dev(lo), line_dev(hi));
+  for (int k = (int)(lo / h) + 1; k < kNZ && k * h < hi; k++) e = std::fmax(e, std::fabs(z[k] - z[i] - g * (k * h - a)));
+  return make_float2((float)g, (float)(e * (1 + 1e-5) + 1e-12));
+}
+
 static FastConst fast_const(const DevCfg &c)
 {
   FastConst f;
@@ -713,6 +788,8 @@ static FastConst fast_const(const DevCfg &c)
     f.zsp[i] = (float)(0.5 + c.zs[i] / c.dx);
   }
   f.idr_cell = (float)(c.glob_idr * c.dx);
+  f.rho = (float)(subsample_radius(c.xs, c.ys, c.zs, c.dx) * (1 + 1e-5) + 1e-6);
+  f.rho_idr = f.rho * f.idr_cell * 1.0001f;
   f.half_n = (float)(c.n / 2);
   f.nu_min = (float)c.nu_min;
   f.inv_dnu = (float)c.inv_dnu;
