@@ -296,6 +296,9 @@ struct FastConst {
   // keys are longer): tour[j] is the j-th sample's index, txsp.. its offsets
   int tour[kNSUB];
   float txsp[kNSUB], tysp[kNSUB], tzsp[kNSUB];
+  // key_lin: the j-th sample's offset from the cell centre and its monomials
+  float tox[kNSUB], toy[kNSUB], toz[kNSUB], toxx[kNSUB], toyy[kNSUB], tozz[kNSUB];
+  float toxy[kNSUB], toxz[kNSUB], toyz[kNSUB], tdxy[kNSUB];
 };
 
 __device__ __forceinline__ bool near_int(float u, float m) { return fabsf(u - rintf(u)) < m; }
@@ -373,6 +376,7 @@ __device__ __forceinline__ int edge_search(const float *ef, int nn, int log2nn, 
 // left to samples two or more bins away.
 struct CellShell {
   float u, s, Rc, m;
+  float gx, gy, gz, ml;  // key_lin: du/do = s r_hat and its bound
   int lo;
   float e0, e1, e2, e3;
 };
@@ -407,17 +411,26 @@ __device__ __forceinline__ CellShell cell_shell(const DevCfg &c, const FastConst
   const float zlo = zz - dZ;
   ok = ok && zlo > 0.25f;
   const float izlo = __fdividef(1.f, zlo);
-  const float lin = fabsf(s) * (3.7e-7f * (Rc + f.rho) + 1.8e-7f * Rc) + d1 * e + 2e-6f * fabsf(s) * f.rho +
-                    A * sc * dZ * dZ * izlo * izlo * izlo + 1.2e-7f * (fabsf(u) + fabsf(s) * f.rho);
+  const float common = d1 * e + 2e-6f * fabsf(s) * f.rho + A * sc * dZ * dZ * izlo * izlo * izlo +
+                       2e-7f * (fabsf(u) + fabsf(s) * f.rho);
+  const float lin = fabsf(s) * (3.7e-7f * (Rc + f.rho) + 1.8e-7f * Rc) + common;
+  // key_lin: R - Rc = r_hat.o + h, 0 <= h <= rho^2 / (2 (Rc - rho)) (|P| is convex; its
+  // Hessian is below 1/|P|); r_hat = C/Rc to 3e-7; FP32 offsets within 1e-7 cells
+  const float linq = fabsf(s) * (__fdividef(f.rho * f.rho, 2.f * (Rc - f.rho)) + 3e-7f * f.rho + 1e-7f) + common;
+  const float inf = __int_as_float(0x7f800000);
   o.u = ok ? u : 0.5f;
   o.s = ok ? s : 0.f;
   o.Rc = Rc;
-  o.m = ok ? mc + 1.5f * lin : __int_as_float(0x7f800000);
+  o.m = ok ? mc + 1.5f * lin : inf;
+  o.ml = ok ? mc + 1.5f * linq : inf;
+  const float sr = o.s * __fdividef(1.f, Rc);
+  o.gx = sr * X;
+  o.gy = sr * Y;
+  o.gz = sr * Z;
   o.lo = 0;
   o.e0 = o.e1 = o.e2 = o.e3 = 0.f;
   if (!c.regular_nu) {
     const int nn = c.n_nu;
-    const float inf = __int_as_float(0x7f800000);
     o.lo = edge_search(ef, nn, log2nn, o.u);
     o.e0 = o.lo - 1 >= 0 ? ef[o.lo - 1] : -inf;
     o.e1 = o.lo >= 0 ? ef[o.lo] : -inf;
@@ -427,16 +440,10 @@ __device__ __forceinline__ CellShell cell_shell(const DevCfg &c, const FastConst
   return o;
 }
 
-__device__ __forceinline__ uint32_t key_fast(const DevCfg &c, const float *ef, int log2nn, const CellShell &cs,
-                                             float X, float Y, float Z)
+// shell bin inu of the coordinate u, unc when u lies within m of a bin edge
+__device__ __forceinline__ void shell_bin(const DevCfg &c, const float *ef, int log2nn, const CellShell &cs, float u,
+                                          float m, int &inu, bool &unc)
 {
-  const float rho2 = fmaf(Y, Y, X * X);
-  const float R2 = fmaf(Z, Z, rho2);
-  const float iR = rsqrtf(R2);
-  const float u = fmaf(cs.s, R2 * iR - cs.Rc, cs.u);
-  const float m = cs.m;
-  int inu;
-  bool unc;
   if (c.regular_nu) {
     unc = near_int(u, m);
     inu = (int)u;  // truncation, src/pixelize.c:216
@@ -454,10 +461,39 @@ __device__ __forceinline__ uint32_t key_fast(const DevCfg &c, const float *ef, i
       unc = below < m || above < m;
     }
   }
-  if (!(rho2 > 0.f) || unc) return kKeyUncertain;
-  if (inu < 0 || inu >= c.n_nu) return kKeyInvalid;
+}
+
+__device__ __forceinline__ uint32_t key_fast(const DevCfg &c, const float *ef, int log2nn, const CellShell &cs,
+                                             float X, float Y, float Z)
+{
+  const float rho2 = fmaf(Y, Y, X * X);
+  const float R2 = fmaf(Z, Z, rho2);
+  const float iR = rsqrtf(R2);
+  int inu;
+  bool unc;
+  shell_bin(c, ef, log2nn, cs, fmaf(cs.s, R2 * iR - cs.Rc, cs.u), cs.m, inu, unc);
+  // selected at the end, like key_lin (the pixel of a sample outside the shells is unused)
   const uint32_t pix = pixel_fast(c, X, Y, Z, rho2, iR);
-  return pix == kKeyUncertain ? kKeyUncertain : pix + (uint32_t)c.npix * (uint32_t)inu;
+  const bool out = (uint32_t)inu >= (uint32_t)c.n_nu;
+  const uint32_t key = pix + (uint32_t)c.npix * (uint32_t)inu;
+  return (!(rho2 > 0.f) | unc) ? kKeyUncertain : (out ? kKeyInvalid : (pix == kKeyUncertain ? kKeyUncertain : key));
+}
+
+// octant decomposition of the azimuth: a = atan(min/max) in [0, pi/4];
+// tt = 2 phi/pi = q + w, q in 0..3, w in [0, 1) within 2.05e-7 of the exact value
+__device__ __forceinline__ void azimuth(float X, float Y, int &q, float &w)
+{
+  const float ax = fabsf(X), ay = fabsf(Y);
+  const bool swap = ay > ax;
+  const float a2 = atan01(__fdividef(fminf(ax, ay), fmaxf(ax, ay))) * 0.63661977f;  // in [0, 0.5]
+  const bool upper = Y >= 0.f, right = X >= 0.f;
+  q = upper ? (right ? 0 : 1) : (right ? 3 : 2);
+  // w = a2 when the octant runs counter-clockwise from the quadrant start, else 1 - a2
+  const bool ccw = ((q & 1) == 0) ? !swap : swap;
+  w = ccw ? a2 : 1.f - a2;
+  const bool wrap = w >= 1.f;
+  w = wrap ? w - 1.f : w;
+  q = wrap ? ((q + 1) & 3) : q;
 }
 
 // RING pixel of (X, Y, Z) (cell units, |error| <= 6e-8 relative), rho2 = X^2 + Y^2,
@@ -469,28 +505,19 @@ __device__ __forceinline__ uint32_t pixel_fast(const DevCfg &c, float X, float Y
   const float cth = Z * iR;
   const float za = fabsf(cth);
   const float dcos = 3.7e-7f;
-  // octant decomposition: a = atan(min/max) in [0, pi/4]; tt = 2 phi/pi = q + w
-  const float ax = fabsf(X), ay = fabsf(Y);
-  const bool swap = ay > ax;
-  const float a2 = atan01(__fdividef(fminf(ax, ay), fmaxf(ax, ay))) * 0.63661977f;  // in [0, 0.5]
-  const bool upper = Y >= 0.f, right = X >= 0.f;
-  int q = upper ? (right ? 0 : 1) : (right ? 3 : 2);
-  // w = a2 when the octant runs counter-clockwise from the quadrant start, else 1 - a2
-  const bool ccw = ((q & 1) == 0) ? !swap : swap;
-  float w = ccw ? a2 : 1.f - a2;
-  const bool wrap = w >= 1.f;
-  w = wrap ? w - 1.f : w;
-  q = wrap ? ((q + 1) & 3) : q;
+  int q;
+  float w;
+  azimuth(X, Y, q, w);
   const float dw = 2.05e-7f;
   const int npix = (int)c.npix;
-  if (fabsf(za - 0.6666667f) < 2.f * dcos + 6e-8f) return kKeyUncertain;
+  bool unc = fabsf(za - 0.6666667f) < 2.f * dcos + 6e-8f;
   int pix;
   if (za <= 0.6666667f) {
     const float t2 = fn * cth * 0.75f;
     const float v = fn * (0.5f + w);
     const float v1 = v - t2, v2 = v + t2;
     const float mu = 2.f * (fn * (dw + 6e-8f + 0.75f * dcos) + 2.f * 1.2e-7f * (1.5f * fn + 1.f));
-    if (near_int(v1, mu) || near_int(v2, mu)) return kKeyUncertain;
+    unc |= near_int(v1, mu) | near_int(v2, mu);
     const int f1 = (int)floorf(v1), f2 = (int)floorf(v2);
     const int ring = nside + 1 + f1 - f2;  // jp - jm: the q nside terms cancel
     const int num = f1 + f2 + (2 * q - 1) * nside + (1 - (ring & 1)) + 1;  // jp + jm - nside + kshift + 1 >= -1
@@ -506,13 +533,119 @@ __device__ __forceinline__ uint32_t pixel_fast(const DevCfg &c, float X, float Y
     const int jp = (int)u3, jm = (int)u4;
     const int ring = jp + jm + 1;
     const float u5 = w * (float)ring;
-    if (near_int(u3, mu) || near_int(u4, mu) || w < 2.f * dw || 1.f - w < 2.f * dw ||
-        near_int(u5, 2.f * ((float)ring * dw + 2.4e-7f * (u5 + 1.f))))
-      return kKeyUncertain;
+    unc |= near_int(u3, mu) | near_int(u4, mu) | (w < 2.f * dw) | (1.f - w < 2.f * dw) |
+           near_int(u5, 2.f * ((float)ring * dw + 2.4e-7f * (u5 + 1.f)));
     const int ip = q * ring + (int)u5;  // floor(tt ring) < 4 ring
     pix = (cth > 0) ? 2 * ring * (ring - 1) + ip : npix - 2 * ring * (ring + 1) + ip;
   }
-  return (uint32_t)pix;
+  // no early returns (as in key_lin); a pixel outside the map only comes from an uncertain sample
+  return (unc | ((uint32_t)pix >= (uint32_t)npix)) ? kKeyUncertain : (uint32_t)pix;
+}
+
+// ---------------------------------------------------------------------------
+// Equatorial cells: the RING floor arguments as quadratics in the sub-sample offset.
+//
+// In the equatorial zone (|cos theta| <= 2/3) the pixel of a point is fixed by
+// floor(V1), floor(V2), V1,2 = n (0.5 + tt) -/+ 0.75 n cos(theta) - n q, with
+// tt = 2 phi/pi = q + w (src/pixelize.c:216-218; the RING scheme of Gorski et
+// al. 2005).  For a cell C whose sub-samples C + o all lie in that zone, on one
+// side of phi = 0, this takes per cell
+//     V(C + o) = V(C) + grad V . o + o.H.o/2 + r3,
+// phi and cos theta expanded to second order at C:
+//   phi: grad = (-y, x, 0)/rxy^2; o.H.o/2 = (xy (ox^2 - oy^2) + (y^2 - x^2) ox oy)/rxy^4;
+//        |r3| <= |o|^3/(3 rxy_min^3) (the k-th derivative of Im log(x + iy) is (k-1)!/|x + iy|^k);
+//   cos theta = z/r: grad = (-xz, -yz, x^2 + y^2)/r^3;
+//        H = -(z P P^T 3/r^2 ... ): H_xx = z (3x^2/r^2 - 1)/r^3, H_yy = z (3y^2/r^2 - 1)/r^3,
+//        H_zz = 3z (z^2/r^2 - 1)/r^3, H_xy = 3xyz/r^5, H_xz = x (3z^2/r^2 - 1)/r^3,
+//        H_yz = y (3z^2/r^2 - 1)/r^3; |r3| <= |o|^3/(2 r_min^3) (third derivative of z/r below
+//        3/r^3 over the sphere), taken twice over.
+// The offsets' monomials are per-sample constants, so a sub-sample costs 13 FMAs for
+// both arguments.  The bound mu (x2 like every fast-path margin) holds the
+// centre's azimuth (2.05e-7) and cos theta (2.4e-7 of |cos|), the rounding of
+// V(C) (3e-7 n) and of the final sum (1.2e-7 n), 1e-6 of the expansion's size
+// for its FP32 coefficients, 1e-7 cells per offset and the third-order terms.
+// ---------------------------------------------------------------------------
+struct CellPix {
+  float v1, v2, mu;
+  int qterm;                                       // (2q - 1) nside
+  float a1, a2, a3, a4;                            // n dtt on ox, oy, ox^2 - oy^2, ox oy
+  float b1, b2, b3, b4, b5, b6, b7, b8, b9;        // 0.75 n dcos on ox, oy, oz, ox^2, oy^2, oz^2, ox oy, ox oz, oy oz
+  bool lin;
+};
+
+__device__ __forceinline__ CellPix cell_pix(const DevCfg &c, const FastConst &f, float X, float Y, float Z, float Rc)
+{
+  CellPix p;
+  const float fn = (float)c.nside, K = fn * 0.63661977f, L = 0.75f * fn, rho = f.rho;
+  const float rxy2 = fmaf(Y, Y, X * X);
+  const float rxy = sqrtf(rxy2);
+  const float cth = __fdiv_rn(Z, Rc);
+  int q;
+  float w;
+  azimuth(X, Y, q, w);
+  const float rmin = Rc - rho, rxymin = rxy - rho;
+  const float i1 = __fdividef(rho, rxymin), i2 = __fdividef(rho, rmin);
+  const float dT = 0.63661977f * i1 + 1e-5f;
+  p.lin = rxymin > 1.f && fabsf(cth) + i2 + 1e-5f < 0.66666f && !((q == 0 && w < dT) || (q == 3 && w > 1.f - dT));
+  const float irxy2 = __fdividef(1.f, rxy2), iR = __fdividef(1.f, Rc);
+  const float Kr = K * irxy2, Kr2 = Kr * irxy2;
+  p.a1 = -Kr * Y;
+  p.a2 = Kr * X;
+  p.a3 = Kr2 * (X * Y);
+  p.a4 = Kr2 * (Y * Y - X * X);
+  const float Lr3 = L * iR * iR * iR, h = 0.5f * Lr3;
+  const float sx = X * iR, sy = Y * iR, c2 = cth * cth, t3 = 3.f * c2 - 1.f;
+  p.b1 = -Lr3 * (X * Z);
+  p.b2 = -Lr3 * (Y * Z);
+  p.b3 = Lr3 * rxy2;
+  p.b4 = h * Z * (3.f * sx * sx - 1.f);
+  p.b5 = h * Z * (3.f * sy * sy - 1.f);
+  p.b6 = 3.f * h * Z * (c2 - 1.f);
+  p.b7 = 3.f * Lr3 * Z * sx * sy;
+  p.b8 = Lr3 * X * t3;
+  p.b9 = Lr3 * Y * t3;
+  const float base = fn * (0.5f + w), Lc = L * cth;
+  p.v1 = base - Lc;
+  p.v2 = base + Lc;
+  p.qterm = (2 * q - 1) * (int)c.nside;
+  const float sa = fabsf(p.a1) + fabsf(p.a2) + fabsf(p.b1) + fabsf(p.b2) + fabsf(p.b3);
+  const float sq = fabsf(p.a3) + fabsf(p.a4) + fabsf(p.b4) + fabsf(p.b5) + fabsf(p.b6) + fabsf(p.b7) +
+                   fabsf(p.b8) + fabsf(p.b9);
+  const float third = K * i1 * i1 * i1 * (1.f / 3.f) + L * i2 * i2 * i2;
+  p.mu = 2.f * (fn * (2.05e-7f + 3e-7f + 1.2e-7f) + L * 2.4e-7f + 1e-6f * (sa * rho + sq * rho * rho) + 1e-7f * sa +
+                third);
+  return p;
+}
+
+// key of sub-sample j (tour order) of a cell with cp.lin: shell from u = u_c + s r_hat.o,
+// pixel from the quadratics (same integer steps as pixel_fast's equatorial branch).
+// Everything is evaluated and the key selected at the end: early returns cost
+// more in branches and convergence barriers than the arithmetic they skip.  A
+// pixel outside the equatorial rings (impossible for a certified sample) goes to
+// the exact key, so no key can leave the maps.
+__device__ __forceinline__ uint32_t key_lin(const DevCfg &c, const FastConst &f, const float *ef, int log2nn,
+                                            const CellShell &cs, const CellPix &p, int j)
+{
+  const float ox = f.tox[j], oy = f.toy[j], oz = f.toz[j];
+  int inu;
+  bool unc;
+  shell_bin(c, ef, log2nn, cs, fmaf(cs.gz, oz, fmaf(cs.gy, oy, fmaf(cs.gx, ox, cs.u))), cs.ml, inu, unc);
+  const float dP = fmaf(p.a4, f.toxy[j], fmaf(p.a3, f.tdxy[j], fmaf(p.a2, oy, p.a1 * ox)));
+  const float dQ = fmaf(p.b9, f.toyz[j], fmaf(p.b8, f.toxz[j], fmaf(p.b7, f.toxy[j], fmaf(p.b6, f.tozz[j],
+                   fmaf(p.b5, f.toyy[j], fmaf(p.b4, f.toxx[j], fmaf(p.b3, oz, fmaf(p.b2, oy, p.b1 * ox))))))));
+  const float v1 = p.v1 + (dP - dQ), v2 = p.v2 + (dP + dQ);
+  const bool pu = near_int(v1, p.mu) | near_int(v2, p.mu);
+  const int nside = (int)c.nside;
+  const int f1 = (int)floorf(v1), f2 = (int)floorf(v2);
+  const int ring = nside + 1 + f1 - f2;
+  const int num = f1 + f2 + p.qterm + (1 - (ring & 1)) + 1;
+  int ip = (num + (num < 0)) >> 1;
+  ip = ip >= 4 * nside ? ip - 4 * nside : ip;
+  const int pix = 2 * nside * (nside - 1) + (ring - 1) * 4 * nside + ip;
+  const bool out = (uint32_t)inu >= (uint32_t)c.n_nu;
+  const bool bad = pu | ((uint32_t)pix >= (uint32_t)c.npix);
+  const uint32_t key = (uint32_t)pix + (uint32_t)c.npix * (uint32_t)inu;
+  return unc ? kKeyUncertain : (out ? kKeyInvalid : (bad ? kKeyUncertain : key));
 }
 
 // ---------------------------------------------------------------------------
@@ -600,17 +733,26 @@ __global__ void __launch_bounds__(kProjThreads, 4) project_kernel(DevCfg c, Fast
     const float msub = mass / 10.f;  // src/pixelize.c:203
     const float Xc = (float)ix - f.half_n, Yc = (float)iy - f.half_n, Zc = (float)iz - f.half_n;
     const CellShell cs = cell_shell(c, f, ef, log2nn, Xc, Yc, Zc, dz);
+    const CellPix cp = cell_pix(c, f, Xc + 0.5f, Yc + 0.5f, Zc + 0.5f, cs.Rc);
     uint32_t cur = 0xFFFFFFFFu, umask = 0;
     float acc = 0.f;
-#pragma unroll kProjUnroll
-    for (int j = 0; j < kNSUB; j++) {
-      const uint32_t key = key_fast(c, ef, log2nn, cs, Xc + f.txsp[j], Yc + f.tysp[j], Zc + f.tzsp[j]);
+    // a key inside the shells extends the run of cur or ends it (one reduction);
+    // written without branches: the reduction is the only predicated step
+    auto take = [&](uint32_t key, int j) {
       umask |= (key == kKeyUncertain ? 1u : 0u) << j;
-      if (key < kKeyUncertain) {  // a key inside the shells; the run of cur ends at a new key
-        if (key != cur && cur != 0xFFFFFFFFu) map_add(maps, cur, acc);
-        acc = key == cur ? acc + msub : msub;
-        cur = key;
-      }
+      const bool valid = key < kKeyUncertain;
+      const bool flush = valid & (key != cur) & (cur != 0xFFFFFFFFu);
+      if (flush) map_add(maps, cur, acc);
+      acc = valid ? (key == cur ? acc + msub : msub) : acc;
+      cur = valid ? key : cur;
+    };
+    if (cp.lin) {
+#pragma unroll
+      for (int j = 0; j < kNSUB; j++) take(key_lin(c, f, ef, log2nn, cs, cp, j), j);
+    } else {
+#pragma unroll kProjUnroll
+      for (int j = 0; j < kNSUB; j++)
+        take(key_fast(c, ef, log2nn, cs, Xc + f.txsp[j], Yc + f.tysp[j], Zc + f.tzsp[j]), j);
     }
     if (cur != 0xFFFFFFFFu) map_add(maps, cur, acc);
     // uncertain samples of the cell: to the tile queue (when it is full, decided here)
@@ -715,10 +857,13 @@ __global__ void sample_keys_kernel(DevCfg c, FastConst f, const float *__restric
     const float dz = dzg[i];
     const float Xc = (float)ix - f.half_n, Yc = (float)iy - f.half_n, Zc = (float)iz - f.half_n;
     const CellShell cs = cell_shell(c, f, c.nu_edges_f, log2nn, Xc, Yc, Zc, dz);
-    for (int is = 0; is < kNSUB; is++) {
+    const CellPix cp = cell_pix(c, f, Xc + 0.5f, Yc + 0.5f, Zc + 0.5f, cs.Rc);
+    for (int j = 0; j < kNSUB; j++) {
+      const int is = f.tour[j];
       uint32_t key = kKeyUncertain;
       if (!exact)
-        key = key_fast(c, c.nu_edges_f, log2nn, cs, Xc + f.xsp[is], Yc + f.ysp[is], Zc + f.zsp[is]);
+        key = cp.lin ? key_lin(c, f, c.nu_edges_f, log2nn, cs, cp, j)
+                     : key_fast(c, c.nu_edges_f, log2nn, cs, Xc + f.txsp[j], Yc + f.tysp[j], Zc + f.tzsp[j]);
       if (key == kKeyUncertain) {
         key = exact ? key_exact(c, ix, iy, iz, is, dz) : key_resolve(c, ix, iy, iz, is, dz);
         nfall++;
@@ -838,6 +983,18 @@ static FastConst fast_const(const DevCfg &c)
     f.txsp[k] = f.xsp[f.tour[k]];
     f.tysp[k] = f.ysp[f.tour[k]];
     f.tzsp[k] = f.zsp[f.tour[k]];
+    // within 4.5e-8 cells of xs/dx: xsp rounds once, the subtraction at most once more
+    const float ox = f.txsp[k] - 0.5f, oy = f.tysp[k] - 0.5f, oz = f.tzsp[k] - 0.5f;
+    f.tox[k] = ox;
+    f.toy[k] = oy;
+    f.toz[k] = oz;
+    f.toxx[k] = ox * ox;
+    f.toyy[k] = oy * oy;
+    f.tozz[k] = oz * oz;
+    f.toxy[k] = ox * oy;
+    f.toxz[k] = ox * oz;
+    f.toyz[k] = oy * oz;
+    f.tdxy[k] = ox * ox - oy * oy;
   }
   return f;
 }
