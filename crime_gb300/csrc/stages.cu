@@ -463,6 +463,16 @@ __device__ __forceinline__ void shell_bin(const DevCfg &c, const float *ef, int 
   }
 }
 
+// every sub-sample of the cell certainly outside the shells (then all its keys are
+// kKeyInvalid): the exact coordinate of each lies within max(m, ml) of the cell's
+// line, which moves by at most |s| rho over the cell
+__device__ __forceinline__ bool cell_outside(const DevCfg &c, const FastConst &f, const float *ef, const CellShell &cs)
+{
+  const float span = fabsf(cs.s) * f.rho * 1.000001f + fmaxf(cs.m, cs.ml) + 1e-6f * fabsf(cs.u) + 1e-6f;
+  const float hi = cs.u + span, lo = cs.u - span;
+  return c.regular_nu ? (hi <= -1.f || lo >= (float)c.n_nu) : (hi < ef[0] || lo >= ef[c.n_nu]);
+}
+
 __device__ __forceinline__ uint32_t key_fast(const DevCfg &c, const float *ef, int log2nn, const CellShell &cs,
                                              float X, float Y, float Z)
 {
@@ -733,6 +743,7 @@ __global__ void __launch_bounds__(kProjThreads, 4) project_kernel(DevCfg c, Fast
     const float msub = mass / 10.f;  // src/pixelize.c:203
     const float Xc = (float)ix - f.half_n, Yc = (float)iy - f.half_n, Zc = (float)iz - f.half_n;
     const CellShell cs = cell_shell(c, f, ef, log2nn, Xc, Yc, Zc, dz);
+    if (cell_outside(c, f, ef, cs)) continue;  // inside the first shell or beyond the last: no keys
     const CellPix cp = cell_pix(c, f, Xc + 0.5f, Yc + 0.5f, Zc + 0.5f, cs.Rc);
     uint32_t cur = 0xFFFFFFFFu, umask = 0;
     float acc = 0.f;
@@ -857,6 +868,10 @@ __global__ void sample_keys_kernel(DevCfg c, FastConst f, const float *__restric
     const float dz = dzg[i];
     const float Xc = (float)ix - f.half_n, Yc = (float)iy - f.half_n, Zc = (float)iz - f.half_n;
     const CellShell cs = cell_shell(c, f, c.nu_edges_f, log2nn, Xc, Yc, Zc, dz);
+    if (!exact && cell_outside(c, f, c.nu_edges_f, cs)) {
+      for (int is = 0; is < kNSUB; is++) keys[i * kNSUB + is] = kKeyInvalid;
+      continue;
+    }
     const CellPix cp = cell_pix(c, f, Xc + 0.5f, Yc + 0.5f, Zc + 0.5f, cs.Rc);
     for (int j = 0; j < kNSUB; j++) {
       const int is = f.tour[j];
