@@ -55,9 +55,12 @@ GEOMETRIES = [  # n, box (Mpc/h), Nside, zmin, zmax, shells: the bench's 512^3, 
 ]
 
 
+@pytest.mark.parametrize("regular", [1, 0], ids=["regular", "frequency_file"])
 @pytest.mark.parametrize("n,box,nside,zmin,zmax,n_nu", GEOMETRIES)
-def test_shell_line_bound(n, box, nside, zmin, zmax, n_nu):
-    rng = np.random.default_rng(n)
+def test_shell_line_bound(n, box, nside, zmin, zmax, n_nu, regular):
+    """u is the channel coordinate of a regular table, or the frequency itself
+    (compared with FP32 edges) for a frequency file."""
+    rng = np.random.default_rng(n + regular)
     o, dx, xs, ys, zs, nu_min, nu_max = geometry(n, box, nside, zmin, zmax, n_nu)
     zt = np.ctypeslib.as_array(o.d.z_r2z).copy()
     gi = o.d.glob_idr
@@ -80,7 +83,7 @@ def test_shell_line_bound(n, box, nside, zmin, zmax, n_nu):
     rho = f32(rho_d * (1 + 1e-5) + 1e-6)
     idr_cell = f32(gi * dx)
     inv_dnu = n_nu / (nu_max - nu_min)
-    sc, off = f32(inv_dnu), f32(nu_min)
+    sc, off = (f32(inv_dnu), f32(nu_min)) if regular else (f32(1), f32(0))
     ncell = 60000
     ix, iy, iz = (rng.integers(0, n, ncell) for _ in range(3))
     dzc = r32(rng.normal(0, 1.5e-3, ncell))
@@ -97,9 +100,9 @@ def test_shell_line_bound(n, box, nside, zmin, zmax, n_nu):
     zz = r32(1 + r32(fma(dzt, r32(trs - ir), z0) + dzc))
     izz = r32(1 / np.float64(zz) * (1 + rng.uniform(-1.2e-7, 1.2e-7, ncell)))
     nu = r32(f32(NU21) * izz)
-    u = r32(r32(nu - off) * sc)
+    u = r32(r32(nu - off) * sc) if regular else nu
     mnu = r32(2 * nu * r32(np.abs(dzt) * trs * f32(1.8e-7) * izz + f32(4.8e-7) + f32(2.7e-7)))
-    mc = r32(r32(mnu + f32(1.2e-7) * nu) * sc + f32(4e-7) * np.abs(u) + f32(1e-6))
+    mc = r32(r32(mnu + f32(1.2e-7) * nu) * sc + f32(4e-7) * np.abs(u) + f32(1e-6)) if regular else mnu
     gg, e = gf[ir], E[ir]
     d1 = r32(f32(NU21) * sc * izz * izz)
     s = r32(-d1 * gg)
@@ -129,7 +132,8 @@ def test_shell_line_bound(n, box, nside, zmin, zmax, n_nu):
         r = np.sqrt(px * px + py * py + pz * pz) * dx  # Mpc/h
         k = (r * gi).astype(np.int64)
         ze = zt[k] + (zt[k + 1] - zt[k]) * (r - rt[k]) * gi
-        te = inv_dnu * (NU21 / (1 + (ze + dzc.astype(np.float64))) - nu_min)
+        nue = NU21 / (1 + (ze + dzc.astype(np.float64)))
+        te = inv_dnu * (nue - nu_min) if regular else nue
         worst_old = max(worst_old, np.max(np.abs(u_old[ok] - te[ok]) / m_old[ok]))
         worst_lin = max(worst_lin, np.max(np.abs(u_lin[ok] - te[ok]) / m_lin[ok]))
     assert ok.mean() > 0.99
