@@ -353,7 +353,8 @@ __device__ __forceinline__ int edge_search(const float *ef, int nn, int log2nn, 
 // t = (nu - nu_min)/dnu of a regular table, the frequency nu itself for a
 // frequency file) is set once per cell as
 //     u(R) = u_c + s (R - Rc),   |u(R) - u_exact(R)| < m,
-// and each sub-sample spends one subtraction and one FMA on it.  u_exact is the
+// and each sub-sample spends one subtraction and one FMA on it (key_fast), or
+// three FMAs on its offset o with R - Rc = r_hat.o (key_lin, bound ml).  u_exact is the
 // FP64 key's value: u of 1 + z(R) + dz, z the piecewise-linear FP64 table
 // (src/cosmo.c:52-62).  s = du/dz g, with g the slope of the table interval
 // the centre falls in; z(R) stays within e of that interval's line for every R
@@ -366,7 +367,7 @@ __device__ __forceinline__ int edge_search(const float *ef, int nn, int log2nn, 
 //   the FP32 slope and the products forming s: 2e-6 |s| rho;
 //   curvature of u in z: |d2u/dz2| dZ^2/2 <= A sc dZ^2 / (1 + z + dz - dZ)^3,
 //     dZ = |g| rho + e the largest change of z over the cell;
-//   rounding of the FMA: 1.2e-7 (|u_c| + |s| rho).
+//   rounding of the FMAs: 2e-7 (|u_c| + |s| rho) (up to three).
 // Cells closer than 2 rho + 2 cells to the observer, or reaching the last table
 // interval, get m = inf: their sub-samples all go to the exact path.
 //
